@@ -1,0 +1,447 @@
+"""Host-side mirror of the reference's stage objects over the C ABI.
+
+The reference's scene code (source/pool.cpp) owns lists and stage objects and
+calls, once per frame:
+
+    mVelocityHandling.apply(dt); mParticleTransfer.apply(dt);
+    mNeighborhoodFluid.set_range_scale(s).apply(); mSpreadKernelWidth.apply();
+    for i < solverIterations: mBoxCollision.apply(); mIncompressibility.apply();
+    mUpdateTransfers.apply();
+
+This module offers the same objects with the same method names
+(set_data / set_range_scale / set_position_range / apply), backed by one
+apbf_ctx that owns the device lists (the reference's gpu_list / indexed_list
+buffers).  Device memory is handed out as torch tensors that alias the
+context's buffers (valid until the next call that edits the lists, like
+gpu_list::buffer()).  torch is used only for device memory and streams.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _native as N
+
+_TYPESTR = {torch.int32: "<i4", torch.float32: "<f4", torch.int64: "<i8", torch.uint8: "|u1"}
+
+
+class _CudaArray:
+    def __init__(self, ptr: int, shape: tuple, typestr: str):
+        self.__cuda_array_interface__ = {
+            "shape": shape,
+            "typestr": typestr,
+            "data": (int(ptr), False),
+            "version": 2,
+            "strides": None,
+        }
+
+
+def device_tensor(ptr: int, shape: tuple, dtype: torch.dtype, device: int = 0) -> torch.Tensor:
+    """A torch tensor aliasing device memory owned by the context (no copy)."""
+    if not ptr:
+        raise ValueError("null device pointer")
+    return torch.as_tensor(_CudaArray(ptr, tuple(shape), _TYPESTR[dtype]), device=f"cuda:{device}")
+
+
+def _stream_handle(stream) -> C.c_void_p:
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return C.c_void_p(stream.cuda_stream)
+
+
+def default_settings() -> N.Settings:
+    s = N.Settings()
+    N.load().apbf_default_settings(C.byref(s))
+    return s
+
+
+FLUID_FIELDS = {
+    # name: (dtype, components)
+    "position": (torch.int32, 4),
+    "velocity": (torch.float32, 4),
+    "inverse_mass": (torch.float32, 1),
+    "radius": (torch.float32, 1),
+    "pos_backup": (torch.int32, 4),
+    "transferring": (torch.int32, 1),
+    "target_radius": (torch.float32, 1),
+    "kernel_width": (torch.float32, 1),
+    "boundariness": (torch.float32, 1),
+    "boundary_distance": (torch.int32, 1),
+}
+
+
+class Context:
+    """One apbf_ctx: the device lists of one scene plus the solver's scratch memory."""
+
+    def __init__(self, particle_capacity: int, max_neighbors: int = 96, transfer_capacity: int = N.MAX_TRANSFERS,
+                 max_log2res: int = 7, device: int = 0):
+        self.lib = N.load()
+        self.device = device
+        torch.cuda.init()
+        cfg = N.Config(particle_capacity, max_neighbors, transfer_capacity, max_log2res, device)
+        h = C.c_void_p()
+        N.check(self.lib.apbf_create(C.byref(cfg), C.byref(h)), "apbf_create")
+        self.handle = h
+        self.capacity = particle_capacity
+        self.max_neighbors = max_neighbors
+        self.transfer_capacity = transfer_capacity
+        self.settings = default_settings()
+
+    # ---- lifetime ----
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            torch.cuda.synchronize(self.device)
+            self.lib.apbf_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- configuration ----
+    def set_settings(self, settings: N.Settings | None = None, **kw) -> "Context":
+        s = settings if settings is not None else self.settings
+        for k, v in kw.items():
+            if not hasattr(s, k):
+                raise AttributeError(k)
+            setattr(s, k, v)
+        N.check(self.lib.apbf_set_settings(self.handle, C.byref(s)), "apbf_set_settings")
+        self.settings = s
+        return self
+
+    def set_scene(self, min_pos, max_pos, log2res: int, acceleration=(0.0, 0.0, 0.0)) -> "Context":
+        sc = N.Scene(N.f3(min_pos), N.f3(max_pos), log2res, N.f3(acceleration))
+        N.check(self.lib.apbf_set_scene(self.handle, C.byref(sc)), "apbf_set_scene")
+        self.scene = (tuple(min_pos), tuple(max_pos), log2res, tuple(acceleration))
+        return self
+
+    def set_boxes(self, box_min: np.ndarray, box_max: np.ndarray) -> "Context":
+        bmin = np.ascontiguousarray(box_min, dtype=np.float32).reshape(-1, 4)
+        bmax = np.ascontiguousarray(box_max, dtype=np.float32).reshape(-1, 4)
+        n = bmin.shape[0]
+        N.check(self.lib.apbf_set_boxes(self.handle, bmin.ctypes.data_as(N._F3), bmax.ctypes.data_as(N._F3), n),
+                "apbf_set_boxes")
+        return self
+
+    def set_debug(self, enable: bool) -> None:
+        N.check(self.lib.apbf_set_debug(self.handle, 1 if enable else 0), "apbf_set_debug")
+
+    # ---- lists ----
+    def fluid_view(self) -> dict:
+        v = N.FluidView()
+        N.check(self.lib.apbf_fluid_get_view(self.handle, C.byref(v)), "apbf_fluid_get_view")
+        out = {}
+        for name, (dt, comp) in FLUID_FIELDS.items():
+            shape = (v.capacity, comp) if comp > 1 else (v.capacity,)
+            out[name] = device_tensor(getattr(v, name), shape, dt, self.device)
+        out["length"] = device_tensor(v.d_length, (1,), torch.int32, self.device)
+        return out
+
+    def transfers_view(self) -> dict:
+        v = N.TransfersView()
+        N.check(self.lib.apbf_transfers_get_view(self.handle, C.byref(v)), "apbf_transfers_get_view")
+        return {
+            "source": device_tensor(v.source, (v.capacity,), torch.int32, self.device),
+            "target": device_tensor(v.target, (v.capacity,), torch.int32, self.device),
+            "time_left": device_tensor(v.time_left, (v.capacity,), torch.float32, self.device),
+            "length": device_tensor(v.d_length, (1,), torch.int32, self.device),
+        }
+
+    def neighbors_view(self) -> dict:
+        v = N.NeighborsView()
+        N.check(self.lib.apbf_neighbors_get_view(self.handle, C.byref(v)), "apbf_neighbors_get_view")
+        return {
+            "count": device_tensor(v.count, (self.capacity,), torch.int32, self.device),
+            "index": device_tensor(v.index, (v.max_per_row, v.row_stride), torch.int32, self.device),
+            "row_stride": v.row_stride,
+        }
+
+    def set_lengths(self, n_particles: int, n_transfers: int = 0, stream=None) -> None:
+        N.check(self.lib.apbf_set_lengths(self.handle, n_particles, n_transfers, _stream_handle(stream)),
+                "apbf_set_lengths")
+
+    def lengths(self, stream=None) -> tuple[int, int]:
+        a, b = C.c_uint32(), C.c_uint32()
+        N.check(self.lib.apbf_get_lengths(self.handle, C.byref(a), C.byref(b), _stream_handle(stream)),
+                "apbf_get_lengths")
+        return a.value, b.value
+
+    def upload(self, state: dict, transfers: dict | None = None, stream=None) -> None:
+        """Copies a host scene state (numpy arrays, see scenes.py) into the lists."""
+        n = int(state["position"].shape[0])
+        if n > self.capacity:
+            raise ValueError(f"{n} particles exceed the capacity {self.capacity}")
+        v = self.fluid_view()
+        for name, (dt, comp) in FLUID_FIELDS.items():
+            if name not in state:
+                continue
+            src = torch.from_numpy(np.ascontiguousarray(state[name]).view(
+                np.int32 if dt == torch.int32 else np.float32))
+            v[name][:n].copy_(src.reshape(v[name][:n].shape), non_blocking=False)
+        nt = 0
+        if transfers is not None:
+            nt = int(transfers["source"].shape[0])
+            tv = self.transfers_view()
+            for k in ("source", "target"):
+                tv[k][:nt].copy_(torch.from_numpy(np.ascontiguousarray(transfers[k]).view(np.int32)))
+            tv["time_left"][:nt].copy_(torch.from_numpy(np.ascontiguousarray(transfers["time_left"], np.float32)))
+        torch.cuda.synchronize(self.device)
+        self.set_lengths(n, nt, stream)
+
+    def download(self, stream=None) -> tuple[dict, dict]:
+        """Host copy of the current lists (numpy), lengths applied."""
+        n, nt = self.lengths(stream)
+        v = self.fluid_view()
+        out = {}
+        for name, (dt, comp) in FLUID_FIELDS.items():
+            a = v[name][:n].cpu().numpy()
+            if name in ("transferring", "boundary_distance"):
+                a = a.view(np.uint32)
+            out[name] = a.copy()
+        tv = self.transfers_view()
+        tr = {
+            "source": tv["source"][:nt].cpu().numpy().view(np.uint32).copy(),
+            "target": tv["target"][:nt].cpu().numpy().view(np.uint32).copy(),
+            "time_left": tv["time_left"][:nt].cpu().numpy().copy(),
+        }
+        return out, tr
+
+    def download_rows(self, stream=None) -> list[np.ndarray]:
+        """Neighbour rows of the last search as sorted numpy arrays (test helper)."""
+        n, _ = self.lengths(stream)
+        nb = self.neighbors_view()
+        cnt = nb["count"][:n].cpu().numpy()
+        idx = nb["index"][:, :n].cpu().numpy()
+        return [np.sort(idx[: cnt[i], i].astype(np.int64)) for i in range(n)]
+
+    # ---- results ----
+    def status(self, clear: bool = True, stream=None) -> N.StatusInfo:
+        info = N.StatusInfo()
+        self.last_status_code = self.lib.apbf_get_status(self.handle, C.byref(info), 1 if clear else 0,
+                                                         _stream_handle(stream))
+        return info
+
+    def check_status(self, stream=None) -> N.StatusInfo:
+        info = N.StatusInfo()
+        code = self.lib.apbf_get_status(self.handle, C.byref(info), 1, _stream_handle(stream))
+        N.check(code, f"device status (flags=0x{info.flags:x}, required_neighbors={info.required_neighbors})")
+        return info
+
+    def reduce_fp64(self, stream=None) -> np.ndarray:
+        out = (C.c_double * 4)()
+        N.check(self.lib.apbf_reduce_fp64(self.handle, out, _stream_handle(stream)), "apbf_reduce_fp64")
+        return np.array(list(out))
+
+    def profile_enable(self, enable: bool = True, capacity: int = 65536) -> None:
+        N.check(self.lib.apbf_profile_enable(self.handle, 1 if enable else 0, capacity), "apbf_profile_enable")
+
+    def profile_read(self, stream=None) -> tuple[dict, int]:
+        """{kernel name: (launches, total ms)} of the launches since the last read."""
+        cap = 64
+        arr = (N.KernelTime * cap)()
+        n = C.c_uint32()
+        dropped = C.c_ulonglong()
+        N.check(self.lib.apbf_profile_read(self.handle, arr, cap, C.byref(n), C.byref(dropped),
+                                           _stream_handle(stream)), "apbf_profile_read")
+        return {arr[i].name.decode(): (arr[i].launches, arr[i].total_ms) for i in range(n.value)}, dropped.value
+
+    def launch_count(self) -> int:
+        v = C.c_ulonglong()
+        N.check(self.lib.apbf_launch_count(self.handle, C.byref(v)), "apbf_launch_count")
+        return v.value
+
+    def substep(self, dt: float, stream=None) -> None:
+        N.check(self.lib.apbf_substep(self.handle, C.c_float(dt), _stream_handle(stream)), "apbf_substep")
+
+    def debug_incompressibility(self, stream=None) -> dict:
+        n, _ = self.lengths(stream)
+        d = torch.empty(self.capacity, dtype=torch.int32, device=f"cuda:{self.device}")
+        g = torch.empty((self.capacity, 4), dtype=torch.int32, device=f"cuda:{self.device}")
+        q = torch.empty(self.capacity, dtype=torch.int32, device=f"cuda:{self.device}")
+        lam = torch.empty(self.capacity, dtype=torch.float32, device=f"cuda:{self.device}")
+        N.check(self.lib.apbf_debug_incompressibility(self.handle, C.c_void_p(d.data_ptr()), C.c_void_p(g.data_ptr()),
+                                                      C.c_void_p(q.data_ptr()), C.c_void_p(lam.data_ptr()),
+                                                      _stream_handle(stream)), "apbf_debug_incompressibility")
+        torch.cuda.synchronize(self.device)
+        return {
+            "density": d[:n].cpu().numpy().view(np.uint32),
+            "grad_sum": g[:n, :3].cpu().numpy(),
+            "sq_grad_sum": q[:n].cpu().numpy().view(np.uint32),
+            "lambda": lam[:n].cpu().numpy(),
+        }
+
+    def debug_sort(self, stream=None) -> tuple[np.ndarray, np.ndarray]:
+        n, _ = self.lengths(stream)
+        p = torch.empty(self.capacity, dtype=torch.int32, device=f"cuda:{self.device}")
+        k = torch.empty(self.capacity, dtype=torch.int32, device=f"cuda:{self.device}")
+        N.check(self.lib.apbf_debug_sort(self.handle, C.c_void_p(p.data_ptr()), C.c_void_p(k.data_ptr()),
+                                         _stream_handle(stream)), "apbf_debug_sort")
+        torch.cuda.synchronize(self.device)
+        return p[:n].cpu().numpy().view(np.uint32), k[:n].cpu().numpy().view(np.uint32)
+
+    def export_pairs(self, capacity: int, stream=None) -> np.ndarray:
+        pairs = torch.empty((capacity, 2), dtype=torch.int32, device=f"cuda:{self.device}")
+        ln = torch.zeros(1, dtype=torch.int32, device=f"cuda:{self.device}")
+        N.check(self.lib.apbf_export_pairs(self.handle, C.c_void_p(pairs.data_ptr()), capacity,
+                                           C.c_void_p(ln.data_ptr()), _stream_handle(stream)), "apbf_export_pairs")
+        torch.cuda.synchronize(self.device)
+        m = min(int(ln.item()), capacity)
+        return pairs[:m].cpu().numpy().view(np.uint32)
+
+
+# ---------------------------------------------------------------------------
+# Stage objects with the reference's method names.
+# ---------------------------------------------------------------------------
+
+
+class velocity_handling:
+    """pbd::velocity_handling (source/velocity_handling.h, velocity_handling.cpp:15-31)."""
+
+    def set_data(self, ctx: Context) -> "velocity_handling":
+        self.ctx = ctx
+        return self
+
+    def set_acceleration(self, a) -> "velocity_handling":
+        self.acc = N.f3(a)
+        return self
+
+    def apply(self, dt: float, stream=None) -> None:
+        N.check(self.ctx.lib.apbf_velocity_handling_apply(self.ctx.handle, C.c_float(dt), self.acc,
+                                                          _stream_handle(stream)), "velocity_handling.apply")
+
+
+class neighborhood_green:
+    """pbd::neighborhood_green (source/neighborhood_green.h:8-23)."""
+
+    def __init__(self):
+        self.range_scale = 1.0
+
+    def set_data(self, ctx: Context) -> "neighborhood_green":
+        self.ctx = ctx
+        return self
+
+    def set_range_scale(self, scale: float) -> "neighborhood_green":
+        self.range_scale = float(scale)
+        return self
+
+    def set_position_range(self, min_pos, max_pos, resolution_log2: int) -> "neighborhood_green":
+        self.min_pos, self.max_pos, self.log2res = N.f3(min_pos), N.f3(max_pos), int(resolution_log2)
+        return self
+
+    def apply(self, stream=None) -> None:
+        N.check(self.ctx.lib.apbf_neighborhood_green_apply(self.ctx.handle, C.c_float(self.range_scale), self.min_pos,
+                                                           self.max_pos, self.log2res, _stream_handle(stream)),
+                "neighborhood_green.apply")
+
+
+class box_collision:
+    """pbd::box_collision (source/box_collision.h, box_collision.cpp:12-24)."""
+
+    def set_data(self, ctx: Context, box_min=None, box_max=None) -> "box_collision":
+        self.ctx = ctx
+        if box_min is not None:
+            ctx.set_boxes(box_min, box_max)
+        return self
+
+    def apply(self, stream=None) -> None:
+        N.check(self.ctx.lib.apbf_box_collision_apply(self.ctx.handle, _stream_handle(stream)), "box_collision.apply")
+
+
+class incompressibility:
+    """pbd::incompressibility (source/incompressibility.h:7-17)."""
+
+    def set_data(self, ctx: Context) -> "incompressibility":
+        self.ctx = ctx
+        return self
+
+    def apply(self, stream=None) -> None:
+        N.check(self.ctx.lib.apbf_incompressibility_apply(self.ctx.handle, _stream_handle(stream)),
+                "incompressibility.apply")
+
+
+class spread_kernel_width:
+    """pbd::spread_kernel_width (source/spread_kernel_width.h, spread_kernel_width.cpp:12-26)."""
+
+    def set_data(self, ctx: Context) -> "spread_kernel_width":
+        self.ctx = ctx
+        return self
+
+    def apply(self, stream=None) -> None:
+        N.check(self.ctx.lib.apbf_spread_kernel_width_apply(self.ctx.handle, _stream_handle(stream)),
+                "spread_kernel_width.apply")
+
+
+class kernel_width_from_boundary_distance:
+    """shader_provider::uint_to_float_with_indexed_lower_bound as called at source/pool.cpp:77-80."""
+
+    def set_data(self, ctx: Context) -> "kernel_width_from_boundary_distance":
+        self.ctx = ctx
+        return self
+
+    def apply(self, stream=None) -> None:
+        N.check(self.ctx.lib.apbf_kernel_width_from_boundary_distance_apply(self.ctx.handle, _stream_handle(stream)),
+                "kernel_width_from_boundary_distance.apply")
+
+
+class update_transfers:
+    """pbd::update_transfers (source/update_transfers.h, update_transfers.cpp:14-71)."""
+
+    def set_data(self, ctx: Context) -> "update_transfers":
+        self.ctx = ctx
+        return self
+
+    def apply(self, stream=None) -> None:
+        N.check(self.ctx.lib.apbf_update_transfers_apply(self.ctx.handle, _stream_handle(stream)),
+                "update_transfers.apply")
+
+
+class particle_transfer:
+    """pbd::particle_transfer (source/particle_transfer.h, particle_transfer.cpp:10-28)."""
+
+    def set_data(self, ctx: Context) -> "particle_transfer":
+        self.ctx = ctx
+        return self
+
+    def apply(self, dt: float, stream=None) -> None:
+        N.check(self.ctx.lib.apbf_particle_transfer_apply(self.ctx.handle, C.c_float(dt), _stream_handle(stream)),
+                "particle_transfer.apply")
+
+
+class algorithms:
+    """pbd::algorithms (source/algorithms.h:12-17) on device tensors."""
+
+    @staticmethod
+    def sort(ctx: Context, keys: torch.Tensor, values: torch.Tensor, count: torch.Tensor, max_count: int,
+             out_keys: torch.Tensor, out_values: torch.Tensor, value_upper_bound: int = 0xFFFFFFFF,
+             stream=None) -> None:
+        N.check(ctx.lib.apbf_sort_pairs(ctx.handle, C.c_void_p(keys.data_ptr()), C.c_void_p(values.data_ptr()),
+                                        C.c_void_p(count.data_ptr()), max_count, value_upper_bound,
+                                        C.c_void_p(out_keys.data_ptr()), C.c_void_p(out_values.data_ptr()),
+                                        _stream_handle(stream)), "algorithms.sort")
+
+    @staticmethod
+    def prefix_sum(ctx: Context, values: torch.Tensor, count: torch.Tensor, max_count: int, stream=None) -> None:
+        N.check(ctx.lib.apbf_prefix_sum(ctx.handle, C.c_void_p(values.data_ptr()), C.c_void_p(count.data_ptr()),
+                                        max_count, _stream_handle(stream)), "algorithms.prefix_sum")
+
+
+@dataclass
+class SubstepStages:
+    """The stage objects of one scene, wired as pool::pool wires them (source/pool.cpp:27-46)."""
+
+    ctx: Context
+
+    def __post_init__(self):
+        self.velocity = velocity_handling().set_data(self.ctx)
+        self.neighborhood = neighborhood_green().set_data(self.ctx)
+        self.boxes = box_collision().set_data(self.ctx)
+        self.incompressibility = incompressibility().set_data(self.ctx)
+        self.spread = spread_kernel_width().set_data(self.ctx)
+        self.kw_bd = kernel_width_from_boundary_distance().set_data(self.ctx)
+        self.update_transfers = update_transfers().set_data(self.ctx)
+        self.particle_transfer = particle_transfer().set_data(self.ctx)

@@ -1,0 +1,373 @@
+// apbf_internal.cuh -- context layout and device helpers shared by the CUDA sources.
+//
+// Data layout in HBM (structure of arrays, one entry per particle, particle order
+// = Morton cell order after every neighbourhood search):
+//   position / pos_backup  int4   (x, y, z, pad) in 2^18 fixed point
+//   velocity               float4
+//   inverse_mass, radius, target_radius, kernel_width, boundariness   float
+//   transferring, boundary_distance                                   uint32
+// Two complete attribute sets exist (cur / alt); a reorder gathers cur -> alt and
+// swaps, the Jacobi position update ping-pongs the position buffers.
+// Neighbour rows are column-major: index[k * row_stride + i] (k < count[i]), so a
+// warp of consecutive particles reads one 128-byte line per k.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/apbf_gb300.h"
+
+#define APBF_FIX 262144.0f
+#define APBF_INV_FIX (1.0f / 262144.0f)
+
+namespace apbf {
+
+constexpr int kBlock = 256;
+constexpr uint32_t kSpinLimit = 1u << 22;  // bounded device-side waits
+
+struct FluidBufs {
+    int4 *pos;
+    float4 *vel;
+    float *inv_mass;
+    float *radius;
+    int4 *pos_backup;
+    uint32_t *transferring;
+    float *target_radius;
+    float *kernel_width;
+    float *boundariness;
+    uint32_t *boundary_distance;
+};
+
+struct TransferBufs {
+    uint32_t *source;
+    uint32_t *target;
+    float *time_left;
+};
+
+// Device status block (one allocation, zeroed by apbf_get_status(clear=1)).
+struct Status {
+    uint32_t flags;
+    uint32_t required_neighbors;
+    uint32_t required_transfers;
+    uint32_t required_particles;
+    unsigned long long range_min;  // smallest fixed-point search radius of the last search
+    unsigned long long range_max;
+    uint32_t symmetric;            // 1 if every search radius was equal (rows are symmetric)
+    uint32_t spin_where;
+    uint32_t pad[2];
+};
+
+// Device length block.
+enum LenSlot : uint32_t {
+    kLenParticles = 0,
+    kLenTransfers = 1,
+    kLenSplits = 2,
+    kLenDelParticles = 3,
+    kLenDelTransfers = 4,
+    kLenMerges = 5,
+    kLenScratch = 6,
+    kLenSlots = 16
+};
+
+// Per-particle Gauss-kernel constants computed once per density pass and reused
+// by the position-update pass (so both evaluate bit-identical gradients).
+struct KConst {
+    float ivd;   // invDoubleVariance (kernels.glsl:87)
+    float norm;  // pow(invDoubleVarianceWithoutPi, D/2) (kernels.glsl:88)
+};
+
+struct Ctx;
+
+// Sort scratch sizes.
+constexpr int kSortItems = 16;
+constexpr int kSortWarps = 8;
+constexpr int kSortTile = kSortItems * 32 * kSortWarps;  // 4096 keys per tile
+
+}  // namespace apbf
+
+namespace apbf {
+// One timed kernel launch: CUDA events recorded on the launching stream.
+struct ProfSlot {
+    const char *name;
+    cudaEvent_t a, b;
+};
+}  // namespace apbf
+
+struct apbf_ctx {
+    apbf_config cfg;
+    apbf_settings settings;
+    apbf_scene scene;
+    int device = 0;
+    int num_sms = 152;
+    float last_dt = 1.0f;  // velocity_handling.h:17
+    uint32_t row_stride = 0;
+
+    apbf::FluidBufs fl[2];
+    apbf::TransferBufs tr[2];
+    int fcur = 0;
+    int tcur = 0;
+    uint32_t *d_len = nullptr;
+
+    uint32_t *nb_count = nullptr;
+    uint32_t *nb_idx = nullptr;
+    uint32_t *rev_count = nullptr;
+    uint32_t *rev_idx = nullptr;
+    unsigned long long *d_pairs = nullptr;
+
+    uint32_t *keys[2] = {nullptr, nullptr};
+    uint32_t *vals[2] = {nullptr, nullptr};
+    uint32_t *sort_hist = nullptr;         // 4 passes x 256
+    uint32_t *sort_status = nullptr;       // tiles x 256
+    uint32_t *sort_counters = nullptr;     // tile counters per pass
+    uint32_t sort_tiles = 0;
+    uint32_t *sorted_keys = nullptr;       // result of the last neighbourhood sort
+    uint32_t *perm = nullptr;              // new id -> old id of the last reorder
+    uint32_t *inv_perm = nullptr;
+    uint32_t *cell_start = nullptr;
+    uint32_t *cell_end = nullptr;
+
+    float *lambda = nullptr;
+    int4 *shift = nullptr;
+    apbf::KConst *kconst = nullptr;
+    uint32_t *dbg_density = nullptr;
+    int4 *dbg_grad = nullptr;
+    uint32_t *dbg_sq = nullptr;
+
+    // adaptive scratch
+    uint32_t *ukw = nullptr;
+    uint32_t *min_nd = nullptr;
+    uint32_t *nearest = nullptr;
+    uint32_t *old_bd = nullptr;
+    uint32_t *proposal = nullptr;  // per particle: packed proposal kind
+    uint32_t *claim = nullptr;     // per particle: min claimant
+    uint32_t *decided = nullptr;
+    uint32_t *flag_scan = nullptr;
+    uint32_t *list_a = nullptr;
+    uint32_t *list_b = nullptr;
+    uint32_t *scan_tmp = nullptr;
+
+    double *red_partials = nullptr;
+    double *red_out = nullptr;
+    int red_blocks = 0;
+
+    float4 *box_min = nullptr;
+    float4 *box_max = nullptr;
+    uint32_t n_boxes = 0;
+
+    apbf::Status *status = nullptr;
+    uint32_t n_cells_log2_alloc = 0;
+    int debug = 0;
+    std::vector<void *> owned;  // every device allocation, freed by apbf_destroy
+
+    // tracing: per-launch events when enabled, launch counter always
+    bool prof_on = false;
+    std::vector<apbf::ProfSlot> prof;
+    size_t prof_used = 0;
+    unsigned long long prof_dropped = 0;
+    unsigned long long launches = 0;
+    apbf::ProfSlot *prof_open = nullptr;
+};
+
+namespace apbf {
+
+void set_error(const std::string &msg);
+apbf_status cuda_check(cudaError_t e, const char *what);
+#define APBF_CUDA(call)                                              \
+    do {                                                             \
+        cudaError_t _e = (call);                                     \
+        if (_e != cudaSuccess) return apbf::cuda_check(_e, #call);   \
+    } while (0)
+#define APBF_LAUNCH_CHECK(what)                                      \
+    do {                                                             \
+        cudaError_t _e = cudaGetLastError();                         \
+        if (_e != cudaSuccess) return apbf::cuda_check(_e, what);    \
+    } while (0)
+
+// Kernel-launch bookkeeping: every launch is counted; when tracing is on, a
+// pair of events is recorded around it on the launching stream.
+inline void before_launch(apbf_ctx *c, cudaStream_t s, const char *name) {
+    ++c->launches;
+    c->prof_open = nullptr;
+    if (!c->prof_on) return;
+    if (c->prof_used >= c->prof.size()) {
+        ++c->prof_dropped;
+        return;
+    }
+    ProfSlot *slot = &c->prof[c->prof_used++];
+    slot->name = name;
+    cudaEventRecord(slot->a, s);
+    c->prof_open = slot;
+}
+inline void after_launch(apbf_ctx *c, cudaStream_t s) {
+    if (c->prof_open) cudaEventRecord(c->prof_open->b, s);
+    c->prof_open = nullptr;
+}
+#define APBF_BEFORE_LAUNCH(ctx, stream, name) apbf::before_launch((ctx), (stream), (name))
+#define APBF_AFTER_LAUNCH(ctx, stream, what)                         \
+    do {                                                             \
+        apbf::after_launch((ctx), (stream));                         \
+        cudaError_t _e = cudaGetLastError();                         \
+        if (_e != cudaSuccess) return apbf::cuda_check(_e, what);    \
+    } while (0)
+
+inline int grid_for(const apbf_ctx *ctx, uint32_t n, int block = kBlock, int per_sm = 8) {
+    uint64_t need = ((uint64_t)n + block - 1) / block;
+    uint64_t cap = (uint64_t)ctx->num_sms * per_sm;
+    if (need < 1) need = 1;
+    return (int)(need < cap ? need : cap);
+}
+
+// ---- host-side stage launchers (defined in the .cu files) ----
+apbf_status sort_pairs_device(apbf_ctx *ctx, const uint32_t *keys_in, const uint32_t *vals_in, const uint32_t *d_count,
+                              uint32_t max_count, uint32_t key_bits, uint32_t *keys_out, uint32_t *vals_out,
+                              cudaStream_t s);
+apbf_status prefix_sum_device(apbf_ctx *ctx, uint32_t *d_values, const uint32_t *d_count, uint32_t max_count,
+                              cudaStream_t s);
+apbf_status neighborhood_green(apbf_ctx *ctx, float range_scale, const float minp[3], const float maxp[3],
+                               uint32_t log2res, cudaStream_t s);
+apbf_status velocity_handling(apbf_ctx *ctx, float dt, const float accel[3], cudaStream_t s);
+apbf_status box_collision(apbf_ctx *ctx, cudaStream_t s);
+apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s);
+apbf_status kw_from_boundary_distance(apbf_ctx *ctx, cudaStream_t s);
+apbf_status spread_kernel_width(apbf_ctx *ctx, cudaStream_t s);
+apbf_status update_transfers(apbf_ctx *ctx, cudaStream_t s);
+apbf_status particle_transfer(apbf_ctx *ctx, float dt, cudaStream_t s);
+apbf_status reduce_fp64(apbf_ctx *ctx, double out[4], cudaStream_t s);
+apbf_status export_pairs(apbf_ctx *ctx, uint32_t *d_pairs, uint32_t cap, uint32_t *d_length, cudaStream_t s);
+apbf_status build_reverse_rows(apbf_ctx *ctx, cudaStream_t s);
+
+// ---- device helpers ----
+#ifdef __CUDACC__
+
+// GLSL int()/uint(): truncate toward zero, saturate, NaN -> 0 (cvt.rzi.sat semantics).
+__device__ __forceinline__ int32_t f2i(float x) { return __float2int_rz(x); }
+__device__ __forceinline__ uint32_t f2u(float x) { return __float2uint_rz(x); }
+__device__ __forceinline__ int32_t wadd(int32_t a, int32_t b) { return (int32_t)((uint32_t)a + (uint32_t)b); }
+
+__device__ __forceinline__ void set_flag(Status *st, uint32_t f) { atomicOr(&st->flags, f); }
+
+// Bits of a 10-bit value spread to every third bit (Morton interleave).
+__device__ __host__ __forceinline__ uint32_t spread3(uint32_t x) {
+    x &= 0x3ffu;
+    x = (x | (x << 16)) & 0x030000FFu;
+    x = (x | (x << 8)) & 0x0300F00Fu;
+    x = (x | (x << 4)) & 0x030C30C3u;
+    x = (x | (x << 2)) & 0x09249249u;
+    return x;
+}
+// calculate_position_hash.comp:29-36: bit i of axis d -> bit 3i + d.
+__device__ __host__ __forceinline__ uint32_t morton3(uint32_t cx, uint32_t cy, uint32_t cz) {
+    return spread3(cx) | (spread3(cy) << 1) | (spread3(cz) << 2);
+}
+
+// Canonical cell of a fixed-point coordinate: clamp(floor((x - lo) * 2^L / (hi - lo))).
+__device__ __forceinline__ uint32_t cell_coord(long long x, long long lo, long long hi, uint32_t L) {
+    const long long cells = 1ll << L;
+    if (x <= lo) return 0u;
+    if (x >= hi) return (uint32_t)(cells - 1);
+    long long c = ((x - lo) << L) / (hi - lo);
+    return (uint32_t)(c > cells - 1 ? cells - 1 : c);
+}
+
+// Fixed-point difference as reference units: vec3(posN - pos) / POS_RESOLUTION.
+__device__ __forceinline__ float3 fdiff(int4 from, int4 to) {
+    return make_float3((float)wadd(to.x, -from.x) * APBF_INV_FIX, (float)wadd(to.y, -from.y) * APBF_INV_FIX,
+                       (float)wadd(to.z, -from.z) * APBF_INV_FIX);
+}
+
+__device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+
+constexpr float kPiF = 3.14159265f;  // kernels.glsl:1
+
+// Gauss constants of a kernel width (kernels.glsl:84-89, 104).
+__device__ __forceinline__ KConst gauss_consts(float kw) {
+    KConst c;
+    float half = kw / 2.0f;
+    float height = 0.6f / (half * half * half);
+    float ivw = powf(height, 2.0f / 3.0f);
+    c.ivd = ivw * kPiF;
+    c.norm = powf(ivw, 1.5f);
+    return c;
+}
+
+__device__ __forceinline__ float gauss_height(float r2, KConst c) { return expf(-r2 * c.ivd) * c.norm; }
+
+// kernel_height (kernels.glsl:99-110).  r2 = dot(r, r).
+__device__ __forceinline__ float kernel_height(int kid, float r2, float h, KConst c) {
+    switch (kid) {
+    case 1: return gauss_height(r2, c);
+    case 0: {
+        float dist = sqrtf(r2);
+        if (dist > h) return 0.0f;
+        float q = dist / h, k = 8.0f / (kPiF * h * h * h);
+        if (q <= 0.5f) { float q2 = q * q; return k * (6.0f * q * q2 - 6.0f * q2 + 1.0f); }
+        float m = 1.0f - q;
+        return k * (2.0f * m * m * m);
+    }
+    case 2: {
+        float h2 = h * h;
+        if (r2 > h2) return 0.0f;
+        float d = h2 - r2, h3 = h * h * h;
+        return 315.0f * (d * d * d) / (64.0f * kPiF * (h3 * h3 * h3));
+    }
+    case 3: {
+        float height = 3.0f / (kPiF * h * h * h);
+        return fmaxf(0.0f, (1.0f - sqrtf(r2) / h) * height);
+    }
+    case 4: {
+        float dist = sqrtf(r2);
+        float a = 15.0f / (2.0f * kPiF * (h * h * h * h * h));
+        if (dist >= h) return 0.0f;
+        return a * (h - dist) * (h - dist);
+    }
+    default: return 0.0f;
+    }
+}
+
+// kernel_gradient (kernels.glsl:112-123).  For Gauss, Wg is the Gauss height at r.
+__device__ __forceinline__ float3 kernel_gradient(int kid, float3 r, float r2, float h, KConst c, float Wg) {
+    switch (kid) {
+    case 1: {
+        if (r2 < 1.0e-8f) return make_float3(0.f, 0.f, 0.f);  // dist < 0.0001
+        float s = -Wg * 2.0f * c.ivd;  // -W * 2 * dist * ivd * normalize(r) = -2 ivd W r
+        return make_float3(s * r.x, s * r.y, s * r.z);
+    }
+    case 0: {
+        float dist = sqrtf(r2);
+        if (dist > h || dist < 0.0001f) return make_float3(0.f, 0.f, 0.f);
+        float q = dist / h, l = 48.0f / (kPiF * h * h * h);
+        float s = q <= 0.5f ? l * q * (3.0f * q - 2.0f) : l * (-(1.0f - q) * (1.0f - q));
+        float inv = 1.0f / (dist * h);
+        return make_float3(s * (r.x * inv), s * (r.y * inv), s * (r.z * inv));
+    }
+    case 2: {
+        float dist = sqrtf(r2);
+        if (dist > h || dist < 0.0001f) return make_float3(0.f, 0.f, 0.f);
+        float h3 = h * h * h, m = h - dist;
+        float s = -45.0f * m * m / (kPiF * h3 * h3);
+        return make_float3(s * (r.x / dist), s * (r.y / dist), s * (r.z / dist));
+    }
+    case 3: {
+        float dist = sqrtf(r2);
+        float st = 3.0f / (kPiF * h * h * h * h);
+        if (dist > h || dist < 0.0001f) return make_float3(0.f, 0.f, 0.f);
+        float s = st / dist;
+        return make_float3(-r.x * s, -r.y * s, -r.z * s);
+    }
+    case 4: {
+        float dist = sqrtf(r2);
+        if (dist > h || dist < 0.0001f) return make_float3(0.f, 0.f, 0.f);
+        float a = 15.0f / (2.0f * kPiF * (h * h * h * h * h));
+        float s = -2.0f * a * fmaxf(0.0f, h - dist) / dist;
+        return make_float3(s * r.x, s * r.y, s * r.z);
+    }
+    default: return make_float3(0.f, 0.f, 0.f);
+    }
+}
+
+#endif  // __CUDACC__
+
+}  // namespace apbf

@@ -1,0 +1,525 @@
+// capi.cu -- the extern "C" boundary declared in include/apbf_gb300.h: context
+// lifetime, list access, stage dispatch and the whole-substep driver.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "apbf_internal.cuh"
+
+namespace apbf {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string &msg) { g_last_error = msg; }
+
+apbf_status cuda_check(cudaError_t e, const char *what) {
+    set_error(std::string(what) + ": " + cudaGetErrorString(e));
+    return APBF_ERR_CUDA;
+}
+
+namespace {
+
+template <typename T>
+apbf_status dalloc(T **p, size_t count, std::vector<void *> &owned) {
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void **)p, count * sizeof(T));
+    if (e != cudaSuccess) return cuda_check(e, "cudaMalloc");
+    owned.push_back((void *)*p);
+    return APBF_OK;
+}
+
+}  // namespace
+}  // namespace apbf
+
+using namespace apbf;
+
+extern "C" {
+
+uint32_t apbf_abi_version(void) { return APBF_ABI_VERSION; }
+
+const char *apbf_last_error(void) { return apbf::g_last_error.c_str(); }
+
+// Reference defaults, source/settings.cpp:5-31 (3D).
+void apbf_default_settings(apbf_settings *o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->height_kernel_id = 1;
+    o->gradient_kernel_id = 1;
+    o->merge = 1;
+    o->split = 1;
+    o->base_kernel_width_on_target_radius = 1;
+    o->base_kernel_width_on_boundary_distance = 1;
+    o->update_target_radius = 1;
+    o->update_boundariness = 1;
+    o->boundariness_calculation_method = 2;
+    o->basic_pbf = 0;
+    o->solver_iterations = 3;
+    o->boundariness_adaption_speed = 0.5f;
+    o->kernel_width_adaption_speed = 0.01f;
+    o->boundariness_self_grad_length_factor = 2.0f;
+    o->boundariness_underpressure_factor = 4.0f;
+    o->merge_duration = 2.0f;
+    o->split_duration = 0.0f;
+    o->smallest_target_radius = 1.0f;
+    o->target_radius_offset = 10.0f;
+    o->target_radius_scale_factor = 0.3f;
+}
+
+apbf_status apbf_destroy(apbf_ctx *ctx) {
+    if (!ctx) return APBF_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    for (auto &p : ctx->prof) {
+        cudaEventDestroy(p.a);
+        cudaEventDestroy(p.b);
+    }
+    for (void *p : ctx->owned) cudaFree(p);
+    delete ctx;
+    return APBF_OK;
+}
+
+apbf_status apbf_create(const apbf_config *cfg, apbf_ctx **out) {
+    if (!cfg || !out) return APBF_ERR_INVALID_ARG;
+    *out = nullptr;
+    if (cfg->particle_capacity == 0 || cfg->particle_capacity >= (1u << 28) || cfg->max_neighbors == 0 ||
+        cfg->max_log2res < 1 || cfg->max_log2res > 9) {
+        set_error("apbf_create: invalid capacities (particles in [1, 2^28), max_neighbors > 0, max_log2res in [1, 9])");
+        return APBF_ERR_INVALID_ARG;
+    }
+    apbf_ctx *ctx = new (std::nothrow) apbf_ctx();
+    if (!ctx) return APBF_ERR_INVALID_ARG;
+    ctx->cfg = *cfg;
+    if (ctx->cfg.transfer_capacity == 0) ctx->cfg.transfer_capacity = APBF_MAX_TRANSFERS;
+    apbf_default_settings(&ctx->settings);
+    std::memset(&ctx->scene, 0, sizeof(ctx->scene));
+    ctx->device = cfg->device;
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) {
+        delete ctx;
+        return cuda_check(e, "cudaSetDevice");
+    }
+    cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    const uint32_t cap = cfg->particle_capacity;
+    const uint32_t tcap = ctx->cfg.transfer_capacity;
+    ctx->row_stride = (cap + 31u) & ~31u;
+    auto &o = ctx->owned;
+    apbf_status r = APBF_OK;
+#define A(ptr, count)                                  \
+    do {                                               \
+        r = dalloc(&(ptr), (size_t)(count), o);        \
+        if (r != APBF_OK) {                            \
+            apbf_destroy(ctx);                         \
+            return r;                                  \
+        }                                              \
+    } while (0)
+    for (int k = 0; k < 2; ++k) {
+        FluidBufs &f = ctx->fl[k];
+        A(f.pos, cap);
+        A(f.vel, cap);
+        A(f.inv_mass, cap);
+        A(f.radius, cap);
+        A(f.pos_backup, cap);
+        A(f.transferring, cap);
+        A(f.target_radius, cap);
+        A(f.kernel_width, cap);
+        A(f.boundariness, cap);
+        A(f.boundary_distance, cap);
+        TransferBufs &t = ctx->tr[k];
+        A(t.source, tcap);
+        A(t.target, tcap);
+        A(t.time_left, tcap);
+    }
+    A(ctx->d_len, kLenSlots);
+    A(ctx->nb_count, cap);
+    A(ctx->rev_count, cap);
+    A(ctx->nb_idx, (size_t)ctx->row_stride * cfg->max_neighbors);
+    A(ctx->rev_idx, (size_t)ctx->row_stride * cfg->max_neighbors);
+    A(ctx->d_pairs, 1);
+    for (int k = 0; k < 2; ++k) {
+        A(ctx->keys[k], cap);
+        A(ctx->vals[k], cap);
+    }
+    ctx->sort_tiles = (cap + kSortTile - 1) / kSortTile;
+    A(ctx->sort_hist, 4 * 256);
+    A(ctx->sort_counters, 8);
+    A(ctx->sort_status, (size_t)4 * ctx->sort_tiles * 256);
+    A(ctx->sorted_keys, cap);
+    A(ctx->perm, cap);
+    A(ctx->inv_perm, cap);
+    A(ctx->scan_tmp, cap);
+    const size_t ncells = (size_t)1 << (3 * cfg->max_log2res);
+    A(ctx->cell_start, ncells);
+    A(ctx->cell_end, ncells);
+    ctx->n_cells_log2_alloc = cfg->max_log2res;
+    A(ctx->lambda, cap);
+    A(ctx->shift, cap);
+    A(ctx->kconst, cap);
+    A(ctx->dbg_density, cap);
+    A(ctx->dbg_grad, cap);
+    A(ctx->dbg_sq, cap);
+    A(ctx->ukw, cap);
+    A(ctx->min_nd, cap);
+    A(ctx->nearest, cap);
+    A(ctx->old_bd, cap);
+    A(ctx->proposal, cap);
+    A(ctx->claim, cap);
+    A(ctx->decided, cap);
+    A(ctx->flag_scan, cap);
+    A(ctx->list_a, cap);
+    A(ctx->list_b, cap);
+    ctx->red_blocks = grid_for(ctx, cap, kBlock, 8);
+    A(ctx->red_partials, (size_t)4 * ctx->red_blocks);
+    A(ctx->red_out, 4);
+    A(ctx->box_min, APBF_MAX_BOXES);
+    A(ctx->box_max, APBF_MAX_BOXES);
+    A(ctx->status, 1);
+#undef A
+    cudaMemset(ctx->d_len, 0, kLenSlots * sizeof(uint32_t));
+    cudaMemset(ctx->status, 0, sizeof(Status));
+    cudaMemset(ctx->red_out, 0, 4 * sizeof(double));
+    cudaMemset(ctx->nb_count, 0, (size_t)cap * sizeof(uint32_t));
+    for (int k = 0; k < 2; ++k) {
+        cudaMemset(ctx->fl[k].pos, 0, (size_t)cap * sizeof(int4));
+        cudaMemset(ctx->fl[k].pos_backup, 0, (size_t)cap * sizeof(int4));
+        cudaMemset(ctx->fl[k].vel, 0, (size_t)cap * sizeof(float4));
+        cudaMemset(ctx->fl[k].transferring, 0, (size_t)cap * sizeof(uint32_t));
+    }
+    e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        apbf_destroy(ctx);
+        return cuda_check(e, "apbf_create");
+    }
+    *out = ctx;
+    return APBF_OK;
+}
+
+apbf_status apbf_set_settings(apbf_ctx *ctx, const apbf_settings *s) {
+    if (!ctx || !s) return APBF_ERR_INVALID_ARG;
+    if (s->height_kernel_id < 0 || s->height_kernel_id > 4 || s->gradient_kernel_id < 0 || s->gradient_kernel_id > 4 ||
+        s->boundariness_calculation_method < 0 || s->boundariness_calculation_method > 2 || s->solver_iterations < 0) {
+        set_error("apbf_set_settings: kernel ids in [0, 4], boundariness method in [0, 2], iterations >= 0");
+        return APBF_ERR_INVALID_ARG;
+    }
+    ctx->settings = *s;
+    return APBF_OK;
+}
+
+apbf_status apbf_set_scene(apbf_ctx *ctx, const apbf_scene *scene) {
+    if (!ctx || !scene) return APBF_ERR_INVALID_ARG;
+    if (scene->log2res < 1 || scene->log2res > ctx->cfg.max_log2res) {
+        set_error("apbf_set_scene: log2res must be in [1, max_log2res]");
+        return APBF_ERR_INVALID_ARG;
+    }
+    ctx->scene = *scene;
+    return APBF_OK;
+}
+
+apbf_status apbf_set_boxes(apbf_ctx *ctx, const float *bmin, const float *bmax, uint32_t n) {
+    if (!ctx || n > APBF_MAX_BOXES || (n && (!bmin || !bmax))) return APBF_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    if (n) {
+        APBF_CUDA(cudaMemcpy(ctx->box_min, bmin, n * sizeof(float4), cudaMemcpyHostToDevice));
+        APBF_CUDA(cudaMemcpy(ctx->box_max, bmax, n * sizeof(float4), cudaMemcpyHostToDevice));
+    }
+    ctx->n_boxes = n;
+    return APBF_OK;
+}
+
+apbf_status apbf_set_debug(apbf_ctx *ctx, int enable) {
+    if (!ctx) return APBF_ERR_INVALID_ARG;
+    ctx->debug = enable ? 1 : 0;
+    return APBF_OK;
+}
+
+apbf_status apbf_fluid_get_view(apbf_ctx *ctx, apbf_fluid_view *o) {
+    if (!ctx || !o) return APBF_ERR_INVALID_ARG;
+    const FluidBufs &f = ctx->fl[ctx->fcur];
+    o->capacity = ctx->cfg.particle_capacity;
+    o->d_length = ctx->d_len + kLenParticles;
+    o->position = (int32_t *)f.pos;
+    o->velocity = (float *)f.vel;
+    o->inverse_mass = f.inv_mass;
+    o->radius = f.radius;
+    o->pos_backup = (int32_t *)f.pos_backup;
+    o->transferring = f.transferring;
+    o->target_radius = f.target_radius;
+    o->kernel_width = f.kernel_width;
+    o->boundariness = f.boundariness;
+    o->boundary_distance = f.boundary_distance;
+    return APBF_OK;
+}
+
+apbf_status apbf_transfers_get_view(apbf_ctx *ctx, apbf_transfers_view *o) {
+    if (!ctx || !o) return APBF_ERR_INVALID_ARG;
+    const TransferBufs &t = ctx->tr[ctx->tcur];
+    o->capacity = ctx->cfg.transfer_capacity;
+    o->d_length = ctx->d_len + kLenTransfers;
+    o->source = t.source;
+    o->target = t.target;
+    o->time_left = t.time_left;
+    return APBF_OK;
+}
+
+apbf_status apbf_neighbors_get_view(apbf_ctx *ctx, apbf_neighbors_view *o) {
+    if (!ctx || !o) return APBF_ERR_INVALID_ARG;
+    o->row_stride = ctx->row_stride;
+    o->max_per_row = ctx->cfg.max_neighbors;
+    o->count = ctx->nb_count;
+    o->index = ctx->nb_idx;
+    o->d_total = ctx->d_pairs;
+    return APBF_OK;
+}
+
+apbf_status apbf_set_lengths(apbf_ctx *ctx, uint32_t np, uint32_t nt, void *stream) {
+    if (!ctx || np > ctx->cfg.particle_capacity || nt > ctx->cfg.transfer_capacity) {
+        set_error("apbf_set_lengths: length above capacity");
+        return APBF_ERR_INVALID_ARG;
+    }
+    uint32_t v[2] = {np, nt};
+    cudaStream_t s = (cudaStream_t)stream;
+    APBF_CUDA(cudaMemcpyAsync(ctx->d_len, v, sizeof(v), cudaMemcpyHostToDevice, s));
+    APBF_CUDA(cudaStreamSynchronize(s));
+    return APBF_OK;
+}
+
+apbf_status apbf_get_lengths(apbf_ctx *ctx, uint32_t *np, uint32_t *nt, void *stream) {
+    if (!ctx) return APBF_ERR_INVALID_ARG;
+    uint32_t v[2];
+    cudaStream_t s = (cudaStream_t)stream;
+    APBF_CUDA(cudaMemcpyAsync(v, ctx->d_len, sizeof(v), cudaMemcpyDeviceToHost, s));
+    APBF_CUDA(cudaStreamSynchronize(s));
+    if (np) *np = v[0];
+    if (nt) *nt = v[1];
+    return APBF_OK;
+}
+
+apbf_status apbf_velocity_handling_apply(apbf_ctx *ctx, float dt, const float acc[3], void *stream) {
+    if (!ctx || !acc) return APBF_ERR_INVALID_ARG;
+    return velocity_handling(ctx, dt, acc, (cudaStream_t)stream);
+}
+
+apbf_status apbf_neighborhood_green_apply(apbf_ctx *ctx, float range_scale, const float minp[3], const float maxp[3],
+                                          uint32_t log2res, void *stream) {
+    if (!ctx || !minp || !maxp) return APBF_ERR_INVALID_ARG;
+    return neighborhood_green(ctx, range_scale, minp, maxp, log2res, (cudaStream_t)stream);
+}
+
+apbf_status apbf_box_collision_apply(apbf_ctx *ctx, void *stream) {
+    if (!ctx) return APBF_ERR_INVALID_ARG;
+    return box_collision(ctx, (cudaStream_t)stream);
+}
+
+apbf_status apbf_incompressibility_apply(apbf_ctx *ctx, void *stream) {
+    if (!ctx) return APBF_ERR_INVALID_ARG;
+    return incompressibility(ctx, (cudaStream_t)stream);
+}
+
+apbf_status apbf_kernel_width_from_boundary_distance_apply(apbf_ctx *ctx, void *stream) {
+    if (!ctx) return APBF_ERR_INVALID_ARG;
+    return kw_from_boundary_distance(ctx, (cudaStream_t)stream);
+}
+
+apbf_status apbf_spread_kernel_width_apply(apbf_ctx *ctx, void *stream) {
+    if (!ctx) return APBF_ERR_INVALID_ARG;
+    return spread_kernel_width(ctx, (cudaStream_t)stream);
+}
+
+apbf_status apbf_update_transfers_apply(apbf_ctx *ctx, void *stream) {
+    if (!ctx) return APBF_ERR_INVALID_ARG;
+    return update_transfers(ctx, (cudaStream_t)stream);
+}
+
+apbf_status apbf_particle_transfer_apply(apbf_ctx *ctx, float dt, void *stream) {
+    if (!ctx) return APBF_ERR_INVALID_ARG;
+    return particle_transfer(ctx, dt, (cudaStream_t)stream);
+}
+
+// pool::update (source/pool.cpp:67-106).
+apbf_status apbf_substep(apbf_ctx *ctx, float dt, void *stream) {
+    if (!ctx) return APBF_ERR_INVALID_ARG;
+    if (ctx->scene.log2res < 1) {
+        set_error("apbf_substep: call apbf_set_scene first");
+        return APBF_ERR_INVALID_ARG;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    const apbf_settings &st = ctx->settings;
+    apbf_status r = velocity_handling(ctx, dt, ctx->scene.acceleration, s);
+    if (r != APBF_OK) return r;
+    const bool adaptive = !st.basic_pbf;
+    if (adaptive && (st.merge || st.split)) {
+        r = particle_transfer(ctx, dt, s);
+        if (r != APBF_OK) return r;
+    }
+    if (adaptive && st.base_kernel_width_on_boundary_distance) {
+        r = kw_from_boundary_distance(ctx, s);
+        if (r != APBF_OK) return r;
+    }
+    const float scale = (st.basic_pbf || st.base_kernel_width_on_boundary_distance) ? 1.0f : 1.5f;
+    r = neighborhood_green(ctx, scale, ctx->scene.min_pos, ctx->scene.max_pos, ctx->scene.log2res, s);
+    if (r != APBF_OK) return r;
+    if (adaptive && !st.base_kernel_width_on_boundary_distance) {
+        r = spread_kernel_width(ctx, s);
+        if (r != APBF_OK) return r;
+    }
+    for (int it = 0; it < st.solver_iterations; ++it) {
+        r = box_collision(ctx, s);
+        if (r != APBF_OK) return r;
+        r = incompressibility(ctx, s);
+        if (r != APBF_OK) return r;
+    }
+    if (adaptive) {
+        r = update_transfers(ctx, s);
+        if (r != APBF_OK) return r;
+    }
+    return APBF_OK;
+}
+
+apbf_status apbf_reduce_fp64(apbf_ctx *ctx, double out[4], void *stream) {
+    if (!ctx || !out) return APBF_ERR_INVALID_ARG;
+    return reduce_fp64(ctx, out, (cudaStream_t)stream);
+}
+
+apbf_status apbf_get_status(apbf_ctx *ctx, apbf_status_info *out, int clear, void *stream) {
+    if (!ctx || !out) return APBF_ERR_INVALID_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    Status hs;
+    unsigned long long pairs = 0;
+    APBF_CUDA(cudaMemcpyAsync(&hs, ctx->status, sizeof(Status), cudaMemcpyDeviceToHost, s));
+    APBF_CUDA(cudaMemcpyAsync(&pairs, ctx->d_pairs, sizeof(pairs), cudaMemcpyDeviceToHost, s));
+    APBF_CUDA(cudaStreamSynchronize(s));
+    out->flags = hs.flags;
+    out->required_neighbors = hs.required_neighbors;
+    out->required_transfers = hs.required_transfers;
+    out->required_particles = hs.required_particles;
+    out->pairs = pairs;
+    if (clear) {
+        Status z = hs;
+        z.flags = 0;
+        z.required_neighbors = z.required_transfers = z.required_particles = 0;
+        z.spin_where = 0;
+        APBF_CUDA(cudaMemcpyAsync(ctx->status, &z, sizeof(Status), cudaMemcpyHostToDevice, s));
+        APBF_CUDA(cudaStreamSynchronize(s));
+    }
+    if (hs.flags & APBF_FLAG_SPIN_LIMIT) return APBF_ERR_SPIN_LIMIT;
+    if (hs.flags & (APBF_FLAG_NEIGHBOR_OVERFLOW | APBF_FLAG_TRANSFER_OVERFLOW | APBF_FLAG_PARTICLE_OVERFLOW |
+                    APBF_FLAG_GRID_OVERFLOW))
+        return APBF_ERR_CAPACITY;
+    if (hs.flags & APBF_FLAG_NONFINITE) return APBF_ERR_NONFINITE;
+    return APBF_OK;
+}
+
+apbf_status apbf_export_pairs(apbf_ctx *ctx, uint32_t *d_pairs, uint32_t cap, uint32_t *d_length, void *stream) {
+    if (!ctx || !d_pairs || !d_length) return APBF_ERR_INVALID_ARG;
+    return export_pairs(ctx, d_pairs, cap, d_length, (cudaStream_t)stream);
+}
+
+apbf_status apbf_debug_incompressibility(apbf_ctx *ctx, uint32_t *d_density, int32_t *d_grad4, uint32_t *d_sq,
+                                         float *d_lambda, void *stream) {
+    if (!ctx) return APBF_ERR_INVALID_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t n = ctx->cfg.particle_capacity;
+    if (d_density) APBF_CUDA(cudaMemcpyAsync(d_density, ctx->dbg_density, n * 4, cudaMemcpyDeviceToDevice, s));
+    if (d_grad4) APBF_CUDA(cudaMemcpyAsync(d_grad4, ctx->dbg_grad, n * 16, cudaMemcpyDeviceToDevice, s));
+    if (d_sq) APBF_CUDA(cudaMemcpyAsync(d_sq, ctx->dbg_sq, n * 4, cudaMemcpyDeviceToDevice, s));
+    if (d_lambda) APBF_CUDA(cudaMemcpyAsync(d_lambda, ctx->lambda, n * 4, cudaMemcpyDeviceToDevice, s));
+    return APBF_OK;
+}
+
+apbf_status apbf_debug_sort(apbf_ctx *ctx, uint32_t *d_perm, uint32_t *d_keys, void *stream) {
+    if (!ctx) return APBF_ERR_INVALID_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t n = ctx->cfg.particle_capacity;
+    if (d_perm) APBF_CUDA(cudaMemcpyAsync(d_perm, ctx->perm, n * 4, cudaMemcpyDeviceToDevice, s));
+    if (d_keys) APBF_CUDA(cudaMemcpyAsync(d_keys, ctx->sorted_keys, n * 4, cudaMemcpyDeviceToDevice, s));
+    return APBF_OK;
+}
+
+apbf_status apbf_profile_enable(apbf_ctx *ctx, int enable, uint32_t capacity) {
+    if (!ctx) return APBF_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    if (enable && capacity > ctx->prof.size()) {
+        size_t old = ctx->prof.size();
+        ctx->prof.resize(capacity);
+        for (size_t i = old; i < capacity; ++i) {
+            APBF_CUDA(cudaEventCreate(&ctx->prof[i].a));
+            APBF_CUDA(cudaEventCreate(&ctx->prof[i].b));
+            ctx->prof[i].name = "";
+        }
+    }
+    ctx->prof_on = enable != 0;
+    ctx->prof_used = 0;
+    ctx->prof_dropped = 0;
+    return APBF_OK;
+}
+
+apbf_status apbf_profile_read(apbf_ctx *ctx, apbf_kernel_time *out, uint32_t cap, uint32_t *n_out,
+                              unsigned long long *dropped, void *stream) {
+    if (!ctx || (!out && cap) || !n_out) return APBF_ERR_INVALID_ARG;
+    APBF_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    std::vector<apbf_kernel_time> agg;
+    for (size_t i = 0; i < ctx->prof_used; ++i) {
+        float ms = 0.0f;
+        APBF_CUDA(cudaEventElapsedTime(&ms, ctx->prof[i].a, ctx->prof[i].b));
+        const char *nm = ctx->prof[i].name;
+        size_t k = 0;
+        for (; k < agg.size(); ++k)
+            if (std::strncmp(agg[k].name, nm, sizeof(agg[k].name)) == 0) break;
+        if (k == agg.size()) {
+            apbf_kernel_time t;
+            std::memset(&t, 0, sizeof(t));
+            std::strncpy(t.name, nm, sizeof(t.name) - 1);
+            agg.push_back(t);
+        }
+        agg[k].launches++;
+        agg[k].total_ms += ms;
+    }
+    uint32_t m = (uint32_t)std::min<size_t>(agg.size(), cap);
+    for (uint32_t k = 0; k < m; ++k) out[k] = agg[k];
+    *n_out = m;
+    if (dropped) *dropped = ctx->prof_dropped;
+    ctx->prof_used = 0;
+    ctx->prof_dropped = 0;
+    return APBF_OK;
+}
+
+apbf_status apbf_launch_count(apbf_ctx *ctx, unsigned long long *out) {
+    if (!ctx || !out) return APBF_ERR_INVALID_ARG;
+    *out = ctx->launches;
+    return APBF_OK;
+}
+
+static uint32_t bit_length(uint32_t v) {
+    uint32_t b = 0;
+    while (v) {
+        ++b;
+        v >>= 1;
+    }
+    return b;
+}
+
+apbf_status apbf_sort_pairs(apbf_ctx *ctx, const uint32_t *d_keys, const uint32_t *d_values, const uint32_t *d_count,
+                            uint32_t max_count, uint32_t value_upper_bound, uint32_t *d_out_keys,
+                            uint32_t *d_out_values, void *stream) {
+    if (!ctx || !d_keys || !d_values || !d_count || !d_out_keys || !d_out_values) return APBF_ERR_INVALID_ARG;
+    if (max_count > ctx->cfg.particle_capacity) {
+        set_error("apbf_sort_pairs: max_count above the context's particle capacity");
+        return APBF_ERR_INVALID_ARG;
+    }
+    return sort_pairs_device(ctx, d_keys, d_values, d_count, max_count, bit_length(value_upper_bound), d_out_keys,
+                             d_out_values, (cudaStream_t)stream);
+}
+
+apbf_status apbf_prefix_sum(apbf_ctx *ctx, uint32_t *d_values, const uint32_t *d_count, uint32_t max_count,
+                            void *stream) {
+    if (!ctx || !d_values || !d_count) return APBF_ERR_INVALID_ARG;
+    if (max_count > ctx->cfg.particle_capacity) {
+        set_error("apbf_prefix_sum: max_count above the context's particle capacity");
+        return APBF_ERR_INVALID_ARG;
+    }
+    return prefix_sum_device(ctx, d_values, d_count, max_count, (cudaStream_t)stream);
+}
+
+}  // extern "C"

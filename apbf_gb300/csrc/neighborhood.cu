@@ -1,0 +1,300 @@
+// neighborhood.cu -- neighborhood_green::apply (source/neighborhood_green.cpp:27-77).
+//
+//  1. k_position_keys: Morton key of each particle's grid cell
+//     (calculate_position_hash.comp:23-46; canonical integer cell mapping).
+//  2. sort_pairs_device: stable sort of (key, particle id).
+//  3. k_reorder: gather every particle attribute into the alternate buffer set and
+//     swap (hidden_list().apply_edit + mParticles->sort(), neighborhood_green.cpp:54-56),
+//     remap the transfer list (indexed_list.h:288-308).
+//  4. k_cell_ranges: [start, end) of every occupied cell (find_value_ranges.comp).
+//  5. k_build_rows: per particle, walk the cells overlapping [X - R, X + R] and keep
+//     every other particle within R (neighborhood_green.comp:49-87), written
+//     column-major so that consecutive particles' k-th entries are contiguous.
+//  6. k_reverse_rows (only when search radii differ): transpose the rows, so the
+//     position-update pass can gather instead of scattering with atomics.
+#include "apbf_internal.cuh"
+
+namespace apbf {
+namespace {
+
+struct Bounds {
+    long long lo[3];
+    long long hi[3];
+};
+
+Bounds fixed_bounds(const float minp[3], const float maxp[3]) {
+    Bounds b;
+    for (int d = 0; d < 3; ++d) {
+        b.lo[d] = llround((double)minp[d] * 262144.0);
+        b.hi[d] = llround((double)maxp[d] * 262144.0);
+        if (b.hi[d] <= b.lo[d]) b.hi[d] = b.lo[d] + 1;
+    }
+    return b;
+}
+
+__global__ void k_position_keys(const int4 *__restrict__ pos, const uint32_t *d_len, Bounds b, uint32_t L,
+                                uint32_t *__restrict__ keys, uint32_t *__restrict__ seq) {
+    uint32_t n = d_len[kLenParticles];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int4 p = pos[i];
+        uint32_t cx = cell_coord(p.x, b.lo[0], b.hi[0], L);
+        uint32_t cy = cell_coord(p.y, b.lo[1], b.hi[1], L);
+        uint32_t cz = cell_coord(p.z, b.lo[2], b.hi[2], L);
+        keys[i] = morton3(cx, cy, cz);
+        seq[i] = i;
+    }
+}
+
+// Gather of every attribute by the sort permutation (copy_scattered_read.comp).
+__global__ void k_reorder(FluidBufs src, FluidBufs dst, const uint32_t *__restrict__ perm,
+                          uint32_t *__restrict__ inv_perm, const uint32_t *d_len) {
+    uint32_t n = d_len[kLenParticles];
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        uint32_t o = perm[k];
+        dst.pos[k] = src.pos[o];
+        dst.vel[k] = src.vel[o];
+        dst.inv_mass[k] = src.inv_mass[o];
+        dst.radius[k] = src.radius[o];
+        dst.pos_backup[k] = src.pos_backup[o];
+        dst.transferring[k] = src.transferring[o];
+        dst.target_radius[k] = src.target_radius[o];
+        dst.kernel_width[k] = src.kernel_width[o];
+        dst.boundariness[k] = src.boundariness[o];
+        dst.boundary_distance[k] = src.boundary_distance[o];
+        inv_perm[o] = k;
+    }
+}
+
+__global__ void k_remap_transfers(TransferBufs t, const uint32_t *__restrict__ inv_perm, const uint32_t *d_len,
+                                  Status *st) {
+    const uint32_t nt = d_len[kLenTransfers], n = d_len[kLenParticles];
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nt; k += gridDim.x * blockDim.x) {
+        const uint32_t s = t.source[k], g = t.target[k];
+        if (s >= n || g >= n) {  // a transfer naming a particle that does not exist
+            set_flag(st, APBF_FLAG_NONFINITE);
+            continue;
+        }
+        t.source[k] = inv_perm[s];
+        t.target[k] = inv_perm[g];
+    }
+}
+
+// find_value_ranges.comp:15-31 (cell arrays zeroed beforehand).
+__global__ void k_cell_ranges(const uint32_t *__restrict__ skeys, const uint32_t *d_len, uint32_t *__restrict__ start,
+                              uint32_t *__restrict__ end) {
+    uint32_t n = d_len[kLenParticles];
+    for (uint32_t id = blockIdx.x * blockDim.x + threadIdx.x; id < n; id += gridDim.x * blockDim.x) {
+        uint32_t cur = skeys[id];
+        uint32_t prev = id == 0 ? cur : skeys[id - 1];
+        if (id == 0 || cur != prev) start[cur] = id;
+        if (id != 0 && cur != prev) end[prev] = id;
+        if (id == n - 1) end[cur] = id + 1u;
+    }
+}
+
+__device__ __forceinline__ long long range_fixed(float kw, float scale) {
+    double r = (double)kw * (double)scale * 262144.0;
+    if (!(r >= 0.0)) return -1;
+    if (r > 4.0e18) r = 4.0e18;
+    return (long long)floor(r);
+}
+
+__device__ __forceinline__ bool within(int4 a, int4 b, long long R) {
+    long long dx = (long long)b.x - a.x, dy = (long long)b.y - a.y, dz = (long long)b.z - a.z;
+    dx = dx < 0 ? -dx : dx;
+    dy = dy < 0 ? -dy : dy;
+    dz = dz < 0 ? -dz : dz;
+    if (dx > R || dy > R || dz > R) return false;
+    unsigned long long s = (unsigned long long)(dx * dx) + (unsigned long long)(dy * dy) + (unsigned long long)(dz * dz);
+    return s <= (unsigned long long)R * (unsigned long long)R;
+}
+
+// neighborhood_green.comp:49-87 with the canonical predicate; rows column-major.
+__global__ void __launch_bounds__(256) k_build_rows(const int4 *__restrict__ pos, const float *__restrict__ range,
+                                                    float scale, const uint32_t *d_len, Bounds b, uint32_t L,
+                                                    const uint32_t *__restrict__ cstart,
+                                                    const uint32_t *__restrict__ cend, uint32_t stride, uint32_t maxn,
+                                                    uint32_t *__restrict__ count, uint32_t *__restrict__ idx,
+                                                    unsigned long long *total, Status *st) {
+    uint32_t n = d_len[kLenParticles];
+    unsigned long long local = 0;
+    long long rmin = 0x7fffffffffffffffll, rmax = -1;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int4 p = pos[i];
+        long long R = range_fixed(range[i], scale);
+        if (R < 0) {
+            set_flag(st, APBF_FLAG_NONFINITE);  // NaN or negative kernel width: no neighbours
+        } else {
+            rmin = R < rmin ? R : rmin;
+            rmax = R > rmax ? R : rmax;
+        }
+        uint32_t c = 0;
+        if (R >= 0) {
+            uint32_t x0 = cell_coord((long long)p.x - R, b.lo[0], b.hi[0], L);
+            uint32_t x1 = cell_coord((long long)p.x + R, b.lo[0], b.hi[0], L);
+            uint32_t y0 = cell_coord((long long)p.y - R, b.lo[1], b.hi[1], L);
+            uint32_t y1 = cell_coord((long long)p.y + R, b.lo[1], b.hi[1], L);
+            uint32_t z0 = cell_coord((long long)p.z - R, b.lo[2], b.hi[2], L);
+            uint32_t z1 = cell_coord((long long)p.z + R, b.lo[2], b.hi[2], L);
+            for (uint32_t cz = z0; cz <= z1; ++cz)
+                for (uint32_t cy = y0; cy <= y1; ++cy)
+                    for (uint32_t cx = x0; cx <= x1; ++cx) {
+                        uint32_t key = morton3(cx, cy, cz);
+                        uint32_t s = cstart[key], e = cend[key];
+                        for (uint32_t j = s; j < e; ++j) {
+                            if (j == i) continue;
+                            if (!within(p, pos[j], R)) continue;
+                            if (c < maxn) idx[(size_t)c * stride + i] = j;
+                            ++c;
+                        }
+                    }
+        }
+        if (c > maxn) {
+            set_flag(st, APBF_FLAG_NEIGHBOR_OVERFLOW);
+            atomicMax(&st->required_neighbors, c);
+        }
+        count[i] = c < maxn ? c : maxn;
+        local += c < maxn ? c : maxn;
+    }
+    // block reduction of the pair count and of the radius range
+    for (int off = 16; off > 0; off >>= 1) {
+        local += __shfl_down_sync(0xffffffffu, local, off);
+        long long a = __shfl_down_sync(0xffffffffu, rmin, off);
+        long long c2 = __shfl_down_sync(0xffffffffu, rmax, off);
+        rmin = a < rmin ? a : rmin;
+        rmax = c2 > rmax ? c2 : rmax;
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (local) atomicAdd(total, local);
+        if (rmax >= 0) {
+            atomicMin(&st->range_min, (unsigned long long)rmin);
+            atomicMax(&st->range_max, (unsigned long long)rmax);
+        }
+    }
+}
+
+__global__ void k_reverse_rows(const uint32_t *d_len, uint32_t stride, uint32_t maxn, const uint32_t *__restrict__ count,
+                               const uint32_t *__restrict__ idx, uint32_t *__restrict__ rcount,
+                               uint32_t *__restrict__ ridx, Status *st) {
+    if (st->range_min == st->range_max) return;  // symmetric rows: reverse = forward
+    uint32_t n = d_len[kLenParticles];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t c = count[i];
+        for (uint32_t k = 0; k < c; ++k) {
+            uint32_t j = idx[(size_t)k * stride + i];
+            uint32_t slot = atomicAdd(&rcount[j], 1u);
+            if (slot < maxn) {
+                ridx[(size_t)slot * stride + j] = i;
+            } else {
+                set_flag(st, APBF_FLAG_NEIGHBOR_OVERFLOW);
+                atomicMax(&st->required_neighbors, slot + 1u);
+            }
+        }
+    }
+}
+
+__global__ void k_clamp_rev(const uint32_t *d_len, uint32_t maxn, uint32_t *rcount, Status *st) {
+    if (st->range_min == st->range_max) return;
+    uint32_t n = d_len[kLenParticles];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        if (rcount[i] > maxn) rcount[i] = maxn;
+}
+
+__global__ void k_reset_search(Status *st, unsigned long long *total) {
+    st->range_min = 0xffffffffffffffffull;
+    st->range_max = 0ull;
+    *total = 0ull;
+}
+
+// Pair export (the reference's uvec2 list): row-major order of the rows.
+__global__ void k_export_pairs(const uint32_t *d_len, uint32_t stride, const uint32_t *__restrict__ count,
+                               const uint32_t *__restrict__ idx, const uint32_t *__restrict__ offsets, uint32_t cap,
+                               uint2 *__restrict__ out) {
+    uint32_t n = d_len[kLenParticles];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t c = count[i];
+        uint32_t o = offsets[i] - c;  // inclusive scan -> row start
+        for (uint32_t k = 0; k < c; ++k)
+            if (o + k < cap) out[o + k] = make_uint2(i, idx[(size_t)k * stride + i]);
+    }
+}
+
+__global__ void k_export_len(const uint32_t *d_len, const uint32_t *offsets, uint32_t *out_len) {
+    uint32_t n = d_len[kLenParticles];
+    *out_len = n ? offsets[n - 1] : 0u;
+}
+
+void swap_all(apbf_ctx *ctx) { ctx->fcur ^= 1; }
+
+}  // namespace
+
+apbf_status neighborhood_green(apbf_ctx *ctx, float range_scale, const float minp[3], const float maxp[3],
+                               uint32_t L, cudaStream_t s) {
+    if (L < 1 || L > ctx->cfg.max_log2res || L > 10) return APBF_ERR_INVALID_ARG;
+    const uint32_t cap = ctx->cfg.particle_capacity;
+    Bounds b = fixed_bounds(minp, maxp);
+    FluidBufs &cur = ctx->fl[ctx->fcur];
+    FluidBufs &alt = ctx->fl[ctx->fcur ^ 1];
+    const int g = grid_for(ctx, cap);
+
+    APBF_BEFORE_LAUNCH(ctx, s, "k_position_keys");
+    k_position_keys<<<g, kBlock, 0, s>>>(cur.pos, ctx->d_len, b, L, ctx->keys[0], ctx->vals[0]);
+    APBF_AFTER_LAUNCH(ctx, s, "k_position_keys");
+    apbf_status r = sort_pairs_device(ctx, ctx->keys[0], ctx->vals[0], ctx->d_len + kLenParticles, cap, 3u * L,
+                                      ctx->sorted_keys, ctx->perm, s);
+    if (r != APBF_OK) return r;
+    k_reorder<<<g, kBlock, 0, s>>>(cur, alt, ctx->perm, ctx->inv_perm, ctx->d_len);
+    APBF_AFTER_LAUNCH(ctx, s, "k_reorder");
+    APBF_BEFORE_LAUNCH(ctx, s, "k_remap_transfers");
+    k_remap_transfers<<<grid_for(ctx, ctx->cfg.transfer_capacity), kBlock, 0, s>>>(ctx->tr[ctx->tcur], ctx->inv_perm,
+                                                                                    ctx->d_len, ctx->status);
+    APBF_AFTER_LAUNCH(ctx, s, "k_remap_transfers");
+    swap_all(ctx);
+    FluidBufs &f = ctx->fl[ctx->fcur];
+
+    const size_t ncells = (size_t)1 << (3 * L);
+    APBF_CUDA(cudaMemsetAsync(ctx->cell_start, 0, ncells * sizeof(uint32_t), s));
+    APBF_CUDA(cudaMemsetAsync(ctx->cell_end, 0, ncells * sizeof(uint32_t), s));
+    APBF_BEFORE_LAUNCH(ctx, s, "k_cell_ranges");
+    k_cell_ranges<<<g, kBlock, 0, s>>>(ctx->sorted_keys, ctx->d_len, ctx->cell_start, ctx->cell_end);
+    APBF_AFTER_LAUNCH(ctx, s, "k_cell_ranges");
+    APBF_BEFORE_LAUNCH(ctx, s, "k_reset_search");
+    k_reset_search<<<1, 1, 0, s>>>(ctx->status, ctx->d_pairs);
+    APBF_AFTER_LAUNCH(ctx, s, "k_reset_search");
+    APBF_BEFORE_LAUNCH(ctx, s, "k_build_rows");
+    k_build_rows<<<grid_for(ctx, cap, kBlock, 16), kBlock, 0, s>>>(
+        f.pos, f.kernel_width, range_scale, ctx->d_len, b, L, ctx->cell_start, ctx->cell_end, ctx->row_stride,
+        ctx->cfg.max_neighbors, ctx->nb_count, ctx->nb_idx, ctx->d_pairs, ctx->status);
+    APBF_AFTER_LAUNCH(ctx, s, "k_build_rows");
+    return build_reverse_rows(ctx, s);
+}
+
+apbf_status build_reverse_rows(apbf_ctx *ctx, cudaStream_t s) {
+    const uint32_t cap = ctx->cfg.particle_capacity;
+    APBF_CUDA(cudaMemsetAsync(ctx->rev_count, 0, (size_t)cap * sizeof(uint32_t), s));
+    APBF_BEFORE_LAUNCH(ctx, s, "k_reverse_rows");
+    k_reverse_rows<<<grid_for(ctx, cap), kBlock, 0, s>>>(ctx->d_len, ctx->row_stride, ctx->cfg.max_neighbors,
+                                                         ctx->nb_count, ctx->nb_idx, ctx->rev_count, ctx->rev_idx,
+                                                         ctx->status);
+    APBF_AFTER_LAUNCH(ctx, s, "k_reverse_rows");
+    APBF_BEFORE_LAUNCH(ctx, s, "k_clamp_rev");
+    k_clamp_rev<<<grid_for(ctx, cap), kBlock, 0, s>>>(ctx->d_len, ctx->cfg.max_neighbors, ctx->rev_count, ctx->status);
+    APBF_AFTER_LAUNCH(ctx, s, "k_clamp_rev");
+    return APBF_OK;
+}
+
+apbf_status export_pairs(apbf_ctx *ctx, uint32_t *d_pairs, uint32_t cap_pairs, uint32_t *d_length, cudaStream_t s) {
+    const uint32_t cap = ctx->cfg.particle_capacity;
+    APBF_CUDA(cudaMemcpyAsync(ctx->scan_tmp, ctx->nb_count, (size_t)cap * 4, cudaMemcpyDeviceToDevice, s));
+    apbf_status r = prefix_sum_device(ctx, ctx->scan_tmp, ctx->d_len + kLenParticles, cap, s);
+    if (r != APBF_OK) return r;
+    k_export_pairs<<<grid_for(ctx, cap), kBlock, 0, s>>>(ctx->d_len, ctx->row_stride, ctx->nb_count, ctx->nb_idx,
+                                                         ctx->scan_tmp, cap_pairs, (uint2 *)d_pairs);
+    APBF_AFTER_LAUNCH(ctx, s, "k_export_pairs");
+    APBF_BEFORE_LAUNCH(ctx, s, "k_export_len");
+    k_export_len<<<1, 1, 0, s>>>(ctx->d_len, ctx->scan_tmp, d_length);
+    APBF_AFTER_LAUNCH(ctx, s, "k_export_len");
+    return APBF_OK;
+}
+
+}  // namespace apbf

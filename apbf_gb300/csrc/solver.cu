@@ -1,0 +1,408 @@
+// solver.cu -- incompressibility::apply (source/incompressibility.cpp:12-45), one
+// Jacobi iteration in two gather passes instead of the reference's four
+// dispatches with per-pair integer atomics:
+//
+//  k_density_lambda (particle i, over its own row):  incompressibility_0.comp
+//    (self density) + incompressibility_1.comp (density, weighted gradient and
+//    squared-gradient sums, as 2^18 fixed-point integers) + incompressibility_2.comp
+//    (lambda, boundariness, self shift) + the boundariness filter of
+//    incompressibility_3.comp:41-46,60.  Writes lambda, the self shift, the
+//    per-particle Gauss constants and the FP64 density-error partials.
+//  k_delta (particle j, over the particles whose rows contain j):
+//    incompressibility_3.comp:62-66 as a gather: x_j += sum_i int(gradW_ij * lambda_i * 2^18)
+//    plus the self shift, into the other position buffer.
+//
+// The per-pair integer terms are computed by the same code from the same inputs
+// as the scatter form, and integer addition is associative, so the gather is
+// bit-identical to the atomic scatter.  Gradients are recomputed in k_delta
+// rather than stored (the reference writes 16 bytes per pair).
+#include "apbf_internal.cuh"
+
+namespace apbf {
+namespace {
+
+// Contraction-proof dot product: k_density_lambda and k_delta must evaluate
+// bit-identical gradients for the same pair.
+__device__ __forceinline__ float dot3x(float3 a, float3 b) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)), __fmul_rn(a.z, b.z));
+}
+
+struct PassA {
+    const int4 *pos;
+    const float *inv_mass;
+    const float *radius;
+    const float *kw;
+    float *bness;
+    const uint32_t *count;
+    const uint32_t *idx;
+    uint32_t stride;
+    float *lambda;
+    int4 *shift;
+    KConst *kc;
+    uint32_t *dbg_dens;
+    int4 *dbg_grad;
+    uint32_t *dbg_sq;
+    double *partials;
+    const uint32_t *d_len;
+    Status *st;
+    float rmin3;  // pow(2 * smallestTargetRadius, 3)
+    int hk, gk, method, update_b;
+    float b_speed, b_sgl_factor, b_up_factor;
+};
+
+template <bool GAUSS>
+__device__ __forceinline__ void pair_terms(int hk, int gk, float3 d, float kw, KConst c, float &W, float3 &g) {
+    float r2 = dot3x(d, d);
+    if (GAUSS) {
+        W = gauss_height(r2, c);
+        g = kernel_gradient(1, d, r2, kw, c, W);
+    } else {
+        W = kernel_height(hk, r2, kw, c);
+        float Wg = gk == 1 ? (hk == 1 ? W : gauss_height(r2, c)) : 0.0f;
+        g = kernel_gradient(gk, d, r2, kw, c, Wg);
+    }
+}
+
+template <bool GAUSS>
+__global__ void __launch_bounds__(256) k_density_lambda(PassA a) {
+    const uint32_t n = a.d_len[kLenParticles];
+    double e1 = 0.0, e2 = 0.0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int4 p = a.pos[i];
+        const float kw = a.kw[i], im = a.inv_mass[i], radius = a.radius[i];
+        const KConst c = gauss_consts(kw);
+        a.kc[i] = c;
+        float W0 = GAUSS ? c.norm : kernel_height(a.hk, 0.0f, kw, c);
+        uint32_t dens = f2u(W0 / im * APBF_FIX);
+        int32_t gx = 0, gy = 0, gz = 0;
+        uint32_t sq = 0;
+        int32_t cx = 0, cy = 0, cz = 0, cw = 0;
+        const uint32_t cnt = a.count[i];
+        for (uint32_t k = 0; k < cnt; ++k) {
+            const uint32_t j = a.idx[(size_t)k * a.stride + i];
+            const int4 q = a.pos[j];
+            const float imn = a.inv_mass[j];
+            const float3 d = fdiff(p, q);
+            float W;
+            float3 g;
+            pair_terms<GAUSS>(a.hk, a.gk, d, kw, c, W, g);
+            dens += f2u(W / imn * APBF_FIX);
+            gx = wadd(gx, f2i(g.x / imn * APBF_FIX));
+            gy = wadd(gy, f2i(g.y / imn * APBF_FIX));
+            gz = wadd(gz, f2i(g.z / imn * APBF_FIX));
+            sq += f2u(dot3x(g, g) / imn * APBF_FIX);
+            if (a.method == 1) {  // incompressibility_1.comp:62-68
+                float den = imn * kw;
+                cx = wadd(cx, f2i((float)wadd(q.x, -p.x) / den));
+                cy = wadd(cy, f2i((float)wadd(q.y, -p.y) / den));
+                cz = wadd(cz, f2i((float)wadd(q.z, -p.z) / den));
+                cw = wadd(cw, f2i(APBF_FIX / imn));
+            }
+        }
+        // incompressibility_2.comp:77-109
+        const float r2x = 2.0f * radius;
+        const float ird = (r2x * r2x * r2x) * im;
+        const float density = (float)dens * APBF_INV_FIX;
+        const float3 wgs = make_float3((float)gx * APBF_INV_FIX, (float)gy * APBF_INV_FIX, (float)gz * APBF_INV_FIX);
+        float sqs = (float)sq * APBF_INV_FIX;
+        const float wgsq = dot3x(wgs, wgs);
+        const float sgl = sqrtf(wgsq) * ird;
+        sqs += wgsq * im;
+        const float under = 1.0f - density * ird;
+        float b = a.bness[i];
+        if (a.update_b) {
+            float bn;
+            if (a.method == 1) {
+                float tm = (float)cw * APBF_INV_FIX + 1.0f / im;
+                float3 cv = make_float3((float)cx, (float)cy, (float)cz);
+                bn = sqrtf(dot3x(cv, cv)) / (APBF_FIX * tm) * a.b_sgl_factor;
+            } else {
+                bn = sgl * kw * a.b_sgl_factor + fmaxf(0.0f, under) * a.b_up_factor;
+            }
+            bn = bn >= 1.0f ? 1.0f : 0.0f;
+            float step = bn - b;
+            b = b + fminf(a.b_speed, fmaxf(-a.b_speed, step));
+            b = fminf(1.0f, b);
+        }
+        float lam = under / (ird * ird * (sqs + 0.01f));
+        lam /= a.rmin3 / ird * im;
+        a.lambda[i] = lam;
+        int4 sh = make_int4(0, 0, 0, 0);
+        if (lam < 0.0f) {
+            const float sc = lam * im * APBF_FIX;
+            sh.x = f2i(-wgs.x * ird * sc);
+            sh.y = f2i(-wgs.y * ird * sc);
+            sh.z = f2i(-wgs.z * ird * sc);
+        } else if (!(lam >= 0.0f)) {
+            set_flag(a.st, APBF_FLAG_NONFINITE);  // NaN lambda: no shift (int(NaN) = 0)
+        }
+        a.shift[i] = sh;
+        // incompressibility_3.comp:41-46,60: filter (only changes a non-zero boundariness)
+        if (a.method == 2 && b > 0.0f) {
+            float3 gi = make_float3((float)gx, (float)gy, (float)gz);
+            float gl = sqrtf(dot3x(gi, gi));
+            if (gl > 0.0f) {
+                float3 ed = make_float3(-gi.x / gl, -gi.y / gl, -gi.z / gl);
+                for (uint32_t k = 0; k < cnt; ++k) {
+                    const uint32_t j = a.idx[(size_t)k * a.stride + i];
+                    const float3 d = fdiff(p, a.pos[j]);
+                    float W;
+                    float3 g;
+                    pair_terms<GAUSS>(a.hk, a.gk, d, kw, c, W, g);
+                    float l = sqrtf(dot3x(g, g));
+                    if (!(l > 0.0f)) continue;
+                    float dd = ed.x * (g.x / l) + ed.y * (g.y / l) + ed.z * (g.z / l);
+                    if (dd > 0.6f) {
+                        b = 0.0f;
+                        break;
+                    }
+                }
+            }
+        }
+        a.bness[i] = b;
+        const double ratio = (double)density * (double)ird - 1.0;
+        e1 += ratio > 0.0 ? ratio : 0.0;
+        e2 += fabs(ratio);
+        if (a.dbg_dens) {
+            a.dbg_dens[i] = dens;
+            a.dbg_grad[i] = make_int4(gx, gy, gz, 0);
+            a.dbg_sq[i] = sq;
+        }
+    }
+    // deterministic block reduction of the error sums
+    __shared__ double s1[8], s2[8];
+    for (int off = 16; off > 0; off >>= 1) {
+        e1 += __shfl_down_sync(0xffffffffu, e1, off);
+        e2 += __shfl_down_sync(0xffffffffu, e2, off);
+    }
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        s1[w] = e1;
+        s2[w] = e2;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t1 = 0.0, t2 = 0.0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+            t1 += s1[k];
+            t2 += s2[k];
+        }
+        a.partials[2 * blockIdx.x] = t1;
+        a.partials[2 * blockIdx.x + 1] = t2;
+    }
+}
+
+struct PassB {
+    const int4 *pos;
+    int4 *pos_out;
+    const float *kw;
+    const float *lambda;
+    const int4 *shift;
+    const KConst *kc;
+    const uint32_t *count;
+    const uint32_t *idx;
+    const uint32_t *rcount;
+    const uint32_t *ridx;
+    uint32_t stride;
+    const uint32_t *d_len;
+    const Status *st;
+    int gk;
+};
+
+template <bool GAUSS>
+__global__ void __launch_bounds__(256) k_delta(PassB a) {
+    const uint32_t n = a.d_len[kLenParticles];
+    const bool sym = a.st->range_min == a.st->range_max;
+    const uint32_t *cnt_arr = sym ? a.count : a.rcount;
+    const uint32_t *idx_arr = sym ? a.idx : a.ridx;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const int4 p = a.pos[j];
+        const int4 sh = a.shift[j];
+        int32_t ax = sh.x, ay = sh.y, az = sh.z;
+        const uint32_t cnt = cnt_arr[j];
+        for (uint32_t k = 0; k < cnt; ++k) {
+            const uint32_t i = idx_arr[(size_t)k * a.stride + j];
+            const float lam = a.lambda[i];
+            if (!(lam < 0.0f)) continue;
+            const int4 q = a.pos[i];
+            const KConst c = a.kc[i];
+            const float3 d = fdiff(q, p);
+            const float r2 = dot3x(d, d);
+            float3 g;
+            if (GAUSS) {
+                g = kernel_gradient(1, d, r2, 0.0f, c, gauss_height(r2, c));
+            } else {
+                const float kwi = a.kw[i];
+                g = kernel_gradient(a.gk, d, r2, kwi, c, a.gk == 1 ? gauss_height(r2, c) : 0.0f);
+            }
+            const float sc = lam * APBF_FIX;
+            ax = wadd(ax, f2i(g.x * sc));
+            ay = wadd(ay, f2i(g.y * sc));
+            az = wadd(az, f2i(g.z * sc));
+        }
+        a.pos_out[j] = make_int4(wadd(p.x, ax), wadd(p.y, ay), wadd(p.z, az), p.w);
+    }
+}
+
+// Fixed-order (deterministic) sum of per-block partial pairs with one block of
+// 256 threads: thread t sums partials t, t+256, ... in order, then a fixed tree.
+__device__ __forceinline__ void block_sum2(const double *partials, int blocks, double &t1, double &t2) {
+    __shared__ double s1[256], s2[256];
+    double a = 0.0, b = 0.0;
+    for (int k = threadIdx.x; k < blocks; k += 256) {
+        a += partials[2 * k];
+        b += partials[2 * k + 1];
+    }
+    s1[threadIdx.x] = a;
+    s2[threadIdx.x] = b;
+    __syncthreads();
+    for (int off = 128; off > 0; off >>= 1) {
+        if ((int)threadIdx.x < off) {
+            s1[threadIdx.x] += s1[threadIdx.x + off];
+            s2[threadIdx.x] += s2[threadIdx.x + off];
+        }
+        __syncthreads();
+    }
+    t1 = s1[0];
+    t2 = s2[0];
+}
+
+__global__ void __launch_bounds__(256) k_finalize_error(const double *partials, int blocks, const uint32_t *d_len,
+                                                        double *out) {
+    double t1, t2;
+    block_sum2(partials, blocks, t1, t2);
+    if (threadIdx.x == 0) {
+        uint32_t n = d_len[kLenParticles];
+        out[2] = n ? t1 / n : 0.0;
+        out[3] = n ? t2 / n : 0.0;
+    }
+}
+
+__global__ void k_mass_volume(const float *inv_mass, const float *radius, const uint32_t *d_len, double *partials) {
+    const uint32_t n = d_len[kLenParticles];
+    double m = 0.0, v = 0.0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        m += 1.0 / (double)inv_mass[i];
+        double r = radius[i];
+        v += r * r * r;
+    }
+    __shared__ double s1[8], s2[8];
+    for (int off = 16; off > 0; off >>= 1) {
+        m += __shfl_down_sync(0xffffffffu, m, off);
+        v += __shfl_down_sync(0xffffffffu, v, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        s1[threadIdx.x >> 5] = m;
+        s2[threadIdx.x >> 5] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t1 = 0.0, t2 = 0.0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+            t1 += s1[k];
+            t2 += s2[k];
+        }
+        partials[2 * blockIdx.x] = t1;
+        partials[2 * blockIdx.x + 1] = t2;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_finalize_mass(const double *partials, int blocks, double *out) {
+    double t1, t2;
+    block_sum2(partials, blocks, t1, t2);
+    if (threadIdx.x == 0) {
+        out[0] = t1;
+        out[1] = t2;
+    }
+}
+
+}  // namespace
+
+apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s) {
+    const uint32_t cap = ctx->cfg.particle_capacity;
+    FluidBufs &f = ctx->fl[ctx->fcur];
+    FluidBufs &alt = ctx->fl[ctx->fcur ^ 1];
+    const apbf_settings &st = ctx->settings;
+    const bool gauss = st.height_kernel_id == 1 && st.gradient_kernel_id == 1;
+    PassA a;
+    a.pos = f.pos;
+    a.inv_mass = f.inv_mass;
+    a.radius = f.radius;
+    a.kw = f.kernel_width;
+    a.bness = f.boundariness;
+    a.count = ctx->nb_count;
+    a.idx = ctx->nb_idx;
+    a.stride = ctx->row_stride;
+    a.lambda = ctx->lambda;
+    a.shift = ctx->shift;
+    a.kc = ctx->kconst;
+    a.dbg_dens = ctx->debug ? ctx->dbg_density : nullptr;
+    a.dbg_grad = ctx->dbg_grad;
+    a.dbg_sq = ctx->dbg_sq;
+    a.partials = ctx->red_partials;
+    a.d_len = ctx->d_len;
+    a.st = ctx->status;
+    const float rm2 = 2.0f * st.smallest_target_radius;
+    a.rmin3 = rm2 * rm2 * rm2;
+    a.hk = st.height_kernel_id;
+    a.gk = st.gradient_kernel_id;
+    a.method = st.boundariness_calculation_method;
+    a.update_b = st.update_boundariness;
+    a.b_speed = st.boundariness_adaption_speed;
+    a.b_sgl_factor = st.boundariness_self_grad_length_factor;
+    a.b_up_factor = st.boundariness_underpressure_factor;
+    const int g = ctx->red_blocks;
+    APBF_BEFORE_LAUNCH(ctx, s, "k_density_lambda");
+    if (gauss)
+        k_density_lambda<true><<<g, kBlock, 0, s>>>(a);
+    else
+        k_density_lambda<false><<<g, kBlock, 0, s>>>(a);
+    APBF_AFTER_LAUNCH(ctx, s, "k_density_lambda");
+    APBF_BEFORE_LAUNCH(ctx, s, "k_finalize_error");
+    k_finalize_error<<<1, 256, 0, s>>>(ctx->red_partials, g, ctx->d_len, ctx->red_out);
+    APBF_AFTER_LAUNCH(ctx, s, "k_finalize_error");
+
+    PassB b;
+    b.pos = f.pos;
+    b.pos_out = alt.pos;
+    b.kw = f.kernel_width;
+    b.lambda = ctx->lambda;
+    b.shift = ctx->shift;
+    b.kc = ctx->kconst;
+    b.count = ctx->nb_count;
+    b.idx = ctx->nb_idx;
+    b.rcount = ctx->rev_count;
+    b.ridx = ctx->rev_idx;
+    b.stride = ctx->row_stride;
+    b.d_len = ctx->d_len;
+    b.st = ctx->status;
+    b.gk = st.gradient_kernel_id;
+    APBF_BEFORE_LAUNCH(ctx, s, "k_delta");
+    if (gauss)
+        k_delta<true><<<grid_for(ctx, cap), kBlock, 0, s>>>(b);
+    else
+        k_delta<false><<<grid_for(ctx, cap), kBlock, 0, s>>>(b);
+    APBF_AFTER_LAUNCH(ctx, s, "k_delta");
+    // the updated positions now live in the alternate buffer: swap position buffers
+    int4 *tmp = f.pos;
+    f.pos = alt.pos;
+    alt.pos = tmp;
+    return APBF_OK;
+}
+
+apbf_status reduce_fp64(apbf_ctx *ctx, double out[4], cudaStream_t s) {
+    FluidBufs &f = ctx->fl[ctx->fcur];
+    const int g = ctx->red_blocks;
+    // the error partials of the last density pass are already reduced into red_out[2..3]
+    APBF_BEFORE_LAUNCH(ctx, s, "k_mass_volume");
+    k_mass_volume<<<g, kBlock, 0, s>>>(f.inv_mass, f.radius, ctx->d_len, ctx->red_partials + 2 * g);
+    APBF_AFTER_LAUNCH(ctx, s, "k_mass_volume");
+    APBF_BEFORE_LAUNCH(ctx, s, "k_finalize_mass");
+    k_finalize_mass<<<1, 256, 0, s>>>(ctx->red_partials + 2 * g, g, ctx->red_out);
+    APBF_AFTER_LAUNCH(ctx, s, "k_finalize_mass");
+    APBF_CUDA(cudaMemcpyAsync(out, ctx->red_out, 4 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    APBF_CUDA(cudaStreamSynchronize(s));
+    return APBF_OK;
+}
+
+}  // namespace apbf

@@ -1,0 +1,394 @@
+"""Throughput benchmark of the adaptive PBF substep on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
+
+A "step" is one substep (pool::update, source/pool.cpp:67-106) of the workload's
+scene.  `value` is whole-job particle-substeps/s with the state resident in HBM;
+`e2e` is the same metric through the C ABI with the particle state coming from
+and going back to pinned host buffers every step.  Multi-GPU runs are replicas:
+every rank simulates its own copy of the scene (seeded by rank), no collective on
+the data path ("scaling": "weak").
+
+--impl reference times the CPU restatement of the reference's shader math (the
+oracle, single-threaded C) on every host core at once, as independent replicas of
+a bounded sample of the same scene.
+
+Rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "particle-substeps/s at <=0.1% density error: learned warm-start vs plain"
+UNIT = "particle-substeps/s"
+
+WORKLOADS = {
+    # name: (scene factory, description)
+    "water_drop_250k": ("water_drop", dict(total=250_000, basic_pbf=False)),
+    "water_drop_250k_plain": ("water_drop", dict(total=250_000, basic_pbf=True)),
+    "dam_break_32k": ("dam_break", dict(n_side=32)),
+}
+DEFAULT_WORKLOAD = "water_drop_250k_plain"
+
+
+def make_spec(name: str, seed: int = 0, scale: float = 1.0):
+    from apbf_gb300 import scenes
+
+    factory, kw = WORKLOADS[name]
+    kw = dict(kw)
+    if "total" in kw:
+        kw["total"] = int(kw["total"] * scale)
+    if factory == "dam_break":
+        return scenes.dam_break(seed=seed, **kw)
+    basic = kw.pop("basic_pbf")
+    return scenes.water_drop(seed=seed, basic_pbf=basic, **kw)
+
+
+def settings_dict(spec) -> dict:
+    from apbf_gb300.api import default_settings
+
+    s = default_settings()
+    s.basic_pbf = 1 if spec.basic_pbf else 0
+    s.solver_iterations = spec.iterations
+    return {f: getattr(s, f) for f, _ in s._fields_ if not f.startswith("pad")}
+
+
+# ----------------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------- roofline
+def algorithmic_bytes(kernel: str, n: int, pairs: int) -> float | None:
+    """Compulsory HBM bytes of one launch (inputs read once, outputs written once,
+    neighbour data counted once per particle, rows as 4 bytes per pair)."""
+    if kernel == "k_density_lambda":
+        return 28.0 * n + 4.0 * pairs  # 4N + 4P + 12N pos + 8N (invMass, kw) + 4N lambda
+    if kernel == "k_delta":
+        return 40.0 * n + 4.0 * pairs  # 4N + 4P + 12N + 4N lambda + 8N + 12N pos out
+    if kernel == "k_build_rows":
+        return 16.0 * n + 4.0 * n + 4.0 * pairs  # pos + range in, counts + rows out
+    return None
+
+
+def measured_peak() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_from_profiles(kernel: str, n: int, pairs: int) -> float | None:
+    """DRAM bytes per launch from the committed ncu summary (scaled to this launch's size)."""
+    p = ROOT / "profiles" / "ncu_traffic.md"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        f = [x.strip() for x in line.strip().strip("|").split("|")]
+        if len(f) >= 5 and f[0] == kernel:
+            try:
+                bytes_, n0, p0 = float(f[1]), float(f[2]), float(f[3])
+            except ValueError:
+                continue
+            a0 = algorithmic_bytes(kernel, int(n0), int(p0))
+            a1 = algorithmic_bytes(kernel, n, pairs)
+            return bytes_ * (a1 / a0) if a0 and a1 else None
+    return None
+
+
+# ----------------------------------------------------------------------------- CPU baseline
+def cpu_baseline(spec, budget_s: float = 15.0) -> dict:
+    from oracle import oracle as orc
+
+    fs = orc.FluidState(spec.state)
+    sc = orc.make_scene(orc.settings_from(settings_dict(spec)), spec.grid_min, spec.grid_max, spec.log2res,
+                        spec.acceleration)
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        orc.substep(fs, sc, (spec.box_min, spec.box_max), np.float32(spec.dt), int(spec.n * 64))
+        steps += 1
+        if time.perf_counter() - t0 > budget_s or steps >= 3:
+            break
+    el = time.perf_counter() - t0
+    return {"value": spec.n * steps / el, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{steps} substep(s) of the full {spec.n}-particle scene, single-threaded FP64 oracle, "
+                      f"{el:.1f} s"}
+
+
+def _replica_worker(args):
+    name, scale, seed, steps = args
+    sys.path.insert(0, str(ROOT))
+    from oracle import oracle as orc
+
+    spec = make_spec(name, seed=seed, scale=scale)
+    fs = orc.FluidState(spec.state)
+    sc = orc.make_scene(orc.settings_from(settings_dict(spec)), spec.grid_min, spec.grid_max, spec.log2res,
+                        spec.acceleration)
+    for _ in range(steps):
+        orc.substep(fs, sc, (spec.box_min, spec.box_max), np.float32(spec.dt), int(spec.n * 64))
+    return spec.n
+
+
+def run_reference(args) -> None:
+    import multiprocessing as mp
+
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    scale = 1.0 / 8.0  # bounded sample: the same scene at 1/8 of the particle count (lengths halved)
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        pool.map(_replica_worker, [(args.workload, scale, s, 1) for s in range(cores)])  # warm-up: load + 1 step
+        durations = []
+        n_sample = make_spec(args.workload, scale=scale).n
+        for _ in range(args.warmup):
+            pool.map(_replica_worker, [(args.workload, scale, s, 1) for s in range(cores)])
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            t1 = time.perf_counter()
+            pool.map(_replica_worker, [(args.workload, scale, s, 1) for s in range(cores)])
+            durations.append(time.perf_counter() - t1)
+        wall = time.perf_counter() - t0
+    value = n_sample * cores * args.steps / wall
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * wall / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded scene generator)",
+        "config": {"workload": args.workload, "sample_particles": n_sample, "replicas": cores},
+        "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{cores} independent replicas of the {n_sample}-particle sample of the scene, "
+                                   f"one substep each per step (the reference has no CPU implementation and "
+                                   f"cannot be built here; the oracle restates its shader math)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------- ours
+def run_ours(args) -> None:
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device(f"cuda:{local}"))
+    from apbf_gb300.api import Context
+
+    spec = make_spec(args.workload, seed=rank)
+    n = spec.n
+    cap = int(n * 1.25) + 1024
+    ctx = Context(particle_capacity=cap, max_neighbors=args.max_neighbors, max_log2res=max(spec.log2res, 3),
+                  device=local)
+    ctx.set_settings(basic_pbf=1 if spec.basic_pbf else 0, solver_iterations=args.iterations or spec.iterations)
+    ctx.set_scene(spec.grid_min, spec.grid_max, spec.log2res, spec.acceleration)
+    ctx.set_boxes(spec.box_min, spec.box_max)
+    ctx.upload(spec.state)
+    stream = torch.cuda.current_stream()
+
+    for _ in range(args.warmup):
+        ctx.substep(spec.dt)
+    ctx.check_status()
+    torch.cuda.synchronize()
+
+    # L2 (129 MB) flush between timed steps: the working set of a 250k scene fits in L2
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    ctx.profile_enable(True, 65536)
+    ctx.profile_read()  # clear
+    launches0 = ctx.launch_count()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    n_now = []
+    for k in range(args.steps):
+        flush.zero_()
+        ev[k][0].record(stream)
+        ctx.substep(spec.dt)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    launches = ctx.launch_count() - launches0
+    prof, dropped = ctx.profile_read()
+    ctx.profile_enable(False, 0)
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    info = ctx.check_status()
+    n_end, _ = ctx.lengths()
+    red = ctx.reduce_fp64()
+    total_ms = float(np.sum(step_ms))
+    particles_processed = n * args.steps
+    if dist:
+        t = torch.tensor([total_ms, particles_processed], dtype=torch.float64, device=f"cuda:{local}")
+        tmax = t.clone()
+        dist.all_reduce(tmax[:1], op=dist.ReduceOp.MAX)
+        dist.all_reduce(t[1:], op=dist.ReduceOp.SUM)
+        total_ms, particles_processed = float(tmax[0]), float(t[1])
+    value = particles_processed / (total_ms / 1000.0)
+
+    # roofline of the dominant kernel (largest share of the timed kernel time)
+    dom = max(prof.items(), key=lambda kv: kv[1][1]) if prof else None
+    roof = None
+    if dom:
+        name, (cnt, ms) = dom
+        per_launch_s = ms / cnt / 1000.0
+        alg = algorithmic_bytes(name, n, int(info.pairs))
+        peak, peak_kind = measured_peak()
+        if alg:
+            ach = alg / per_launch_s / 1e9
+            roof = {"kernel": name, "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                    "frac": ach / peak, "peak_source": peak_kind,
+                    "traffic": traffic_from_profiles(name, n, int(info.pairs)),
+                    "algorithmic_bytes": alg, "launch_us": per_launch_s * 1e6}
+    kernel_share = {k: round(v[1] / max(sum(x[1] for x in prof.values()), 1e-9), 4) for k, v in prof.items()}
+
+    # e2e: the same substep driven from pinned host buffers through the C ABI
+    e2e = run_e2e(ctx, spec, args, local)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(spec)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (int32 fixed-point positions and sums)",
+            "data": "synthetic (seeded scene generator)",
+            "config": {"workload": args.workload, "particles": n, "particles_after": int(n_end),
+                       "iterations": int(ctx.settings.solver_iterations), "dt": spec.dt,
+                       "adaptive": not spec.basic_pbf, "pairs": int(info.pairs),
+                       "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas x{world}",
+                       "density_error_last_iteration": float(red[2]), "abs_density_error": float(red[3])},
+            "roofline": roof, "kernel_share": kernel_share, "gpu_launches": int(launches),
+            "profiler_dropped": int(dropped), "clocks": clk, "e2e": e2e, "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def run_e2e(ctx, spec, args, local) -> dict:
+    """Per step: H2D of the full particle state from pinned host memory, one substep,
+    D2H of the full resulting state into pinned host memory."""
+    import torch
+
+    from apbf_gb300.api import FLUID_FIELDS
+
+    st, _ = ctx.download()
+    n = st["position"].shape[0]
+    host = {k: torch.from_numpy(np.ascontiguousarray(st[k]).view(np.int32 if FLUID_FIELDS[k][0] == torch.int32
+                                                                  else np.float32)).pin_memory()
+            for k in FLUID_FIELDS}
+    h2d = sum(t.numel() * 4 for t in host.values())
+    steps = max(3, min(args.steps, 10))
+    stream = torch.cuda.current_stream()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        v = ctx.fluid_view()
+        for k, t in host.items():
+            v[k][:n].copy_(t.view(v[k][:n].shape), non_blocking=True)
+        ctx.substep(spec.dt)
+        v = ctx.fluid_view()
+        for k, t in host.items():
+            t.view(v[k][:n].shape).copy_(v[k][:n], non_blocking=True)
+        stream.synchronize()
+    el = time.perf_counter() - t0
+    return {"value": n * steps / el, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(h2d),
+            "steps": steps}
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
+    ap.add_argument("--iterations", type=int, default=0)
+    ap.add_argument("--max-neighbors", type=int, default=192)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,256 @@
+/*
+ * apbf_gb300.h -- C ABI of the GB300-native adaptive PBF substep.
+ *
+ * This is the drop-in boundary for the hot path of cg-tuwien/APBF: the stage
+ * objects that scene code calls once per frame (pool::update, source/pool.cpp:67-106)
+ * -- neighbourhood search, incompressibility solve, kernel-width adaptation,
+ * split/merge and particle transfer -- plus the parallel primitives they use.
+ *
+ * Conventions, kept from the reference's device list model (source/gpu_list.h,
+ * source/gpu_list_data.h:8-14):
+ *  - Particle data is structure-of-arrays in device memory.  Positions are ivec4
+ *    (x, y, z, pad) in 2^18 fixed point (cpu_gpu_shared_config.h:7); velocities
+ *    are vec4.
+ *  - Every list length lives in device memory (a uint32_t), so a whole substep
+ *    runs without a host round trip and can be captured in a CUDA graph.
+ *    Capacities are fixed at apbf_create time (the reference's "requested length").
+ *  - The context owns all list buffers, like gpu_list owns pooled buffers.  Device
+ *    pointers returned by the *_view functions stay valid until the next call that
+ *    edits the lists (a neighbourhood search reorders particles into the alternate
+ *    buffer set; particle transfer and split/merge change lengths), exactly as
+ *    gpu_list::buffer() is "valid until another function of this object is called"
+ *    (source/indexed_list.h:40).
+ *  - Every stage call is asynchronous on the given stream and never synchronises.
+ *    Overflows and device-side failures are recorded in a device status word;
+ *    apbf_get_status() reads it (and synchronises the stream).
+ *  - Units are the reference's: lengths in particle radii of the smallest particle
+ *    (scenes use radius 1, source/main.cpp:63-68), kernel width 4 radii.
+ *
+ * All functions return an apbf_status.  No function throws or aborts.
+ */
+#ifndef APBF_GB300_H
+#define APBF_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define APBF_ABI_VERSION 1u
+#define APBF_POS_RESOLUTION 262144.0f /* cpu_gpu_shared_config.h:7 */
+#define APBF_KERNEL_SCALE 4.0f        /* cpu_gpu_shared_config.h:14 */
+#define APBF_MAX_TRANSFERS 10000u     /* cpu_gpu_shared_config.h:17 */
+#define APBF_MAX_BOXES 64u
+
+typedef enum apbf_status {
+    APBF_OK = 0,
+    APBF_ERR_INVALID_ARG = 1,
+    APBF_ERR_CAPACITY = 2,   /* a list overflowed; apbf_status_info.required_* says how much was needed */
+    APBF_ERR_NONFINITE = 3,  /* NaN / inf found in a position or lambda */
+    APBF_ERR_SPIN_LIMIT = 4, /* a device-side wait gave up (bounded spin) */
+    APBF_ERR_CUDA = 5,       /* a CUDA runtime call failed; apbf_last_error() has the text */
+    APBF_ERR_NOT_BUILT = 6
+} apbf_status;
+
+/* Device status flags (bit set in apbf_status_info.flags). */
+#define APBF_FLAG_NEIGHBOR_OVERFLOW 0x1u
+#define APBF_FLAG_TRANSFER_OVERFLOW 0x2u
+#define APBF_FLAG_PARTICLE_OVERFLOW 0x4u
+#define APBF_FLAG_SPIN_LIMIT 0x8u
+#define APBF_FLAG_NONFINITE 0x10u
+#define APBF_FLAG_GRID_OVERFLOW 0x20u
+
+/* Run-time switches: apbf_settings UBO (cpu_gpu_shared_config.h:74-94) plus the
+ * host-side pbd::settings that steer the substep (source/settings.cpp:5-31).
+ * apbf_default_settings() returns the reference defaults. */
+typedef struct apbf_settings {
+    int32_t height_kernel_id;   /* 0 cubic, 1 Gauss (default), 2 poly6, 3 cone, 4 quadratic spike */
+    int32_t gradient_kernel_id; /* 0 cubic, 1 Gauss (default), 2 spiky, 3 cone, 4 quadratic spike */
+    int32_t merge;
+    int32_t split;
+    int32_t base_kernel_width_on_target_radius;
+    int32_t base_kernel_width_on_boundary_distance;
+    int32_t update_target_radius;
+    int32_t update_boundariness;
+    int32_t boundariness_calculation_method; /* 0 gradient, 1 centre of mass, 2 gradient + filter */
+    int32_t basic_pbf;
+    int32_t solver_iterations;
+    int32_t pad0;
+    float boundariness_adaption_speed;
+    float kernel_width_adaption_speed;
+    float boundariness_self_grad_length_factor;
+    float boundariness_underpressure_factor;
+    float merge_duration;
+    float split_duration;
+    float smallest_target_radius;
+    float target_radius_offset;
+    float target_radius_scale_factor;
+    float pad1[3];
+} apbf_settings;
+
+/* Capacities (the reference's requested lengths, source/pool.cpp:7-15). */
+typedef struct apbf_config {
+    uint32_t particle_capacity;
+    uint32_t max_neighbors;     /* neighbour row capacity per particle */
+    uint32_t transfer_capacity; /* APBF_MAX_TRANSFERS in the reference */
+    uint32_t max_log2res;       /* largest grid resolution (bits per axis) the context may be asked for */
+    int32_t device;
+    uint32_t reserved[3];
+} apbf_config;
+
+/* Scene parameters used by apbf_substep (pool::update, source/pool.cpp:67-106) and
+ * by neighborhood_green::set_position_range (source/neighborhood_green.h:13). */
+typedef struct apbf_scene {
+    float min_pos[3];
+    float max_pos[3];
+    uint32_t log2res;
+    float acceleration[3];
+} apbf_scene;
+
+/* Particle and fluid lists: hidden_particles + fluid (source/list_definitions.h:9-14),
+ * one entry per particle (the fluid index list is the identity after every sort). */
+typedef struct apbf_fluid_view {
+    uint32_t capacity;
+    uint32_t *d_length;
+    int32_t *position;     /* int4 */
+    float *velocity;       /* float4 */
+    float *inverse_mass;
+    float *radius;
+    int32_t *pos_backup;   /* int4 */
+    uint32_t *transferring;
+    float *target_radius;
+    float *kernel_width;
+    float *boundariness;
+    uint32_t *boundary_distance;
+} apbf_fluid_view;
+
+/* transfers = indexed_list<hidden_transfers> (source/list_definitions.h:16-18). */
+typedef struct apbf_transfers_view {
+    uint32_t capacity;
+    uint32_t *d_length;
+    uint32_t *source;
+    uint32_t *target;
+    float *time_left; /* > 0 merge, <= 0 split (particle_transfer.comp:37-39) */
+} apbf_transfers_view;
+
+/* Neighbour rows, column-major ("transposed ELL"): the k-th neighbour of particle i
+ * is index[k * row_stride + i], for k < count[i].  This replaces the reference's
+ * unordered uvec2 pair list (source/list_definitions.h:20); apbf_export_pairs()
+ * produces that list. */
+typedef struct apbf_neighbors_view {
+    uint32_t row_stride;
+    uint32_t max_per_row;
+    uint32_t *count;
+    uint32_t *index;
+    unsigned long long *d_total; /* total pairs of the last search */
+} apbf_neighbors_view;
+
+typedef struct apbf_status_info {
+    uint32_t flags;
+    uint32_t required_neighbors; /* largest row seen when APBF_FLAG_NEIGHBOR_OVERFLOW is set */
+    uint32_t required_transfers;
+    uint32_t required_particles;
+    unsigned long long pairs;    /* pairs of the last neighbourhood search */
+} apbf_status_info;
+
+typedef struct apbf_ctx apbf_ctx;
+
+/* ---- lifetime and configuration ---- */
+uint32_t apbf_abi_version(void);
+const char *apbf_last_error(void);
+void apbf_default_settings(apbf_settings *out);                         /* source/settings.cpp:5-31 */
+apbf_status apbf_create(const apbf_config *cfg, apbf_ctx **out);
+apbf_status apbf_destroy(apbf_ctx *ctx);
+apbf_status apbf_set_settings(apbf_ctx *ctx, const apbf_settings *s);   /* settings.cpp:66-90 */
+apbf_status apbf_set_scene(apbf_ctx *ctx, const apbf_scene *scene);
+/* Axis-aligned collision boxes, vec4 min / vec4 max host arrays (user_controlled_boxes). */
+apbf_status apbf_set_boxes(apbf_ctx *ctx, const float *box_min4, const float *box_max4, uint32_t n);
+
+/* ---- list access (gpu_list::buffer / length, source/gpu_list.h) ---- */
+apbf_status apbf_fluid_get_view(apbf_ctx *ctx, apbf_fluid_view *out);
+apbf_status apbf_transfers_get_view(apbf_ctx *ctx, apbf_transfers_view *out);
+apbf_status apbf_neighbors_get_view(apbf_ctx *ctx, apbf_neighbors_view *out);
+/* gpu_list::set_length with a host value (source/gpu_list.h:85-90). */
+apbf_status apbf_set_lengths(apbf_ctx *ctx, uint32_t n_particles, uint32_t n_transfers, void *stream);
+/* Reads the device lengths (synchronises the stream). */
+apbf_status apbf_get_lengths(apbf_ctx *ctx, uint32_t *n_particles, uint32_t *n_transfers, void *stream);
+
+/* ---- stages (each replaces one reference stage's apply()) ---- */
+/* velocity_handling::apply (source/velocity_handling.cpp:15-31). */
+apbf_status apbf_velocity_handling_apply(apbf_ctx *ctx, float dt, const float acceleration[3], void *stream);
+/* neighborhood_green::set_range_scale / set_position_range / apply
+ * (source/neighborhood_green.h:11-14, source/neighborhood_green.cpp:27-77). */
+apbf_status apbf_neighborhood_green_apply(apbf_ctx *ctx, float range_scale, const float min_pos[3],
+                                          const float max_pos[3], uint32_t log2res, void *stream);
+/* box_collision::apply (source/box_collision.cpp:12-24). */
+apbf_status apbf_box_collision_apply(apbf_ctx *ctx, void *stream);
+/* incompressibility::apply, one Jacobi iteration (source/incompressibility.cpp:12-45). */
+apbf_status apbf_incompressibility_apply(apbf_ctx *ctx, void *stream);
+/* uint_to_float_with_indexed_lower_bound as called at source/pool.cpp:77-80. */
+apbf_status apbf_kernel_width_from_boundary_distance_apply(apbf_ctx *ctx, void *stream);
+/* spread_kernel_width::apply (source/spread_kernel_width.cpp:12-26). */
+apbf_status apbf_spread_kernel_width_apply(apbf_ctx *ctx, void *stream);
+/* update_transfers::apply (source/update_transfers.cpp:14-71). */
+apbf_status apbf_update_transfers_apply(apbf_ctx *ctx, void *stream);
+/* particle_transfer::apply (source/particle_transfer.cpp:10-28). */
+apbf_status apbf_particle_transfer_apply(apbf_ctx *ctx, float dt, void *stream);
+/* pool::update (source/pool.cpp:67-106): the whole substep with the scene set by
+ * apbf_set_scene and the iteration count of the settings. */
+apbf_status apbf_substep(apbf_ctx *ctx, float dt, void *stream);
+
+/* ---- results and diagnostics ---- */
+/* FP64 reductions into out[4] (host): total mass, total volume, mean compression
+ * error max(0, rho/rho0 - 1) and mean |rho/rho0 - 1| of the last density pass.
+ * No reference counterpart.  Synchronises the stream. */
+apbf_status apbf_reduce_fp64(apbf_ctx *ctx, double out[4], void *stream);
+/* Device status word (synchronises the stream); clears it when clear != 0. */
+apbf_status apbf_get_status(apbf_ctx *ctx, apbf_status_info *out, int clear, void *stream);
+/* The neighbour rows as the reference's uvec2 pair list (id, neighbour id); writes
+ * min(pairs, capacity_pairs) pairs and the pair count to *d_length. */
+apbf_status apbf_export_pairs(apbf_ctx *ctx, uint32_t *d_pairs, uint32_t capacity_pairs, uint32_t *d_length,
+                              void *stream);
+/* Enables (1) or disables (0) the capture of per-particle incompressibility
+ * intermediates read by apbf_debug_incompressibility (costs 24 bytes per particle
+ * of extra writes per iteration). */
+apbf_status apbf_set_debug(apbf_ctx *ctx, int enable);
+/* Per-particle intermediates of the last incompressibility iteration (debug):
+ * density and squared-gradient sums (2^18 fixed point), weighted gradient sums
+ * (int4), lambda.  Any pointer may be NULL. */
+apbf_status apbf_debug_incompressibility(apbf_ctx *ctx, uint32_t *d_density, int32_t *d_grad_sum4,
+                                         uint32_t *d_sq_grad_sum, float *d_lambda, void *stream);
+/* Sort permutation (new id -> old id) and sorted cell keys of the last neighbourhood search. */
+apbf_status apbf_debug_sort(apbf_ctx *ctx, uint32_t *d_perm, uint32_t *d_keys, void *stream);
+
+/* ---- tracing (replaces measurements::record_timing_interval_*, source/measurements.cpp:27-62) ---- */
+typedef struct apbf_kernel_time {
+    char name[48];
+    uint32_t launches;
+    uint32_t pad;
+    double total_ms; /* sum of CUDA-event durations on the launching stream */
+} apbf_kernel_time;
+/* Enables per-launch CUDA-event timing (capacity = events pairs kept until the
+ * next apbf_profile_read; launches beyond it are counted as dropped). */
+apbf_status apbf_profile_enable(apbf_ctx *ctx, int enable, uint32_t capacity);
+/* Synchronises the stream, aggregates the recorded launches per kernel name into
+ * out[0..*n_out) and clears the record. */
+apbf_status apbf_profile_read(apbf_ctx *ctx, apbf_kernel_time *out, uint32_t cap, uint32_t *n_out,
+                              unsigned long long *dropped, void *stream);
+/* Number of kernels this context has launched since creation. */
+apbf_status apbf_launch_count(apbf_ctx *ctx, unsigned long long *out);
+
+/* ---- parallel primitives (source/algorithms.h:12-17) ---- */
+/* algorithms::sort (source/algorithms.cpp:59-91): stable sort of (key, value) pairs
+ * by key; only key bits below the highest set bit of value_upper_bound are used.
+ * n is read from d_count; max_count bounds it. */
+apbf_status apbf_sort_pairs(apbf_ctx *ctx, const uint32_t *d_keys, const uint32_t *d_values, const uint32_t *d_count,
+                            uint32_t max_count, uint32_t value_upper_bound, uint32_t *d_out_keys,
+                            uint32_t *d_out_values, void *stream);
+/* algorithms::prefix_sum (source/algorithms.cpp:93-101): inclusive scan in place. */
+apbf_status apbf_prefix_sum(apbf_ctx *ctx, uint32_t *d_values, const uint32_t *d_count, uint32_t max_count,
+                            void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,1012 @@
+/*
+ * apbf_oracle.c -- CPU restatement of the APBF substep shaders (TEST INFRASTRUCTURE).
+ *
+ * This is the correctness oracle for the CUDA implementation; the product never
+ * links or calls it.  See apbf_oracle.h for the precision policy.  Build with
+ * -ffp-contract=off so that the FP32-emulated stages round exactly like the
+ * device code (which uses __fmul_rn / __fadd_rn where the order matters).
+ *
+ * Canonical rules (the reference is racy or undefined at these points; the
+ * CUDA path implements the same rules):
+ *  C1 cell of a position: clamp(floor((X - Xmin) * 2^L / (Xmax - Xmin)), 0, 2^L-1)
+ *     on 2^18 fixed-point int64 (reference: FP32 uint() conversion,
+ *     calculate_position_hash.comp:23-26, neighborhood_green.comp:35-37).
+ *  C2 neighbour predicate: j != i and |X_j - X_i|^2 <= R_i^2 in exact integers,
+ *     R_i = floor(kw_i * range_scale * 2^18) evaluated in FP64 from the FP32
+ *     inputs (reference: FP32 distance(), neighborhood_green.comp:83).
+ *  C3 sort: stable LSD by key from the identity permutation (test.cpp:335).
+ *  C4 float -> int conversions truncate toward zero and saturate; NaN -> 0
+ *     (GLSL int()/uint(); out-of-range is undefined in GLSL).
+ *  C5 fixed-point lengths in split/merge: floor(isqrt(int64 |d|^2))
+ *     (find_split_and_merge_1.comp:31, _2.comp:33 use FP32 length()).
+ *  C6 nearest-neighbour tie: smallest j (find_split_and_merge_2.comp:35-37 is
+ *     last-writer-wins); a particle without neighbours has no nearest neighbour
+ *     and does not merge (the reference reads an uninitialised entry).
+ *  C7 claims: sequential semantics in particle-index order
+ *     (find_split_and_merge_3.comp:94-121 races on atomicExchange); capacity
+ *     limits keep the first accepted transfers / splits in index order and
+ *     release the rest for this substep.
+ *  C8 append order of transfers, splits and list edits: index order.
+ *  C9 a split duplicate has inverse mass +inf (initialize_split_particles.comp:31
+ *     writes the undefined integer 1/0); particle_transfer then gives the target
+ *     inverse mass invMassS / factor, the limit of invMassS*invMassT*normFactor
+ *     (particle_transfer.comp:61 would produce inf*0 = NaN).
+ *  C10 pow(x, 3) in the merge test is x*x*x in FP32.
+ *  C11 the box-collision jitter uses the particle's sorted id
+ *      (box_collision.comp:46 uses the racy order of the pool's index list).
+ *  C12 quadratic-spike height uses (h - |r|)^2 for |r| < h (kernels.glsl:69
+ *      raises a negative base to pow(), which GLSL leaves undefined).
+ */
+#include "apbf_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define F32(x) ((double)(float)(x))
+static const double kPi = F32(3.14159265);          /* kernels.glsl:1 */
+static const double kTwoThirds = F32(2.0f / 3.0f);  /* 2.0f / DIMENSIONS */
+
+/* ------------------------------------------------------------------ */
+/* conversions (C4)                                                    */
+/* ------------------------------------------------------------------ */
+static int32_t f2i(double x) {
+    if (x != x) return 0;
+    if (x >= 2147483647.0) return INT32_MAX;
+    if (x <= -2147483648.0) return INT32_MIN;
+    return (int32_t)x; /* C truncates toward zero */
+}
+static uint32_t f2u(double x) {
+    if (x != x || x <= 0.0) return 0u;
+    if (x >= 4294967295.0) return UINT32_MAX;
+    return (uint32_t)x;
+}
+static int32_t f2i_f(float x) { return f2i((double)x); }
+static uint32_t f2u_f(float x) { return f2u((double)x); }
+static int32_t wrap_add(int32_t a, int32_t b) { return (int32_t)((uint32_t)a + (uint32_t)b); }
+
+/* ------------------------------------------------------------------ */
+/* primitives                                                          */
+/* ------------------------------------------------------------------ */
+
+/* Inclusive prefix sum (algorithms.cpp:93-118, prefix_sum_apply_on_block_level.comp). */
+void or_prefix_sum_inclusive(const uint32_t *in, uint32_t *out, size_t n) {
+    uint32_t s = 0;
+    for (size_t i = 0; i < n; ++i) {
+        s += in[i];
+        out[i] = s;
+    }
+}
+
+/* Stable key/value sort (algorithms.cpp:59-91): LSD passes of 8-bit digits. */
+void or_sort_pairs_stable(const uint32_t *keys, const uint32_t *vals, size_t n, uint32_t *out_keys,
+                          uint32_t *out_vals) {
+    uint32_t *ka = (uint32_t *)malloc((n ? n : 1) * sizeof(uint32_t));
+    uint32_t *va = (uint32_t *)malloc((n ? n : 1) * sizeof(uint32_t));
+    uint32_t *kb = (uint32_t *)malloc((n ? n : 1) * sizeof(uint32_t));
+    uint32_t *vb = (uint32_t *)malloc((n ? n : 1) * sizeof(uint32_t));
+    memcpy(ka, keys, n * sizeof(uint32_t));
+    memcpy(va, vals, n * sizeof(uint32_t));
+    for (int shift = 0; shift < 32; shift += 8) {
+        size_t count[257];
+        memset(count, 0, sizeof(count));
+        for (size_t i = 0; i < n; ++i) count[((ka[i] >> shift) & 255u) + 1]++;
+        for (int d = 0; d < 256; ++d) count[d + 1] += count[d];
+        for (size_t i = 0; i < n; ++i) {
+            size_t p = count[(ka[i] >> shift) & 255u]++;
+            kb[p] = ka[i];
+            vb[p] = va[i];
+        }
+        uint32_t *t = ka; ka = kb; kb = t;
+        t = va; va = vb; vb = t;
+    }
+    memcpy(out_keys, ka, n * sizeof(uint32_t));
+    memcpy(out_vals, va, n * sizeof(uint32_t));
+    free(ka); free(va); free(kb); free(vb);
+}
+
+/* gpu_list::apply_edit (gpu_list.h:125-135) via copy_scattered_read.comp:20-30. */
+void or_apply_edit_u32(const uint32_t *src, const uint32_t *edit, size_t n_edit, uint32_t stride_words,
+                       uint32_t *dst) {
+    for (size_t e = 0; e < n_edit; ++e)
+        for (uint32_t o = 0; o < stride_words; ++o) dst[e * stride_words + o] = src[(size_t)edit[e] * stride_words + o];
+}
+
+/* Edit list of indexed_list::delete_these (indexed_list.h:125-138): scattered_write
+ * marks deleted hidden entries with 0, prefix_sum, find_value_changes.comp:15-28
+ * emits the surviving hidden ids in increasing order.  Returns the new length. */
+uint32_t or_delete_edit_list(uint32_t n_hidden, const uint32_t *deleted, uint32_t n_deleted, uint32_t *edit) {
+    uint32_t *helper = (uint32_t *)calloc(n_hidden ? n_hidden : 1, sizeof(uint32_t));
+    for (uint32_t i = 0; i < n_hidden; ++i) helper[i] = 1u;
+    for (uint32_t k = 0; k < n_deleted; ++k) helper[deleted[k]] = 0u;
+    or_prefix_sum_inclusive(helper, helper, n_hidden);
+    uint32_t len = 0;
+    for (uint32_t id = 0; id < n_hidden; ++id) {
+        uint32_t cur = helper[id];
+        uint32_t prev = id == 0 ? 0u : helper[id - 1];
+        if (id == n_hidden - 1) len = cur;
+        if (cur != prev) edit[prev] = id;
+    }
+    free(helper);
+    return len;
+}
+
+/* indexed_list::apply_hidden_edit (indexed_list.h:288-308): after the hidden list
+ * is rebuilt from `edit` (new hidden id e takes old hidden id edit[e]), an index
+ * list pointing into the hidden list gets one entry e for every old entry equal
+ * to edit[e].  atomic_swap.comp chains equal entries and
+ * generate_new_index_and_edit_list.comp emits them with an atomic counter; the
+ * canonical order is by e, then by old position (C8).  new_edit (may be NULL)
+ * receives, per new entry, the old index-list position it came from.  Returns
+ * the new length (at most max_out). */
+uint32_t or_remap_index_list(const uint32_t *list, uint32_t n_list, const uint32_t *edit, uint32_t n_edit,
+                             uint32_t n_hidden_old, uint32_t *out, uint32_t *new_edit, uint32_t max_out) {
+    uint32_t *head = (uint32_t *)malloc((size_t)(n_hidden_old ? n_hidden_old : 1) * sizeof(uint32_t));
+    uint32_t *next = (uint32_t *)malloc((size_t)(n_list ? n_list : 1) * sizeof(uint32_t));
+    for (uint32_t h = 0; h < n_hidden_old; ++h) head[h] = UINT32_MAX;
+    for (uint32_t p = n_list; p-- > 0;) { /* build chains in increasing position order */
+        uint32_t h = list[p];
+        if (h >= n_hidden_old) continue;
+        next[p] = head[h];
+        head[h] = p;
+    }
+    uint32_t m = 0;
+    for (uint32_t e = 0; e < n_edit; ++e) {
+        uint32_t h = edit[e];
+        if (h >= n_hidden_old) continue;
+        for (uint32_t p = head[h]; p != UINT32_MAX; p = next[p]) {
+            if (m >= max_out) break;
+            out[m] = e;
+            if (new_edit) new_edit[m] = p;
+            ++m;
+        }
+    }
+    free(head);
+    free(next);
+    return m;
+}
+
+/* ------------------------------------------------------------------ */
+/* neighbour search                                                    */
+/* ------------------------------------------------------------------ */
+
+void or_fixed_bounds(const float minp[3], const float maxp[3], int64_t out_min[3], int64_t out_max[3]) {
+    for (int d = 0; d < 3; ++d) {
+        out_min[d] = (int64_t)llround((double)minp[d] * OR_POS_RESOLUTION);
+        out_max[d] = (int64_t)llround((double)maxp[d] * OR_POS_RESOLUTION);
+        if (out_max[d] <= out_min[d]) out_max[d] = out_min[d] + 1;
+    }
+}
+
+/* C1: cell coordinate of a fixed-point coordinate. */
+uint32_t or_cell_coord(int64_t x, int64_t xmin, int64_t xmax, uint32_t log2res) {
+    const int64_t cells = (int64_t)1 << log2res;
+    if (x <= xmin) return 0u;
+    if (x >= xmax) return (uint32_t)(cells - 1);
+    int64_t c = ((x - xmin) << log2res) / (xmax - xmin);
+    if (c > cells - 1) c = cells - 1;
+    return (uint32_t)c;
+}
+
+/* Z-order interleave, bit i of dimension d -> bit i*3+d (calculate_position_hash.comp:29-36). */
+uint32_t or_morton(const uint32_t c[3], uint32_t log2res) {
+    uint32_t r = 0u;
+    for (uint32_t i = 0; i < log2res; ++i)
+        for (uint32_t d = 0; d < 3; ++d) r += ((c[d] >> i) & 1u) << (i * 3u + d);
+    return r;
+}
+
+/* calculate_position_hash.comp:39-46 */
+void or_position_keys(const int32_t *pos4, size_t n, const float minp[3], const float maxp[3],
+                      uint32_t log2res, uint32_t *keys) {
+    int64_t lo[3], hi[3];
+    or_fixed_bounds(minp, maxp, lo, hi);
+    for (size_t i = 0; i < n; ++i) {
+        uint32_t c[3];
+        for (int d = 0; d < 3; ++d) c[d] = or_cell_coord(pos4[4 * i + d], lo[d], hi[d], log2res);
+        keys[i] = or_morton(c, log2res);
+    }
+}
+
+/* find_value_ranges.comp:15-31 with the zero fill of neighborhood_green.cpp:61-62. */
+void or_cell_ranges(const uint32_t *sorted_keys, size_t n, uint32_t ncells, uint32_t *start, uint32_t *end) {
+    memset(start, 0, (size_t)ncells * sizeof(uint32_t));
+    memset(end, 0, (size_t)ncells * sizeof(uint32_t));
+    for (size_t id = 0; id < n; ++id) {
+        uint32_t cur = sorted_keys[id];
+        uint32_t prev = id == 0 ? cur : sorted_keys[id - 1];
+        if (id == 0 || cur != prev) start[cur] = (uint32_t)id;
+        if (id != 0 && cur != prev) end[prev] = (uint32_t)id;
+        if (id == n - 1) end[cur] = (uint32_t)id + 1u;
+    }
+}
+
+/* C2: fixed-point search radius. */
+int64_t or_range_fixed(float kernel_width, float range_scale) {
+    double r = (double)kernel_width * (double)range_scale * OR_POS_RESOLUTION;
+    if (!(r >= 0.0)) return -1;
+    if (r > 4.0e18) r = 4.0e18;
+    return (int64_t)floor(r);
+}
+
+static int within(const int32_t *a, const int32_t *b, int64_t R) {
+    if (R < 0) return 0;
+    uint64_t s = 0;
+    for (int d = 0; d < 3; ++d) {
+        int64_t dd = (int64_t)b[d] - (int64_t)a[d];
+        if (dd < 0) dd = -dd;
+        if (dd > R) return 0;
+        s += (uint64_t)(dd * dd);
+    }
+    return s <= (uint64_t)R * (uint64_t)R;
+}
+
+static int cmp_u32(const void *a, const void *b) {
+    uint32_t x = *(const uint32_t *)a, y = *(const uint32_t *)b;
+    return x < y ? -1 : x > y;
+}
+
+/* neighborhood_green.comp:49-87: walk the cells overlapping [X - R, X + R]. */
+uint64_t or_neighbors_build(const int32_t *pos4, const float *range, float range_scale, size_t n,
+                            const float minp[3], const float maxp[3], uint32_t log2res,
+                            const uint32_t *cell_start, const uint32_t *cell_end, or_neighbors *nb) {
+    int64_t lo[3], hi[3];
+    or_fixed_bounds(minp, maxp, lo, hi);
+    uint64_t total = 0;
+    int write = 1;
+    nb->n = (uint32_t)n;
+    nb->offsets[0] = 0;
+    for (size_t i = 0; i < n; ++i) {
+        const int32_t *p = pos4 + 4 * i;
+        int64_t R = or_range_fixed(range[i], range_scale);
+        uint64_t row_begin = total;
+        if (R >= 0) {
+            uint32_t cmin[3], cmax[3];
+            for (int d = 0; d < 3; ++d) {
+                cmin[d] = or_cell_coord((int64_t)p[d] - R, lo[d], hi[d], log2res);
+                cmax[d] = or_cell_coord((int64_t)p[d] + R, lo[d], hi[d], log2res);
+            }
+            uint32_t c[3];
+            for (c[2] = cmin[2]; c[2] <= cmax[2]; ++c[2])
+                for (c[1] = cmin[1]; c[1] <= cmax[1]; ++c[1])
+                    for (c[0] = cmin[0]; c[0] <= cmax[0]; ++c[0]) {
+                        uint32_t key = or_morton(c, log2res);
+                        for (uint32_t j = cell_start[key]; j < cell_end[key]; ++j) {
+                            if (j == i) continue;
+                            if (!within(p, pos4 + 4 * (size_t)j, R)) continue;
+                            if (total >= nb->cap) write = 0;
+                            if (write) nb->idx[total] = j;
+                            ++total;
+                        }
+                    }
+        }
+        if (write) {
+            qsort(nb->idx + row_begin, (size_t)(total - row_begin), sizeof(uint32_t), cmp_u32);
+            nb->offsets[i + 1] = (uint32_t)total;
+        }
+    }
+    return total;
+}
+
+/* O(n^2) version of the same predicate, for tiny self-checks. */
+uint64_t or_neighbors_brute(const int32_t *pos4, const float *range, float range_scale, size_t n,
+                            or_neighbors *nb) {
+    uint64_t total = 0;
+    int write = 1;
+    nb->n = (uint32_t)n;
+    nb->offsets[0] = 0;
+    for (size_t i = 0; i < n; ++i) {
+        int64_t R = or_range_fixed(range[i], range_scale);
+        for (size_t j = 0; j < n; ++j) {
+            if (j == i || !within(pos4 + 4 * i, pos4 + 4 * j, R)) continue;
+            if (total >= nb->cap) write = 0;
+            if (write) nb->idx[total] = (uint32_t)j;
+            ++total;
+        }
+        if (write) nb->offsets[i + 1] = (uint32_t)total;
+    }
+    return total;
+}
+
+static void permute_f(float *a, const uint32_t *perm, size_t n, size_t w, void *tmp) {
+    float *t = (float *)tmp;
+    for (size_t k = 0; k < n; ++k) memcpy(t + k * w, a + (size_t)perm[k] * w, w * sizeof(float));
+    memcpy(a, t, n * w * sizeof(float));
+}
+static void permute_u(uint32_t *a, const uint32_t *perm, size_t n, size_t w, void *tmp) {
+    uint32_t *t = (uint32_t *)tmp;
+    for (size_t k = 0; k < n; ++k) memcpy(t + k * w, a + (size_t)perm[k] * w, w * sizeof(uint32_t));
+    memcpy(a, t, n * w * sizeof(uint32_t));
+}
+
+/* Gather every attribute by an edit list (new id -> old id), gpu_list.h:125-135. */
+static void fluid_apply_edit(or_fluid *f, const uint32_t *edit, uint32_t n_new) {
+    size_t m = n_new > f->n ? n_new : f->n;
+    void *tmp = malloc((m ? m : 1) * 16);
+    permute_u((uint32_t *)f->pos, edit, n_new, 4, tmp);
+    permute_f(f->vel, edit, n_new, 4, tmp);
+    permute_f(f->inv_mass, edit, n_new, 1, tmp);
+    permute_f(f->radius, edit, n_new, 1, tmp);
+    permute_u((uint32_t *)f->pos_backup, edit, n_new, 4, tmp);
+    permute_u(f->transferring, edit, n_new, 1, tmp);
+    permute_f(f->target_radius, edit, n_new, 1, tmp);
+    permute_f(f->kernel_width, edit, n_new, 1, tmp);
+    permute_f(f->boundariness, edit, n_new, 1, tmp);
+    permute_u(f->boundary_distance, edit, n_new, 1, tmp);
+    f->n = n_new;
+    free(tmp);
+}
+
+/* Remap transfer particle ids after a particle edit (indexed_list.h:288-308):
+ * a transfer survives iff both of its particles survive; order is kept (C8). */
+static void transfers_remap(or_transfers *t, const uint32_t *edit, uint32_t n_new, uint32_t n_old) {
+    if (!t || t->n == 0) return;
+    uint32_t *inv = (uint32_t *)malloc((n_old ? n_old : 1) * sizeof(uint32_t));
+    for (uint32_t i = 0; i < n_old; ++i) inv[i] = UINT32_MAX;
+    for (uint32_t k = 0; k < n_new; ++k)
+        if (inv[edit[k]] == UINT32_MAX) inv[edit[k]] = k;
+    uint32_t m = 0;
+    for (uint32_t k = 0; k < t->n; ++k) {
+        uint32_t s = t->source[k] < n_old ? inv[t->source[k]] : UINT32_MAX;
+        uint32_t g = t->target[k] < n_old ? inv[t->target[k]] : UINT32_MAX;
+        if (s == UINT32_MAX || g == UINT32_MAX) continue;
+        t->source[m] = s;
+        t->target[m] = g;
+        t->time_left[m] = t->time_left[k];
+        ++m;
+    }
+    t->n = m;
+    free(inv);
+}
+
+/* neighborhood_green::apply (neighborhood_green.cpp:27-77). */
+uint64_t or_neighborhood_green(or_fluid *f, or_transfers *t, float range_scale, const float minp[3],
+                               const float maxp[3], uint32_t log2res, or_neighbors *nb,
+                               uint32_t *perm_out, uint32_t *keys_out) {
+    size_t n = f->n;
+    uint32_t ncells = 1u << (3u * log2res);
+    uint32_t *keys = (uint32_t *)malloc((n ? n : 1) * sizeof(uint32_t));
+    uint32_t *seq = (uint32_t *)malloc((n ? n : 1) * sizeof(uint32_t));
+    uint32_t *skeys = (uint32_t *)malloc((n ? n : 1) * sizeof(uint32_t));
+    uint32_t *perm = (uint32_t *)malloc((n ? n : 1) * sizeof(uint32_t));
+    uint32_t *cs = (uint32_t *)malloc((size_t)ncells * sizeof(uint32_t));
+    uint32_t *ce = (uint32_t *)malloc((size_t)ncells * sizeof(uint32_t));
+    or_position_keys(f->pos, n, minp, maxp, log2res, keys);
+    for (size_t i = 0; i < n; ++i) seq[i] = (uint32_t)i;
+    or_sort_pairs_stable(keys, seq, n, skeys, perm);
+    fluid_apply_edit(f, perm, (uint32_t)n);
+    transfers_remap(t, perm, (uint32_t)n, (uint32_t)n);
+    or_cell_ranges(skeys, n, ncells, cs, ce);
+    uint64_t total = or_neighbors_build(f->pos, f->kernel_width, range_scale, n, minp, maxp, log2res, cs, ce, nb);
+    if (perm_out) memcpy(perm_out, perm, n * sizeof(uint32_t));
+    if (keys_out) memcpy(keys_out, skeys, n * sizeof(uint32_t));
+    free(keys); free(seq); free(skeys); free(perm); free(cs); free(ce);
+    return total;
+}
+
+/* ------------------------------------------------------------------ */
+/* smoothing kernels (kernels.glsl), FP64                              */
+/* ------------------------------------------------------------------ */
+static double dot3(const double a[3], const double b[3]) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+static double len3(const double a[3]) { return sqrt(dot3(a, a)); }
+
+static double gauss_height_param(double kw) {  /* kernels.glsl:104 */
+    double half = kw / 2.0;
+    return F32(0.6f) / (half * half * half);
+}
+static double gauss_height(const double r[3], double height) {  /* kernels.glsl:84-89 */
+    double ivw = pow(height, kTwoThirds);
+    double ivd = ivw * kPi;
+    return exp(-dot3(r, r) * ivd) * pow(ivw, 1.5);
+}
+
+double or_kernel_height(int id, const double r[3], double h) {
+    double dist = len3(r);
+    switch (id) {
+    case 0: { /* cubic, kernels.glsl:18-31 */
+        if (dist > h) return 0.0;
+        double q = dist / h;
+        double k = 8.0 / (kPi * h * h * h);
+        if (q <= 0.5) return k * (6.0 * q * q * q - 6.0 * q * q + 1.0);
+        return k * (2.0 * pow(1.0 - q, 3.0));
+    }
+    case 1: return gauss_height(r, gauss_height_param(h));
+    case 2: { /* poly6, kernels.glsl:3-9 */
+        double r2 = dot3(r, r), h2 = h * h;
+        if (r2 > h2) return 0.0;
+        return 315.0 * pow(h2 - r2, 3.0) / (64.0 * kPi * pow(h, 9.0));
+    }
+    case 3: { /* cone, kernels.glsl:48-52 */
+        double height = 3.0 / (kPi * pow(h, 3.0));
+        double v = (1.0 - dist / h) * height;
+        return v > 0.0 ? v : 0.0;
+    }
+    case 4: { /* quadratic spike, kernels.glsl:62-70 (C12) */
+        double a = 15.0 / (2.0 * kPi * pow(h, 5.0));
+        if (dist >= h) return 0.0;
+        return a * (h - dist) * (h - dist);
+    }
+    default: return 0.0;
+    }
+}
+
+void or_kernel_gradient(int id, const double r[3], double h, double out[3]) {
+    double dist = len3(r);
+    out[0] = out[1] = out[2] = 0.0;
+    switch (id) {
+    case 0: { /* kernels.glsl:33-46 */
+        if (dist > h || dist < F32(0.0001f)) return;
+        double q = dist / h;
+        double l = 48.0 / (kPi * h * h * h);
+        double s = q <= 0.5 ? l * q * (3.0 * q - 2.0) : l * (-(1.0 - q) * (1.0 - q));
+        double inv = 1.0 / (dist * h);
+        for (int d = 0; d < 3; ++d) out[d] = s * (r[d] * inv);
+        return;
+    }
+    case 1: { /* kernels.glsl:91-97 */
+        if (dist < F32(0.0001f)) return;
+        double height = gauss_height_param(h);
+        double ivd = pow(height, kTwoThirds) * kPi;
+        double s = -gauss_height(r, height) * 2.0 * dist * ivd;
+        for (int d = 0; d < 3; ++d) out[d] = s * (r[d] / dist);
+        return;
+    }
+    case 2: { /* spiky, kernels.glsl:11-16 */
+        if (dist > h || dist < F32(0.0001f)) return;
+        double s = -45.0 * (h - dist) * (h - dist) / (kPi * pow(h, 6.0));
+        for (int d = 0; d < 3; ++d) out[d] = s * (r[d] / dist);
+        return;
+    }
+    case 3: { /* cone, kernels.glsl:54-60 */
+        double st = 3.0 / (kPi * pow(h, 4.0));
+        if (dist > h || dist < F32(0.0001f)) return;
+        for (int d = 0; d < 3; ++d) out[d] = -r[d] * (st / dist);
+        return;
+    }
+    case 4: { /* kernels.glsl:72-82 */
+        if (dist > h || dist < F32(0.0001f)) return;
+        double a = 15.0 / (2.0 * kPi * pow(h, 5.0));
+        double m = h - dist;
+        if (m < 0.0) m = 0.0;
+        double s = -2.0 * a * m / dist;
+        for (int d = 0; d < 3; ++d) out[d] = s * r[d];
+        return;
+    }
+    default: return;
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* incompressibility (incompressibility.cpp:12-45), FP64               */
+/* ------------------------------------------------------------------ */
+static double move_towards_lin(double old_v, double new_v, double step) {  /* incompressibility_2.comp:37-41 */
+    double s = new_v - old_v;
+    if (s < -step) s = -step;
+    if (s > step) s = step;
+    return old_v + s;
+}
+
+void or_incompressibility_apply(or_fluid *f, const or_neighbors *nb, const or_settings *s, or_incomp_out *out) {
+    const uint32_t n = f->n;
+    uint32_t *dens = (uint32_t *)calloc(n ? n : 1, sizeof(uint32_t));
+    int32_t *gsum = (int32_t *)calloc(3 * (size_t)(n ? n : 1), sizeof(int32_t));
+    uint32_t *sq = (uint32_t *)calloc(n ? n : 1, sizeof(uint32_t));
+    int32_t *com = (int32_t *)calloc(4 * (size_t)(n ? n : 1), sizeof(int32_t));
+    double *lambda = (double *)calloc(n ? n : 1, sizeof(double));
+    int32_t *shift = (int32_t *)calloc(3 * (size_t)(n ? n : 1), sizeof(int32_t));
+    const double R = OR_POS_RESOLUTION;
+
+    /* incompressibility_0.comp:32-45 */
+    for (uint32_t i = 0; i < n; ++i) {
+        double zero[3] = {0, 0, 0};
+        dens[i] = f2u(or_kernel_height(s->height_kernel_id, zero, f->kernel_width[i]) / f->inv_mass[i] * R);
+    }
+    /* incompressibility_1.comp:37-69 (gather over row i; integer sums are order-free) */
+    for (uint32_t i = 0; i < n; ++i) {
+        const int32_t *p = f->pos + 4 * (size_t)i;
+        double kw = f->kernel_width[i];
+        for (uint32_t e = nb->offsets[i]; e < nb->offsets[i + 1]; ++e) {
+            uint32_t j = nb->idx[e];
+            const int32_t *q = f->pos + 4 * (size_t)j;
+            double imn = f->inv_mass[j];
+            double d[3], g[3];
+            for (int c = 0; c < 3; ++c) d[c] = (double)(int32_t)((uint32_t)q[c] - (uint32_t)p[c]) / R;
+            or_kernel_gradient(s->gradient_kernel_id, d, kw, g);
+            dens[i] += f2u(or_kernel_height(s->height_kernel_id, d, kw) / imn * R);
+            for (int c = 0; c < 3; ++c) gsum[3 * i + c] = wrap_add(gsum[3 * i + c], f2i(g[c] / imn * R));
+            sq[i] += f2u(dot3(g, g) / imn * R);
+            if (s->boundariness_calculation_method == 1) {
+                for (int c = 0; c < 3; ++c)
+                    com[4 * i + c] = wrap_add(com[4 * i + c],
+                                              f2i((double)(int32_t)((uint32_t)q[c] - (uint32_t)p[c]) / (imn * kw)));
+                com[4 * i + 3] = wrap_add(com[4 * i + 3], f2i(R / imn));
+            }
+        }
+    }
+    /* incompressibility_2.comp:71-110 */
+    for (uint32_t i = 0; i < n; ++i) {
+        double radius = f->radius[i], im = f->inv_mass[i], kw = f->kernel_width[i];
+        double ird = pow(2.0 * radius, 3.0) * im;
+        double density = (double)dens[i] / R;
+        double wgs[3] = {(double)gsum[3 * i] / R, (double)gsum[3 * i + 1] / R, (double)gsum[3 * i + 2] / R};
+        double sqs = (double)sq[i] / R;
+        double wgsq = dot3(wgs, wgs);
+        double sgl = sqrt(wgsq) * ird;
+        sqs += wgsq * im;
+        double under = 1.0 - density * ird;
+        if (s->update_boundariness) {
+            double b;
+            if (s->boundariness_calculation_method == 1) {
+                double tm = (double)com[4 * i + 3] / R + 1.0 / im;
+                double cv[3] = {(double)com[4 * i], (double)com[4 * i + 1], (double)com[4 * i + 2]};
+                b = len3(cv) / (R * tm) * (double)s->boundariness_self_grad_length_factor;
+            } else {
+                double up = under > 0.0 ? under : 0.0;
+                b = sgl * kw * (double)s->boundariness_self_grad_length_factor +
+                    up * (double)s->boundariness_underpressure_factor;
+            }
+            b = b >= 1.0 ? 1.0 : 0.0;
+            b = move_towards_lin((double)f->boundariness[i], b, (double)s->boundariness_adaption_speed);
+            f->boundariness[i] = (float)(b < 1.0 ? b : 1.0);
+        }
+        double lam = under / (ird * ird * (sqs + F32(0.01f)));
+        double rmin2 = 2.0 * (double)s->smallest_target_radius;
+        lam /= (rmin2 * rmin2 * rmin2) / ird * im;
+        lambda[i] = lam;
+        if (lam < 0.0) {
+            for (int c = 0; c < 3; ++c) shift[3 * i + c] = wrap_add(shift[3 * i + c], f2i(-wgs[c] * ird * (lam * im * R)));
+        }
+    }
+    /* incompressibility_3.comp:48-67 */
+    for (uint32_t i = 0; i < n; ++i) {
+        const int32_t *p = f->pos + 4 * (size_t)i;
+        double kw = f->kernel_width[i];
+        double gi[3] = {(double)gsum[3 * i], (double)gsum[3 * i + 1], (double)gsum[3 * i + 2]};
+        double gl = len3(gi);
+        for (uint32_t e = nb->offsets[i]; e < nb->offsets[i + 1]; ++e) {
+            uint32_t j = nb->idx[e];
+            const int32_t *q = f->pos + 4 * (size_t)j;
+            double d[3], g[3];
+            for (int c = 0; c < 3; ++c) d[c] = (double)(int32_t)((uint32_t)q[c] - (uint32_t)p[c]) / R;
+            or_kernel_gradient(s->gradient_kernel_id, d, kw, g);
+            if (s->boundariness_calculation_method == 2) {
+                double l = len3(g);
+                if (gl > 0.0 && l > 0.0) {
+                    double dd = 0.0;
+                    for (int c = 0; c < 3; ++c) dd += (-gi[c] / gl) * (g[c] / l);
+                    if (dd > F32(0.6f)) f->boundariness[i] = 0.0f;
+                }
+            }
+            if (!(lambda[i] < 0.0)) continue;
+            for (int c = 0; c < 3; ++c) shift[3 * j + c] = wrap_add(shift[3 * j + c], f2i(g[c] * (lambda[i] * R)));
+        }
+    }
+    for (uint32_t i = 0; i < n; ++i)
+        for (int c = 0; c < 3; ++c) f->pos[4 * i + c] = wrap_add(f->pos[4 * i + c], shift[3 * i + c]);
+    if (out) {
+        if (out->density) memcpy(out->density, dens, n * sizeof(uint32_t));
+        if (out->grad_sum) memcpy(out->grad_sum, gsum, 3 * (size_t)n * sizeof(int32_t));
+        if (out->sq_grad_sum) memcpy(out->sq_grad_sum, sq, n * sizeof(uint32_t));
+        if (out->lambda)
+            for (uint32_t i = 0; i < n; ++i) out->lambda[i] = (float)lambda[i];
+    }
+    free(dens); free(gsum); free(sq); free(com); free(lambda); free(shift);
+}
+
+/* ------------------------------------------------------------------ */
+/* substep glue, exact FP32                                            */
+/* ------------------------------------------------------------------ */
+static float fractf(float x) { return x - floorf(x); }
+
+/* box_collision.comp:20-25 (hash31, MIT-licensed shadertoy hash, restated). */
+static void hash31(float p, float out[3]) {
+    float p3[3] = {fractf(p * 0.1031f), fractf(p * 0.1030f), fractf(p * 0.0973f)};
+    float t = p3[0] * (p3[1] + 33.33f);
+    t = t + p3[1] * (p3[2] + 33.33f);
+    t = t + p3[2] * (p3[0] + 33.33f);
+    p3[0] += t; p3[1] += t; p3[2] += t;
+    out[0] = fractf((p3[0] + p3[1]) * p3[2]);
+    out[1] = fractf((p3[0] + p3[2]) * p3[1]);
+    out[2] = fractf((p3[1] + p3[2]) * p3[0]);
+}
+
+static void smallest_component(const float v[3], float m[3]) {  /* box_collision.comp:27-33 */
+    int b1 = v[0] <= v[1], b2 = v[0] <= v[2], b3 = v[1] <= v[2];
+    m[0] = (b1 && b2) ? 1.0f : 0.0f;
+    m[1] = (!b1 && b3) ? 1.0f : 0.0f;
+    m[2] = (!b2 && !b3) ? 1.0f : 0.0f;
+}
+
+/* box_collision.comp:35-60 */
+void or_box_collision(or_fluid *f, const or_boxes *b) {
+    for (uint32_t id = 0; id < f->n; ++id) {
+        int32_t *ip = f->pos + 4 * (size_t)id;
+        float pos[3] = {(float)ip[0] / 262144.0f, (float)ip[1] / 262144.0f, (float)ip[2] / 262144.0f};
+        float radius = f->radius[id];
+        for (uint32_t k = 0; k < b->n; ++k) {
+            float h1[3], h2[3], bmin[3], bmax[3], tmin[3], tmax[3], m1[3], m2[3], neg[3];
+            hash31(((float)id * pos[0] - pos[1]) - pos[2], h1);
+            hash31(((float)id * pos[1] + pos[0]) + pos[2], h2);
+            for (int c = 0; c < 3; ++c) {
+                bmin[c] = (b->bmin[4 * k + c] - radius) - h1[c] * 0.05f;
+                bmax[c] = (b->bmax[4 * k + c] + radius) + h2[c] * 0.05f;
+                tmin[c] = bmin[c] - pos[c];
+                tmax[c] = bmax[c] - pos[c];
+                neg[c] = -tmin[c];
+            }
+            smallest_component(neg, m1);
+            smallest_component(tmax, m2);
+            for (int c = 0; c < 3; ++c) {
+                tmin[c] *= m1[c];
+                tmax[c] *= m2[c];
+            }
+            float dmin = -((tmin[0] + tmin[1]) + tmin[2]);
+            float dmax = (tmax[0] + tmax[1]) + tmax[2];
+            if (dmin <= 0.0f || dmax <= 0.0f) continue;
+            for (int c = 0; c < 3; ++c) pos[c] += dmin < dmax ? tmin[c] : tmax[c];
+        }
+        for (int c = 0; c < 3; ++c) ip[c] = f2i_f(pos[c] * 262144.0f);
+    }
+}
+
+/* velocity_handling.cpp:15-31; infer_velocity.comp:30-31, apply_acceleration.comp:26-27,
+ * apply_velocity.comp:29-30. */
+void or_velocity_handling(or_fluid *f, float dt, float last_dt, const float accel[3]) {
+    if (dt == 0.0f) {
+        memcpy(f->pos_backup, f->pos, 16 * (size_t)f->n);
+        return;
+    }
+    float inv_den = last_dt * 262144.0f;
+    float a[3] = {accel[0] * dt, accel[1] * dt, accel[2] * dt};
+    float sc = dt * 262144.0f;
+    for (uint32_t i = 0; i < f->n; ++i) {
+        int32_t *p = f->pos + 4 * (size_t)i;
+        int32_t *bk = f->pos_backup + 4 * (size_t)i;
+        float *v = f->vel + 4 * (size_t)i;
+        for (int c = 0; c < 3; ++c) {
+            int32_t d = (int32_t)((uint32_t)p[c] - (uint32_t)bk[c]);
+            v[c] = (float)d / inv_den;
+        }
+        memcpy(bk, p, 16);
+        for (int c = 0; c < 3; ++c) {
+            v[c] = v[c] + a[c];
+            p[c] = wrap_add(p[c], f2i_f(v[c] * sc));
+        }
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* adaptive stages                                                     */
+/* ------------------------------------------------------------------ */
+
+/* move_towards of uint_to_float_*.comp (geometric step), FP32. */
+static float move_towards_geo(float old_v, float new_v, float step) {
+    float dir = (new_v > old_v) ? 1.0f : (new_v < old_v ? -1.0f : 0.0f);
+    float result = old_v * (1.0f + step * dir);
+    int reached = (old_v < new_v) != (result < new_v);
+    return reached ? new_v : result;
+}
+
+/* pool.cpp:77-80 -> uint_to_float_with_indexed_lower_bound.comp:31-45, FP32. */
+void or_kernel_width_from_boundary_distance(or_fluid *f, const or_settings *s) {
+    float factor = s->target_radius_scale_factor / 262144.0f;
+    for (uint32_t i = 0; i < f->n; ++i) {
+        float value = (float)f->boundary_distance[i] * factor;
+        float lb = f->radius[i] * 4.0f;
+        value = move_towards_geo(f->kernel_width[i], value, s->kernel_width_adaption_speed);
+        f->kernel_width[i] = fmaxf(value, lb);
+    }
+}
+
+static float len_fixed_f32(const int32_t *p, const int32_t *q) {
+    float d[3];
+    for (int c = 0; c < 3; ++c) d[c] = (float)(int32_t)((uint32_t)q[c] - (uint32_t)p[c]) / 262144.0f;
+    return sqrtf((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]);
+}
+
+/* spread_kernel_width.cpp:12-26 -> kernel_width_init.comp, kernel_width.comp,
+ * uint_to_float_but_gradual.comp; FP32.  Prunes nb rows in place (order kept). */
+void or_spread_kernel_width(or_fluid *f, or_neighbors *nb, const or_settings *s) {
+    uint32_t n = f->n;
+    uint32_t *ukw = (uint32_t *)malloc((n ? n : 1) * sizeof(uint32_t));
+    for (uint32_t i = 0; i < n; ++i) {
+        float tr = s->base_kernel_width_on_target_radius ? f->target_radius[i] : 0.0f;
+        float ok = fmaxf(f->radius[i], tr) * 4.0f;
+        ukw[i] = f2u_f(ok * 262144.0f);
+    }
+    uint32_t w = 0;
+    uint32_t row_start = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        float tr = s->base_kernel_width_on_target_radius ? f->target_radius[i] : 0.0f;
+        float ok = fmaxf(f->radius[i], tr) * 4.0f;
+        float cut = ok > f->kernel_width[i] ? ok : f->kernel_width[i];
+        uint32_t b = row_start, e = nb->offsets[i + 1];
+        row_start = e;
+        nb->offsets[i] = w;
+        for (uint32_t k = b; k < e; ++k) {
+            uint32_t j = nb->idx[k];
+            float dist = len_fixed_f32(f->pos + 4 * (size_t)i, f->pos + 4 * (size_t)j);
+            float dfk = dist - ok;
+            float t = dfk / (ok * 0.5f);
+            float infl = fmaxf(0.0f, 1.0f - fmaxf(0.0f, t));
+            uint32_t v = f2u_f((ok * infl) * 262144.0f);
+            if (v > ukw[j]) ukw[j] = v;
+            if (dist <= cut) nb->idx[w++] = j;
+        }
+    }
+    nb->offsets[n] = w;
+    for (uint32_t i = 0; i < n; ++i) {
+        float value = (float)ukw[i] * (1.0f / 262144.0f);
+        value = move_towards_geo(f->kernel_width[i], value, s->kernel_width_adaption_speed);
+        f->kernel_width[i] = fmaxf(value, -INFINITY);
+    }
+    free(ukw);
+}
+
+static uint32_t isqrt_u64(uint64_t x) {  /* floor(sqrt(x)) */
+    uint64_t r = (uint64_t)sqrt((double)x);
+    while (r * r > x) --r;
+    while ((r + 1) * (r + 1) <= x) ++r;
+    return (uint32_t)r;
+}
+static uint32_t fixed_dist(const int32_t *p, const int32_t *q) {  /* C5 */
+    uint64_t s = 0;
+    for (int c = 0; c < 3; ++c) {
+        int64_t d = (int64_t)q[c] - (int64_t)p[c];
+        s += (uint64_t)(d * d);
+    }
+    return isqrt_u64(s);
+}
+
+/* Constant of the split test, pow(2.0, 1.0 / DIMENSIONS) * 0.99 (find_split_and_merge_3.comp:90). */
+static float split_constant(void) { return (float)(cbrt(2.0) * 0.99); }
+
+/* update_transfers::apply (update_transfers.cpp:14-71). */
+void or_update_transfers(or_fluid *f, const or_neighbors *nb, or_transfers *t, const or_settings *s,
+                         uint32_t max_transfers) {
+    uint32_t n = f->n;
+    uint32_t *old_bd = (uint32_t *)malloc((n ? n : 1) * sizeof(uint32_t));
+    uint32_t *min_nd = (uint32_t *)malloc((n ? n : 1) * sizeof(uint32_t));
+    uint32_t *nearest = (uint32_t *)malloc((n ? n : 1) * sizeof(uint32_t));
+    uint32_t *splits = (uint32_t *)malloc((n ? n : 1) * sizeof(uint32_t));
+    memcpy(old_bd, f->boundary_distance, n * sizeof(uint32_t));
+    /* find_split_and_merge_1.comp:17-35 */
+    for (uint32_t i = 0; i < n; ++i) {
+        uint32_t bd = UINT32_MAX, md = UINT32_MAX;
+        for (uint32_t e = nb->offsets[i]; e < nb->offsets[i + 1]; ++e) {
+            uint32_t j = nb->idx[e];
+            uint32_t d = fixed_dist(f->pos + 4 * (size_t)i, f->pos + 4 * (size_t)j);
+            uint32_t c = old_bd[j] + d;
+            if (c < bd) bd = c;
+            if (d < md) md = d;
+        }
+        f->boundary_distance[i] = bd;
+        min_nd[i] = md;
+    }
+    /* find_split_and_merge_2.comp:19-38 (C6) */
+    for (uint32_t i = 0; i < n; ++i) {
+        nearest[i] = UINT32_MAX;
+        for (uint32_t e = nb->offsets[i]; e < nb->offsets[i + 1]; ++e) {
+            uint32_t j = nb->idx[e];
+            if (fixed_dist(f->pos + 4 * (size_t)i, f->pos + 4 * (size_t)j) == min_nd[i] && j < nearest[i]) nearest[i] = j;
+        }
+    }
+    /* find_split_and_merge_3.comp:46-122, FP32, claims in index order (C7) */
+    const float C = split_constant();
+    const float sf = s->target_radius_scale_factor;
+    uint32_t n_splits = 0, n_merges = 0;
+    uint32_t *msrc = (uint32_t *)malloc((n ? n : 1) * sizeof(uint32_t));
+    uint32_t *mtgt = (uint32_t *)malloc((n ? n : 1) * sizeof(uint32_t));
+    for (uint32_t id = 0; id < n; ++id) {
+        const int32_t *p = f->pos + 4 * (size_t)id;
+        float radius = f->radius[id];
+        float bdist = (float)f->boundary_distance[id] / 262144.0f;
+        float bness = f->boundariness[id];
+        uint32_t nn = nearest[id];
+        int has_nn = nn != UINT32_MAX;
+        float nnd = 0.0f, nnr = 0.0f;
+        int nn_larger = 0;
+        if (has_nn) {
+            float d[3];
+            for (int c = 0; c < 3; ++c) d[c] = (float)(int32_t)((uint32_t)f->pos[4 * (size_t)nn + c] - (uint32_t)p[c]);
+            nnd = sqrtf((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]) / 262144.0f;
+            nnr = f->radius[nn];
+            nn_larger = nnr > radius || (nnr == radius && nn > id);
+        }
+        float target;
+        if (s->update_target_radius) {
+            if (s->base_kernel_width_on_boundary_distance) {
+                target = (sf / (4.0f + 4.0f * sf)) * bdist;
+                target = fmaxf(target, s->smallest_target_radius);
+            } else {
+                target = s->smallest_target_radius + fmaxf(0.0f, (bdist - s->target_radius_offset) * sf);
+            }
+            f->target_radius[id] = target;
+        } else {
+            target = f->target_radius[id];
+        }
+        bness = bness >= 1.0f ? 1.0f : 0.0f;
+        f->boundary_distance[id] = f2u_f((bdist * (1.0f - bness) + radius * bness) * 262144.0f);
+        f->boundariness[id] = bness;
+
+        int split = s->split && (target * C <= radius);
+        int merge = s->merge && has_nn && nnd < radius &&
+                    (radius * radius * radius + nnr * nnr * nnr <= target * target * target);
+        if (!merge && !split) continue;
+        uint32_t src = (merge && nn_larger) ? nn : id;
+        uint32_t tgt = (merge && nn_larger) ? id : nn;
+        if (f->transferring[src] == 1u) continue;
+        f->transferring[src] = 1u;
+        if (merge) {
+            if (f->transferring[tgt] == 1u) {
+                f->transferring[src] = 0u;
+                continue;
+            }
+            f->transferring[tgt] = 1u;
+            msrc[n_merges] = src;
+            mtgt[n_merges] = tgt;
+            n_merges++;
+        } else {
+            splits[n_splits++] = id;
+        }
+    }
+    /* C7 capacity: keep the first accepted merges in index order, release the rest. */
+    {
+        uint32_t room = max_transfers > t->n ? max_transfers - t->n : 0u;
+        if (room > t->cap - t->n) room = t->cap - t->n;
+        for (uint32_t k = 0; k < n_merges; ++k) {
+            if (k < room) {
+                t->source[t->n] = msrc[k];
+                t->target[t->n] = mtgt[k];
+                t->time_left[t->n] = fmaxf(0.0001f, s->merge_duration);
+                t->n++;
+            } else {
+                f->transferring[msrc[k]] = 0u;
+                f->transferring[mtgt[k]] = 0u;
+            }
+        }
+    }
+    free(msrc); free(mtgt);
+    /* remove_impossible_splits.comp:29-45 */
+    if (s->split) {
+        uint32_t keep = n_splits;
+        uint32_t free_t = max_transfers > t->n ? max_transfers - t->n : 0u;
+        uint32_t free_p = f->cap > n ? f->cap - n : 0u;
+        if (keep > free_t) keep = free_t;
+        if (keep > free_p) keep = free_p;
+        for (uint32_t k = keep; k < n_splits; ++k) f->transferring[splits[k]] = 0u;
+        /* indexed_list::duplicate_these (indexed_list.h:140-152) + initialize_split_particles.comp */
+        uint32_t *edit = (uint32_t *)malloc((size_t)(n + keep ? n + keep : 1) * sizeof(uint32_t));
+        for (uint32_t i = 0; i < n; ++i) edit[i] = i;
+        for (uint32_t k = 0; k < keep; ++k) edit[n + k] = splits[k];
+        fluid_apply_edit(f, edit, n + keep);
+        for (uint32_t k = 0; k < keep; ++k) {
+            uint32_t d = n + k;
+            float r = f->radius[d];
+            f->pos[4 * (size_t)d] = wrap_add(f->pos[4 * (size_t)d], f2i_f((r * 262144.0f) * 0.1f));
+            f->radius[d] = 0.0f;
+            f->inv_mass[d] = INFINITY;
+            t->source[t->n] = splits[k];
+            t->target[t->n] = d;
+            t->time_left[t->n] = -s->split_duration;
+            t->n++;
+        }
+        free(edit);
+    } else {
+        for (uint32_t k = 0; k < n_splits; ++k) f->transferring[splits[k]] = 0u;
+    }
+    free(old_bd); free(min_nd); free(nearest); free(splits);
+}
+
+/* particle_transfer::apply (particle_transfer.cpp:10-28) + particle_transfer.comp:31-85.
+ * Volumes and masses in FP64; the time-left countdown in FP32 so that the step at
+ * which a transfer finishes matches the FP32 device path exactly. */
+void or_particle_transfer(or_fluid *f, or_transfers *t, float dt) {
+    uint32_t n = f->n;
+    uint32_t *del_p = (uint32_t *)malloc((t->n ? t->n : 1) * sizeof(uint32_t));
+    uint8_t *del_t = (uint8_t *)calloc(t->n ? t->n : 1, 1);
+    uint32_t nd = 0;
+    for (uint32_t k = 0; k < t->n; ++k) {
+        float tt = t->time_left[k];
+        float att = fabsf(tt);
+        float ttl = dt > att ? dt : att;
+        int merge = tt > 0.0f;
+        uint32_t S = t->source[k], T = t->target[k];
+        double rS = f->radius[S], rT = f->radius[T];
+        double imS = f->inv_mass[S], imT = f->inv_mass[T];
+        double volS = rS * rS * rS, volT = rT * rT * rT;
+        double factor = merge ? fmin(1.0, (double)dt / (double)ttl)
+                              : (double)dt * (volS - volT) / (2.0 * (double)ttl * volS);
+        double tv = factor * volS;
+        f->inv_mass[S] = (float)(imS / (1.0 - factor));
+        if (isinf(imT)) f->inv_mass[T] = (float)(imS / factor); /* C9 */
+        else f->inv_mass[T] = (float)(imS * imT / (imS + factor * imT));
+        f->radius[S] = (float)cbrt(volS - tv);
+        f->radius[T] = (float)cbrt(volT + tv);
+        t->time_left[k] = (ttl - dt) * (merge ? 1.0f : -1.0f);
+        if (ttl == dt) {
+            if (merge) del_p[nd++] = S;
+            else del_t[k] = 1;
+            f->transferring[S] = 0u;
+            f->transferring[T] = 0u;
+        }
+    }
+    /* deleteTransferList.delete_these() */
+    uint32_t m = 0;
+    for (uint32_t k = 0; k < t->n; ++k) {
+        if (del_t[k]) continue;
+        t->source[m] = t->source[k];
+        t->target[m] = t->target[k];
+        t->time_left[m] = t->time_left[k];
+        ++m;
+    }
+    t->n = m;
+    /* deleteParticleList.delete_these() */
+    if (nd) {
+        uint32_t *edit = (uint32_t *)malloc((n ? n : 1) * sizeof(uint32_t));
+        uint32_t nn = or_delete_edit_list(n, del_p, nd, edit);
+        fluid_apply_edit(f, edit, nn);
+        transfers_remap(t, edit, nn, n);
+        free(edit);
+    }
+    free(del_p); free(del_t);
+}
+
+/* Global reductions, FP64: mass, volume, mean compression error (no reference counterpart). */
+void or_reduce(const or_fluid *f, double out[3]) {
+    double m = 0.0, v = 0.0;
+    for (uint32_t i = 0; i < f->n; ++i) {
+        m += 1.0 / (double)f->inv_mass[i];
+        double r = f->radius[i];
+        v += r * r * r;
+    }
+    out[0] = m;
+    out[1] = v;
+    out[2] = 0.0;
+}
+
+/* Mean density error on the substep's neighbour list at the current positions:
+ * out[0] = mean max(0, rho_i / rho0_i - 1), out[1] = mean |rho_i / rho0_i - 1|
+ * (densities as incompressibility_0/1 compute them; rho0_i^-1 as
+ * incompressibility_2.comp:81).  No reference counterpart. */
+void or_density_error(const or_fluid *f, const or_neighbors *nb, const or_settings *s, double out[2]) {
+    const double R = OR_POS_RESOLUTION;
+    double e1 = 0.0, e2 = 0.0;
+    for (uint32_t i = 0; i < f->n; ++i) {
+        const int32_t *p = f->pos + 4 * (size_t)i;
+        double kw = f->kernel_width[i];
+        double zero[3] = {0, 0, 0};
+        uint32_t dens = f2u(or_kernel_height(s->height_kernel_id, zero, kw) / f->inv_mass[i] * R);
+        for (uint32_t e = nb->offsets[i]; e < nb->offsets[i + 1]; ++e) {
+            const int32_t *q = f->pos + 4 * (size_t)nb->idx[e];
+            double d[3];
+            for (int c = 0; c < 3; ++c) d[c] = (double)(int32_t)((uint32_t)q[c] - (uint32_t)p[c]) / R;
+            dens += f2u(or_kernel_height(s->height_kernel_id, d, kw) / f->inv_mass[nb->idx[e]] * R);
+        }
+        double ird = pow(2.0 * (double)f->radius[i], 3.0) * (double)f->inv_mass[i];
+        double ratio = (double)dens / R * ird - 1.0;
+        e1 += ratio > 0.0 ? ratio : 0.0;
+        e2 += fabs(ratio);
+    }
+    out[0] = f->n ? e1 / f->n : 0.0;
+    out[1] = f->n ? e2 / f->n : 0.0;
+}
+
+/* pool::update (pool.cpp:67-106). */
+uint64_t or_substep(or_fluid *f, or_transfers *t, or_neighbors *nb, const or_boxes *b, or_scene *sc, float dt) {
+    const or_settings *s = &sc->settings;
+    or_velocity_handling(f, dt, sc->last_dt, sc->accel);
+    if (dt != 0.0f) sc->last_dt = dt;
+    if (!s->basic_pbf && (s->merge || s->split)) or_particle_transfer(f, t, dt);
+    if (!s->basic_pbf && s->base_kernel_width_on_boundary_distance) or_kernel_width_from_boundary_distance(f, s);
+    float scale = (s->basic_pbf || s->base_kernel_width_on_boundary_distance) ? 1.0f : 1.5f;
+    uint64_t pairs = or_neighborhood_green(f, t, scale, sc->minp, sc->maxp, sc->log2res, nb, NULL, NULL);
+    if (pairs > nb->cap) return pairs;
+    if (!s->basic_pbf && !s->base_kernel_width_on_boundary_distance) or_spread_kernel_width(f, nb, s);
+    for (int it = 0; it < s->solver_iterations; ++it) {
+        or_box_collision(f, b);
+        or_incompressibility_apply(f, nb, s, NULL);
+    }
+    if (!s->basic_pbf) or_update_transfers(f, nb, t, s, sc->max_transfers);
+    return pairs;
+}
