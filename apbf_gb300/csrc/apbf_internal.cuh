@@ -142,7 +142,8 @@ struct apbf_ctx {
     uint32_t *nearest = nullptr;
     uint32_t *old_bd = nullptr;
     uint32_t *proposal = nullptr;  // per particle: packed proposal kind
-    uint32_t *claim = nullptr;     // per particle: min claimant
+    uint32_t *claim = nullptr;     // proposal list (particle ids in index order)
+    uint32_t *owner = nullptr;     // per particle: smallest claimant slot, all ones between calls
     uint32_t *decided = nullptr;
     uint32_t *flag_scan = nullptr;
     uint32_t *list_a = nullptr;

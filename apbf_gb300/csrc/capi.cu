@@ -166,6 +166,7 @@ apbf_status apbf_create(const apbf_config *cfg, apbf_ctx **out) {
     A(ctx->old_bd, cap);
     A(ctx->proposal, cap);
     A(ctx->claim, cap);
+    A(ctx->owner, cap);
     A(ctx->decided, cap);
     A(ctx->flag_scan, cap);
     A(ctx->list_a, cap);
@@ -181,6 +182,7 @@ apbf_status apbf_create(const apbf_config *cfg, apbf_ctx **out) {
     cudaMemset(ctx->status, 0, sizeof(Status));
     cudaMemset(ctx->red_out, 0, 4 * sizeof(double));
     cudaMemset(ctx->nb_count, 0, (size_t)cap * sizeof(uint32_t));
+    cudaMemset(ctx->owner, 0xff, (size_t)cap * sizeof(uint32_t));
     for (int k = 0; k < 2; ++k) {
         cudaMemset(ctx->fl[k].pos, 0, (size_t)cap * sizeof(int4));
         cudaMemset(ctx->fl[k].pos_backup, 0, (size_t)cap * sizeof(int4));

@@ -92,21 +92,26 @@ __global__ void k_cell_ranges(const uint32_t *__restrict__ skeys, const uint32_t
     }
 }
 
+// Canonical search radius: floor(kw * scale * 2^18) from the FP32 inputs, clamped
+// below 2^31 (positions are int32, so no distance needs more).
 __device__ __forceinline__ long long range_fixed(float kw, float scale) {
     double r = (double)kw * (double)scale * 262144.0;
     if (!(r >= 0.0)) return -1;
-    if (r > 4.0e18) r = 4.0e18;
+    if (r > 2147483647.0) r = 2147483647.0;
     return (long long)floor(r);
 }
 
+// |b - a|^2 <= R^2 exactly.  Once every |d| <= R < 2^31 is known, each square is
+// one 32x32 -> 64-bit multiply and the sum cannot overflow 64 bits.
 __device__ __forceinline__ bool within(int4 a, int4 b, long long R) {
     long long dx = (long long)b.x - a.x, dy = (long long)b.y - a.y, dz = (long long)b.z - a.z;
     dx = dx < 0 ? -dx : dx;
     dy = dy < 0 ? -dy : dy;
     dz = dz < 0 ? -dz : dz;
     if (dx > R || dy > R || dz > R) return false;
-    unsigned long long s = (unsigned long long)(dx * dx) + (unsigned long long)(dy * dy) + (unsigned long long)(dz * dz);
-    return s <= (unsigned long long)R * (unsigned long long)R;
+    const uint32_t ux = (uint32_t)dx, uy = (uint32_t)dy, uz = (uint32_t)dz, ur = (uint32_t)R;
+    unsigned long long s = (unsigned long long)ux * ux + (unsigned long long)uy * uy + (unsigned long long)uz * uz;
+    return s <= (unsigned long long)ur * ur;
 }
 
 // neighborhood_green.comp:49-87 with the canonical predicate; rows column-major.
@@ -139,13 +144,20 @@ __global__ void __launch_bounds__(256) k_build_rows(const int4 *__restrict__ pos
             for (uint32_t cz = z0; cz <= z1; ++cz)
                 for (uint32_t cy = y0; cy <= y1; ++cy)
                     for (uint32_t cx = x0; cx <= x1; ++cx) {
-                        uint32_t key = morton3(cx, cy, cz);
-                        uint32_t s = cstart[key], e = cend[key];
-                        for (uint32_t j = s; j < e; ++j) {
-                            if (j == i) continue;
-                            if (!within(p, pos[j], R)) continue;
-                            if (c < maxn) idx[(size_t)c * stride + i] = j;
-                            ++c;
+                        const uint32_t key = morton3(cx, cy, cz);
+                        const uint32_t s = cstart[key], e = cend[key];
+                        // candidates in batches of 4 loads
+                        for (uint32_t j0 = s; j0 < e; j0 += 4) {
+                            int4 q[4];
+#pragma unroll
+                            for (int u = 0; u < 4; ++u) q[u] = j0 + u < e ? pos[j0 + u] : p;
+#pragma unroll
+                            for (int u = 0; u < 4; ++u) {
+                                const uint32_t j = j0 + u;
+                                if (j >= e || j == i || !within(p, q[u], R)) continue;
+                                if (c < maxn) idx[(size_t)c * stride + i] = j;
+                                ++c;
+                            }
                         }
                     }
         }

@@ -63,8 +63,10 @@ __device__ __forceinline__ void pair_terms(int hk, int gk, float3 d, float kw, K
     }
 }
 
+constexpr int kUnroll = 4;
+
 template <bool GAUSS>
-__global__ void __launch_bounds__(256) k_density_lambda(PassA a) {
+__global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) {
     const uint32_t n = a.d_len[kLenParticles];
     double e1 = 0.0, e2 = 0.0;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -78,25 +80,41 @@ __global__ void __launch_bounds__(256) k_density_lambda(PassA a) {
         uint32_t sq = 0;
         int32_t cx = 0, cy = 0, cz = 0, cw = 0;
         const uint32_t cnt = a.count[i];
-        for (uint32_t k = 0; k < cnt; ++k) {
-            const uint32_t j = a.idx[(size_t)k * a.stride + i];
-            const int4 q = a.pos[j];
-            const float imn = a.inv_mass[j];
-            const float3 d = fdiff(p, q);
-            float W;
-            float3 g;
-            pair_terms<GAUSS>(a.hk, a.gk, d, kw, c, W, g);
-            dens += f2u(W / imn * APBF_FIX);
-            gx = wadd(gx, f2i(g.x / imn * APBF_FIX));
-            gy = wadd(gy, f2i(g.y / imn * APBF_FIX));
-            gz = wadd(gz, f2i(g.z / imn * APBF_FIX));
-            sq += f2u(dot3x(g, g) / imn * APBF_FIX);
-            if (a.method == 1) {  // incompressibility_1.comp:62-68
-                float den = imn * kw;
-                cx = wadd(cx, f2i((float)wadd(q.x, -p.x) / den));
-                cy = wadd(cy, f2i((float)wadd(q.y, -p.y) / den));
-                cz = wadd(cz, f2i((float)wadd(q.z, -p.z) / den));
-                cw = wadd(cw, f2i(APBF_FIX / imn));
+        const uint32_t *row = a.idx + i;
+        // Batches of kUnroll pairs: all row entries, then all neighbour gathers, then
+        // the arithmetic, so each thread keeps kUnroll loads in flight.
+        for (uint32_t k0 = 0; k0 < cnt; k0 += kUnroll) {
+            uint32_t jj[kUnroll];
+            int4 qq[kUnroll];
+            float mm[kUnroll];
+#pragma unroll
+            for (int u = 0; u < kUnroll; ++u) jj[u] = k0 + u < cnt ? row[(size_t)(k0 + u) * a.stride] : i;
+#pragma unroll
+            for (int u = 0; u < kUnroll; ++u) {
+                qq[u] = a.pos[jj[u]];
+                mm[u] = a.inv_mass[jj[u]];
+            }
+#pragma unroll
+            for (int u = 0; u < kUnroll; ++u) {
+                if (k0 + u >= cnt) break;
+                const int4 q = qq[u];
+                const float mj = __frcp_rn(mm[u]);  // mass of the neighbour (x / invMassN = x * mj)
+                const float3 d = fdiff(p, q);
+                float W;
+                float3 g;
+                pair_terms<GAUSS>(a.hk, a.gk, d, kw, c, W, g);
+                dens += f2u(W * mj * APBF_FIX);
+                gx = wadd(gx, f2i(g.x * mj * APBF_FIX));
+                gy = wadd(gy, f2i(g.y * mj * APBF_FIX));
+                gz = wadd(gz, f2i(g.z * mj * APBF_FIX));
+                sq += f2u(dot3x(g, g) * mj * APBF_FIX);
+                if (a.method == 1) {  // incompressibility_1.comp:62-68
+                    const float den = mm[u] * kw;
+                    cx = wadd(cx, f2i((float)wadd(q.x, -p.x) / den));
+                    cy = wadd(cy, f2i((float)wadd(q.y, -p.y) / den));
+                    cz = wadd(cz, f2i((float)wadd(q.z, -p.z) / den));
+                    cw = wadd(cw, f2i(APBF_FIX * mj));
+                }
             }
         }
         // incompressibility_2.comp:77-109
@@ -210,7 +228,7 @@ struct PassB {
 };
 
 template <bool GAUSS>
-__global__ void __launch_bounds__(256) k_delta(PassB a) {
+__global__ void __launch_bounds__(256, GAUSS ? 5 : 4) k_delta(PassB a) {
     const uint32_t n = a.d_len[kLenParticles];
     const bool sym = a.st->range_min == a.st->range_max;
     const uint32_t *cnt_arr = sym ? a.count : a.rcount;
@@ -220,25 +238,39 @@ __global__ void __launch_bounds__(256) k_delta(PassB a) {
         const int4 sh = a.shift[j];
         int32_t ax = sh.x, ay = sh.y, az = sh.z;
         const uint32_t cnt = cnt_arr[j];
-        for (uint32_t k = 0; k < cnt; ++k) {
-            const uint32_t i = idx_arr[(size_t)k * a.stride + j];
-            const float lam = a.lambda[i];
-            if (!(lam < 0.0f)) continue;
-            const int4 q = a.pos[i];
-            const KConst c = a.kc[i];
-            const float3 d = fdiff(q, p);
-            const float r2 = dot3x(d, d);
-            float3 g;
-            if (GAUSS) {
-                g = kernel_gradient(1, d, r2, 0.0f, c, gauss_height(r2, c));
-            } else {
-                const float kwi = a.kw[i];
-                g = kernel_gradient(a.gk, d, r2, kwi, c, a.gk == 1 ? gauss_height(r2, c) : 0.0f);
+        const uint32_t *row = idx_arr + j;
+        for (uint32_t k0 = 0; k0 < cnt; k0 += kUnroll) {
+            uint32_t ii[kUnroll];
+            float ll[kUnroll];
+            int4 qq[kUnroll];
+            KConst cc[kUnroll];
+            float hh[kUnroll];
+#pragma unroll
+            for (int u = 0; u < kUnroll; ++u) ii[u] = k0 + u < cnt ? row[(size_t)(k0 + u) * a.stride] : j;
+#pragma unroll
+            for (int u = 0; u < kUnroll; ++u) {
+                ll[u] = k0 + u < cnt ? a.lambda[ii[u]] : 0.0f;
+                qq[u] = a.pos[ii[u]];
+                cc[u] = a.kc[ii[u]];
+                hh[u] = GAUSS ? 0.0f : a.kw[ii[u]];
             }
-            const float sc = lam * APBF_FIX;
-            ax = wadd(ax, f2i(g.x * sc));
-            ay = wadd(ay, f2i(g.y * sc));
-            az = wadd(az, f2i(g.z * sc));
+#pragma unroll
+            for (int u = 0; u < kUnroll; ++u) {
+                const float lam = ll[u];
+                if (!(lam < 0.0f)) continue;  // incompressibility_3.comp:63 (also the padding lanes)
+                const float3 d = fdiff(qq[u], p);
+                const float r2 = dot3x(d, d);
+                float3 g;
+                if (GAUSS) {
+                    g = kernel_gradient(1, d, r2, 0.0f, cc[u], gauss_height(r2, cc[u]));
+                } else {
+                    g = kernel_gradient(a.gk, d, r2, hh[u], cc[u], a.gk == 1 ? gauss_height(r2, cc[u]) : 0.0f);
+                }
+                const float sc = lam * APBF_FIX;
+                ax = wadd(ax, f2i(g.x * sc));
+                ay = wadd(ay, f2i(g.y * sc));
+                az = wadd(az, f2i(g.z * sc));
+            }
         }
         a.pos_out[j] = make_int4(wadd(p.x, ax), wadd(p.y, ay), wadd(p.z, az), p.w);
     }

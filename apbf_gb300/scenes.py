@@ -97,15 +97,17 @@ def lattice(origin, counts, spacing: float, jitter: float, rng: np.random.Genera
     return p
 
 
-def _grid_for(lo, hi, kernel_width: float = 4.0, max_log2res: int = 9):
-    """Cubic Morton grid covering [lo, hi] whose cells are at least one kernel width wide."""
+def _grid_for(lo, hi, kernel_width: float = 4.0, max_log2res: int = 8):
+    """Cubic Morton grid covering [lo, hi] with the coarsest resolution whose cells
+    are at most one kernel width wide: a search then visits about (2h/c + 1)^3
+    cells of c^3/8 particles each, which keeps candidates per particle near
+    150-250 instead of the ~900 of cells twice as wide."""
     lo = np.asarray(lo, np.float64) - 4.0
     hi = np.asarray(hi, np.float64) + 4.0
     side = float(np.max(hi - lo))
     L = 1
-    while L < max_log2res and side / (1 << (L + 1)) >= kernel_width:
+    while L < max_log2res and side / (1 << L) > kernel_width:
         L += 1
-    side = max(side, kernel_width * (1 << L))
     return tuple(lo.tolist()), tuple((lo + side).tolist()), L
 
 

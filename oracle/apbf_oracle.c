@@ -12,8 +12,8 @@
  *     on 2^18 fixed-point int64 (reference: FP32 uint() conversion,
  *     calculate_position_hash.comp:23-26, neighborhood_green.comp:35-37).
  *  C2 neighbour predicate: j != i and |X_j - X_i|^2 <= R_i^2 in exact integers,
- *     R_i = floor(kw_i * range_scale * 2^18) evaluated in FP64 from the FP32
- *     inputs (reference: FP32 distance(), neighborhood_green.comp:83).
+ *     R_i = min(floor(kw_i * range_scale * 2^18), 2^31 - 1) evaluated in FP64 from
+ *     the FP32 inputs (reference: FP32 distance(), neighborhood_green.comp:83).
  *  C3 sort: stable LSD by key from the identity permutation (test.cpp:335).
  *  C4 float -> int conversions truncate toward zero and saturate; NaN -> 0
  *     (GLSL int()/uint(); out-of-range is undefined in GLSL).
@@ -225,7 +225,7 @@ void or_cell_ranges(const uint32_t *sorted_keys, size_t n, uint32_t ncells, uint
 int64_t or_range_fixed(float kernel_width, float range_scale) {
     double r = (double)kernel_width * (double)range_scale * OR_POS_RESOLUTION;
     if (!(r >= 0.0)) return -1;
-    if (r > 4.0e18) r = 4.0e18;
+    if (r > 2147483647.0) r = 2147483647.0; /* positions are int32: no distance needs more */
     return (int64_t)floor(r);
 }
 

@@ -23,6 +23,13 @@
  * Canonical rules where the reference is racy or undefined are listed in
  * apbf_oracle.c next to the code that implements them.
  *
+ * Pinning: the primitives and list edits are checked against every known-answer
+ * vector of the reference's source/test.cpp (tests/golden).  The reference has no
+ * test of its physics and cannot be run here, so for the neighbour search,
+ * kernels, incompressibility, kernel width, split/merge and transfer the oracle's
+ * parity with the reference is unpinned: it is a line-by-line restatement of the
+ * cited shaders, self-checked only.
+ *
  * Every fluid array is indexed by the same particle id (hidden-list order equals
  * fluid order, as it does in every reference scene after the neighbour sort).
  */
