@@ -172,6 +172,7 @@ SIGNATURES = {
                                 C.POINTER(C.c_ulonglong), _P]),
     "apbf_launch_count": (_ST, [_P, C.POINTER(C.c_ulonglong)]),
     "apbf_sort_pairs": (_ST, [_P, _P, _P, _P, C.c_uint32, C.c_uint32, _P, _P, _P]),
+    "apbf_sort_pairs_noalloc": (_ST, [_P, _P, _P, C.c_uint32, C.c_uint32, _P, _P, _P]),
     "apbf_prefix_sum": (_ST, [_P, _P, _P, C.c_uint32, _P]),
 }
 

@@ -15,6 +15,7 @@
 // Every wait on another tile is bounded (kSpinLimit) and records
 // APBF_FLAG_SPIN_LIMIT instead of hanging.
 #include <algorithm>
+#include <mutex>
 
 #include "apbf_internal.cuh"
 
@@ -303,3 +304,124 @@ apbf_status prefix_sum_device(apbf_ctx *ctx, uint32_t *d_values, const uint32_t 
 }
 
 }  // namespace apbf
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of the stable radix sort (apbf_sort_pairs_noalloc).
+//
+// Some callers cannot call cudaMalloc: a host whose device memory belongs to
+// another allocator, or a per-frame path on which cudaMalloc / cudaFree would
+// synchronise the device and stall the frame.  For them this entry point keeps
+// its scratch (the second key/value buffer, digit histograms, tile counters and
+// look-back words) in one file-scope device array of fixed size, so a call needs
+// no context and allocates nothing.  Every device that loads the library holds
+// the array (about 9 MB) until the process exits.
+namespace apbf {
+namespace {
+
+constexpr uint32_t kNoAllocMax = 1u << 20;  // largest max_count accepted
+constexpr uint32_t kNoAllocTiles = (kNoAllocMax + kSortTile - 1) / kSortTile;
+
+struct NoAllocScratch {
+    uint32_t keys[kNoAllocMax];
+    uint32_t vals[kNoAllocMax];
+    uint32_t hist[4 * 256];
+    uint32_t counters[8];
+    uint32_t tile_status[4 * kNoAllocTiles * 256];
+    Status status;
+};
+
+static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
+
+constexpr int kMaxDevices = 64;
+NoAllocScratch *g_noalloc_addr[kMaxDevices] = {};
+int g_noalloc_sms[kMaxDevices] = {};
+std::mutex g_noalloc_mutex;
+
+// Device address of the scratch array on the current device (looked up once per
+// device; a host-side use of g_noalloc_scratch would name host memory).
+apbf_status noalloc_scratch(int dev, NoAllocScratch **out, int *sms) {
+    if (dev < 0 || dev >= kMaxDevices) {
+        set_error("apbf_sort_pairs_noalloc: device ordinal out of range");
+        return APBF_ERR_INVALID_ARG;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_addr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_check(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+        int n = 0;
+        e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess) return cuda_check(e, "cudaDeviceGetAttribute");
+        g_noalloc_addr[dev] = (NoAllocScratch *)p;
+        g_noalloc_sms[dev] = n;
+    }
+    *out = g_noalloc_addr[dev];
+    *sms = g_noalloc_sms[dev];
+    return APBF_OK;
+}
+
+}  // namespace
+}  // namespace apbf
+
+extern "C" apbf_status apbf_sort_pairs_noalloc(const uint32_t *d_keys, const uint32_t *d_values,
+                                               const uint32_t *d_count, uint32_t max_count,
+                                               uint32_t value_upper_bound, uint32_t *d_out_keys,
+                                               uint32_t *d_out_values, void *stream) {
+    using namespace apbf;
+    if (!d_keys || !d_values || !d_count || !d_out_keys || !d_out_values) {
+        set_error("apbf_sort_pairs_noalloc: null pointer");
+        return APBF_ERR_INVALID_ARG;
+    }
+    if (max_count > kNoAllocMax) {
+        set_error("apbf_sort_pairs_noalloc: max_count above the fixed scratch size of 1048576 elements");
+        return APBF_ERR_INVALID_ARG;
+    }
+    if (d_keys == d_out_keys || d_keys == d_out_values || d_values == d_out_keys || d_values == d_out_values) {
+        set_error("apbf_sort_pairs_noalloc: inputs must not alias outputs");
+        return APBF_ERR_INVALID_ARG;
+    }
+    if (max_count == 0) return APBF_OK;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_check(e, "cudaGetDevice");
+    NoAllocScratch *sc = nullptr;
+    int sms = 0;
+    apbf_status r = noalloc_scratch(dev, &sc, &sms);
+    if (r != APBF_OK) return r;
+    cudaStream_t s = (cudaStream_t)stream;
+    uint32_t bits = 0;
+    for (uint32_t v = value_upper_bound; v; v >>= 1) ++bits;
+    uint32_t nib = (bits + 3u) / 4u;
+    if (nib > 8u) nib = 8u;
+    bits = nib * 4u;
+    const uint32_t key_mask = bits >= 32u ? 0xffffffffu : ((1u << bits) - 1u);
+    const int passes = (int)((bits + 7u) / 8u);
+    const uint32_t tiles = (max_count + kSortTile - 1) / kSortTile;
+    if (passes == 0) {
+        APBF_CUDA(cudaMemcpyAsync(d_out_keys, d_keys, (size_t)max_count * 4, cudaMemcpyDeviceToDevice, s));
+        APBF_CUDA(cudaMemcpyAsync(d_out_values, d_values, (size_t)max_count * 4, cudaMemcpyDeviceToDevice, s));
+        return APBF_OK;
+    }
+    // the array keeps the previous call's contents: clear what must start at zero
+    APBF_CUDA(cudaMemsetAsync(sc->hist, 0, sizeof(sc->hist), s));
+    APBF_CUDA(cudaMemsetAsync(sc->counters, 0, sizeof(sc->counters), s));
+    APBF_CUDA(cudaMemsetAsync(sc->tile_status, 0, (size_t)passes * tiles * 256 * sizeof(uint32_t), s));
+    APBF_CUDA(cudaMemsetAsync(&sc->status, 0, sizeof(Status), s));
+    uint64_t need = ((uint64_t)max_count + 255) / 256;
+    const int hist_grid = (int)std::min<uint64_t>(std::max<uint64_t>(need, 1), (uint64_t)sms * 4);
+    k_sort_hist<<<hist_grid, 256, 0, s>>>(d_keys, d_count, max_count, key_mask, passes, sc->hist);
+    APBF_CUDA(cudaGetLastError());
+    const uint32_t *src_k = d_keys, *src_v = d_values;
+    for (int p = 0; p < passes; ++p) {
+        const bool to_out = ((passes - 1 - p) & 1) == 0;
+        uint32_t *dk = to_out ? d_out_keys : sc->keys;
+        uint32_t *dv = to_out ? d_out_values : sc->vals;
+        k_onesweep<<<tiles, 256, 0, s>>>(src_k, src_v, dk, dv, d_count, max_count, key_mask, 8 * p,
+                                         sc->hist + p * 256, sc->counters + p,
+                                         sc->tile_status + (size_t)p * tiles * 256, &sc->status);
+        APBF_CUDA(cudaGetLastError());
+        src_k = dk;
+        src_v = dv;
+    }
+    return APBF_OK;
+}

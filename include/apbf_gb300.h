@@ -246,6 +246,21 @@ apbf_status apbf_launch_count(apbf_ctx *ctx, unsigned long long *out);
 apbf_status apbf_sort_pairs(apbf_ctx *ctx, const uint32_t *d_keys, const uint32_t *d_values, const uint32_t *d_count,
                             uint32_t max_count, uint32_t value_upper_bound, uint32_t *d_out_keys,
                             uint32_t *d_out_values, void *stream);
+/* The same stable sort as apbf_sort_pairs, but it allocates nothing and needs no
+ * context.  It has no counterpart in the reference.  It is meant for callers that
+ * cannot call cudaMalloc: hosts whose device memory is owned by another allocator,
+ * and per-frame code on which cudaMalloc / cudaFree would synchronise the device.
+ * Its scratch is one fixed array in the library's device memory, held on every
+ * device that loads the library until the process exits; max_count above
+ * 1048576 (1 << 20) is rejected with APBF_ERR_INVALID_ARG, as are inputs that
+ * alias outputs.  The first call on a device looks up that array's address on the
+ * current device; make that first call before any stream capture.  All calls
+ * share the array: calls whose work overlaps on the GPU (other streams, other
+ * threads) race and must be serialised by the caller.  A bounded look-back wait
+ * that gives up (which does not happen in normal operation) is not reported. */
+apbf_status apbf_sort_pairs_noalloc(const uint32_t *d_keys, const uint32_t *d_values, const uint32_t *d_count,
+                                    uint32_t max_count, uint32_t value_upper_bound, uint32_t *d_out_keys,
+                                    uint32_t *d_out_values, void *stream);
 /* algorithms::prefix_sum (source/algorithms.cpp:93-101): inclusive scan in place. */
 apbf_status apbf_prefix_sum(apbf_ctx *ctx, uint32_t *d_values, const uint32_t *d_count, uint32_t max_count,
                             void *stream);
