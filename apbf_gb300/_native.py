@@ -58,7 +58,8 @@ class Settings(C.Structure):
         ("smallest_target_radius", C.c_float),
         ("target_radius_offset", C.c_float),
         ("target_radius_scale_factor", C.c_float),
-        ("pad1", C.c_float * 3),
+        ("density_error_target", C.c_float),
+        ("pad1", C.c_float * 2),
     ]
 
 
@@ -126,6 +127,8 @@ class StatusInfo(C.Structure):
         ("required_transfers", C.c_uint32),
         ("required_particles", C.c_uint32),
         ("pairs", C.c_ulonglong),
+        ("density_passes", C.c_uint32),
+        ("pad", C.c_uint32),
     ]
 
 

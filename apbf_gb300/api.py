@@ -203,6 +203,8 @@ class Context:
             if name in ("transferring", "boundary_distance"):
                 a = a.view(np.uint32)
             out[name] = a.copy()
+            if name in ("position", "pos_backup"):
+                out[name][:, 3] = 0  # w is the library's scratch lane, not particle state
         tv = self.transfers_view()
         tr = {
             "source": tv["source"][:nt].cpu().numpy().view(np.uint32).copy(),

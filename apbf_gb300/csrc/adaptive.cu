@@ -539,8 +539,8 @@ apbf_status particle_transfer(apbf_ctx *ctx, float dt, cudaStream_t s) {
     TransferBufs &t = ctx->tr[ctx->tcur];
     uint32_t *pdel = ctx->flag_scan;   // per particle: deleted
     uint32_t *pscan = ctx->scan_tmp;   // per particle: inclusive scan of kept
-    uint32_t *tkeep = ctx->proposal;   // per transfer: kept
-    uint32_t *tscan = ctx->claim;      // per transfer: inclusive scan of kept
+    uint32_t *tkeep = ctx->t_keep;     // per transfer: kept
+    uint32_t *tscan = ctx->t_scan;     // per transfer: inclusive scan of kept
     APBF_CUDA(cudaMemsetAsync(pdel, 0, (size_t)cap * 4, s));
     APBF_BEFORE_LAUNCH(ctx, s, "k_transfer");
     k_transfer<<<grid_for(ctx, tcap), kBlock, 0, s>>>(f, t, pdel, tkeep, ctx->d_len, dt);

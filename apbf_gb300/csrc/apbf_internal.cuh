@@ -57,7 +57,10 @@ struct Status {
     unsigned long long range_max;
     uint32_t symmetric;            // 1 if every search radius was equal (rows are symmetric)
     uint32_t spin_where;
-    uint32_t pad[2];
+    uint32_t density_passes;       // density passes executed (not skipped after convergence)
+    uint32_t converged;            // set by a density pass whose error met the target
+    uint32_t done_blocks;          // last-block counter of the density pass reduction
+    uint32_t pad[3];
 };
 
 // Device length block.
@@ -75,7 +78,7 @@ enum LenSlot : uint32_t {
 // Per-particle Gauss-kernel constants computed once per density pass and reused
 // by the position-update pass (so both evaluate bit-identical gradients).
 struct KConst {
-    float ivd;   // invDoubleVariance (kernels.glsl:87)
+    float ivd;   // -invDoubleVariance * log2(e) (kernels.glsl:87), the exponent scale of exp2
     float norm;  // pow(invDoubleVarianceWithoutPi, D/2) (kernels.glsl:88)
 };
 
@@ -131,7 +134,7 @@ struct apbf_ctx {
 
     float *lambda = nullptr;
     int4 *shift = nullptr;
-    apbf::KConst *kconst = nullptr;
+    float4 *solve_rec = nullptr;   // per particle: lambda, Gauss constants (ivd, norm), kernel width
     uint32_t *dbg_density = nullptr;
     int4 *dbg_grad = nullptr;
     uint32_t *dbg_sq = nullptr;
@@ -149,6 +152,8 @@ struct apbf_ctx {
     uint32_t *list_a = nullptr;
     uint32_t *list_b = nullptr;
     uint32_t *scan_tmp = nullptr;
+    uint32_t *t_keep = nullptr;    // per transfer: kept after particle_transfer
+    uint32_t *t_scan = nullptr;    // per transfer: inclusive scan of t_keep
 
     double *red_partials = nullptr;
     double *red_out = nullptr;
@@ -228,10 +233,10 @@ apbf_status sort_pairs_device(apbf_ctx *ctx, const uint32_t *keys_in, const uint
 apbf_status prefix_sum_device(apbf_ctx *ctx, uint32_t *d_values, const uint32_t *d_count, uint32_t max_count,
                               cudaStream_t s);
 apbf_status neighborhood_green(apbf_ctx *ctx, float range_scale, const float minp[3], const float maxp[3],
-                               uint32_t log2res, cudaStream_t s);
+                               uint32_t log2res, cudaStream_t s, bool fuse_box = false);
 apbf_status velocity_handling(apbf_ctx *ctx, float dt, const float accel[3], cudaStream_t s);
 apbf_status box_collision(apbf_ctx *ctx, cudaStream_t s);
-apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s);
+apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s, bool box_after = false, bool converge = false);
 apbf_status kw_from_boundary_distance(apbf_ctx *ctx, cudaStream_t s);
 apbf_status spread_kernel_width(apbf_ctx *ctx, cudaStream_t s);
 apbf_status update_transfers(apbf_ctx *ctx, cudaStream_t s);
@@ -283,18 +288,20 @@ __device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a
 
 constexpr float kPiF = 3.14159265f;  // kernels.glsl:1
 
-// Gauss constants of a kernel width (kernels.glsl:84-89, 104).
+// Gauss constants of a kernel width (kernels.glsl:84-89, 104) in closed form:
+// height = 0.6 / (kw/2)^3, ivw = height^(2/3) = 0.6^(2/3) (2/kw)^2 and
+// norm = ivw^(3/2) = height (the reference's two pow() calls, without them).
 __device__ __forceinline__ KConst gauss_consts(float kw) {
     KConst c;
-    float half = kw / 2.0f;
-    float height = 0.6f / (half * half * half);
-    float ivw = powf(height, 2.0f / 3.0f);
-    c.ivd = ivw * kPiF;
-    c.norm = powf(ivw, 1.5f);
+    const float inv_half = 2.0f / kw;
+    const float ivw = 0.71137866089801251f * (inv_half * inv_half);
+    c.ivd = -(ivw * kPiF) * 1.44269504088896341f;
+    c.norm = 0.6f * (inv_half * inv_half * inv_half);
     return c;
 }
 
-__device__ __forceinline__ float gauss_height(float r2, KConst c) { return expf(-r2 * c.ivd) * c.norm; }
+// exp(-r2 * ivd) * norm as exp2 of a pre-scaled exponent (ivd holds -ivd * log2(e)).
+__device__ __forceinline__ float gauss_height(float r2, KConst c) { return exp2f(r2 * c.ivd) * c.norm; }
 
 // kernel_height (kernels.glsl:99-110).  r2 = dot(r, r).
 __device__ __forceinline__ float kernel_height(int kid, float r2, float h, KConst c) {
@@ -333,7 +340,8 @@ __device__ __forceinline__ float3 kernel_gradient(int kid, float3 r, float r2, f
     switch (kid) {
     case 1: {
         if (r2 < 1.0e-8f) return make_float3(0.f, 0.f, 0.f);  // dist < 0.0001
-        float s = -Wg * 2.0f * c.ivd;  // -W * 2 * dist * ivd * normalize(r) = -2 ivd W r
+        // -W * 2 * dist * ivd * normalize(r) = -2 ivd W r, with ivd = -c.ivd / log2(e)
+        float s = Wg * 2.0f * (c.ivd * 0.693147180559945309f);
         return make_float3(s * r.x, s * r.y, s * r.z);
     }
     case 0: {
@@ -367,6 +375,70 @@ __device__ __forceinline__ float3 kernel_gradient(int kid, float3 r, float r2, f
     }
     default: return make_float3(0.f, 0.f, 0.f);
     }
+}
+
+// ---- box collision (box_collision.comp:19-60), every operation rounded on its
+// own so that any translation unit reproduces the FP32 evaluation exactly ----
+__device__ __forceinline__ float fract_rn(float x) { return __fsub_rn(x, floorf(x)); }
+
+__device__ __forceinline__ float3 hash31_rn(float p) {  // shadertoy 4djSRW hash31 (MIT licence)
+    float3 q = make_float3(fract_rn(__fmul_rn(p, 0.1031f)), fract_rn(__fmul_rn(p, 0.1030f)),
+                           fract_rn(__fmul_rn(p, 0.0973f)));
+    float t = __fmul_rn(q.x, __fadd_rn(q.y, 33.33f));
+    t = __fadd_rn(t, __fmul_rn(q.y, __fadd_rn(q.z, 33.33f)));
+    t = __fadd_rn(t, __fmul_rn(q.z, __fadd_rn(q.x, 33.33f)));
+    q.x = __fadd_rn(q.x, t);
+    q.y = __fadd_rn(q.y, t);
+    q.z = __fadd_rn(q.z, t);
+    return make_float3(fract_rn(__fmul_rn(__fadd_rn(q.x, q.y), q.z)), fract_rn(__fmul_rn(__fadd_rn(q.x, q.z), q.y)),
+                       fract_rn(__fmul_rn(__fadd_rn(q.y, q.z), q.x)));
+}
+
+// Pushes one particle (sorted id `id`, radius r) out of every box.
+__device__ __forceinline__ int4 box_push(int4 ip, float r, uint32_t id, const float4 *__restrict__ bmin,
+                                         const float4 *__restrict__ bmax, uint32_t nb) {
+    if (nb == 0) return ip;
+    float px = __fdiv_rn((float)ip.x, 262144.0f), py = __fdiv_rn((float)ip.y, 262144.0f),
+          pz = __fdiv_rn((float)ip.z, 262144.0f);
+    const float fid = (float)id;
+    for (uint32_t k = 0; k < nb; ++k) {
+        const float3 h1 = hash31_rn(__fsub_rn(__fsub_rn(__fmul_rn(fid, px), py), pz));
+        const float3 h2 = hash31_rn(__fadd_rn(__fadd_rn(__fmul_rn(fid, py), px), pz));
+        const float4 lo = bmin[k], hi = bmax[k];
+        float tx0 = __fsub_rn(__fsub_rn(__fsub_rn(lo.x, r), __fmul_rn(h1.x, 0.05f)), px);
+        float ty0 = __fsub_rn(__fsub_rn(__fsub_rn(lo.y, r), __fmul_rn(h1.y, 0.05f)), py);
+        float tz0 = __fsub_rn(__fsub_rn(__fsub_rn(lo.z, r), __fmul_rn(h1.z, 0.05f)), pz);
+        float tx1 = __fsub_rn(__fadd_rn(__fadd_rn(hi.x, r), __fmul_rn(h2.x, 0.05f)), px);
+        float ty1 = __fsub_rn(__fadd_rn(__fadd_rn(hi.y, r), __fmul_rn(h2.y, 0.05f)), py);
+        float tz1 = __fsub_rn(__fadd_rn(__fadd_rn(hi.z, r), __fmul_rn(h2.z, 0.05f)), pz);
+        // smallestComponent(-toMin) and smallestComponent(toMax), box_collision.comp:27-33
+        {
+            const float vx = -tx0, vy = -ty0, vz = -tz0;
+            const bool b1 = vx <= vy, b2 = vx <= vz, b3 = vy <= vz;
+            tx0 = __fmul_rn(tx0, (b1 && b2) ? 1.0f : 0.0f);
+            ty0 = __fmul_rn(ty0, (!b1 && b3) ? 1.0f : 0.0f);
+            tz0 = __fmul_rn(tz0, (!b2 && !b3) ? 1.0f : 0.0f);
+        }
+        {
+            const bool b1 = tx1 <= ty1, b2 = tx1 <= tz1, b3 = ty1 <= tz1;
+            tx1 = __fmul_rn(tx1, (b1 && b2) ? 1.0f : 0.0f);
+            ty1 = __fmul_rn(ty1, (!b1 && b3) ? 1.0f : 0.0f);
+            tz1 = __fmul_rn(tz1, (!b2 && !b3) ? 1.0f : 0.0f);
+        }
+        const float dmin = -__fadd_rn(__fadd_rn(tx0, ty0), tz0);
+        const float dmax = __fadd_rn(__fadd_rn(tx1, ty1), tz1);
+        if (dmin <= 0.0f || dmax <= 0.0f) continue;
+        if (dmin < dmax) {
+            px = __fadd_rn(px, tx0);
+            py = __fadd_rn(py, ty0);
+            pz = __fadd_rn(pz, tz0);
+        } else {
+            px = __fadd_rn(px, tx1);
+            py = __fadd_rn(py, ty1);
+            pz = __fadd_rn(pz, tz1);
+        }
+    }
+    return make_int4(f2i(__fmul_rn(px, 262144.0f)), f2i(__fmul_rn(py, 262144.0f)), f2i(__fmul_rn(pz, 262144.0f)), ip.w);
 }
 
 #endif  // __CUDACC__

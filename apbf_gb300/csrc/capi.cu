@@ -150,13 +150,15 @@ apbf_status apbf_create(const apbf_config *cfg, apbf_ctx **out) {
     A(ctx->perm, cap);
     A(ctx->inv_perm, cap);
     A(ctx->scan_tmp, cap);
+    A(ctx->t_keep, tcap);
+    A(ctx->t_scan, tcap);
     const size_t ncells = (size_t)1 << (3 * cfg->max_log2res);
     A(ctx->cell_start, ncells);
     A(ctx->cell_end, ncells);
     ctx->n_cells_log2_alloc = cfg->max_log2res;
     A(ctx->lambda, cap);
     A(ctx->shift, cap);
-    A(ctx->kconst, cap);
+    A(ctx->solve_rec, cap);
     A(ctx->dbg_density, cap);
     A(ctx->dbg_grad, cap);
     A(ctx->dbg_sq, cap);
@@ -360,16 +362,26 @@ apbf_status apbf_substep(apbf_ctx *ctx, float dt, void *stream) {
         if (r != APBF_OK) return r;
     }
     const float scale = (st.basic_pbf || st.base_kernel_width_on_boundary_distance) ? 1.0f : 1.5f;
-    r = neighborhood_green(ctx, scale, ctx->scene.min_pos, ctx->scene.max_pos, ctx->scene.log2res, s);
+    // The box pass of each Jacobi iteration (pool.cpp:92-95) is fused into the kernel
+    // before it: the neighbour-row build for the first iteration (not when
+    // spread_kernel_width must still see the pre-box positions), the position
+    // update of the previous iteration for the others.
+    const bool spread = adaptive && !st.base_kernel_width_on_boundary_distance;
+    const bool fuse_first = st.solver_iterations > 0 && !spread;
+    r = neighborhood_green(ctx, scale, ctx->scene.min_pos, ctx->scene.max_pos, ctx->scene.log2res, s, fuse_first);
     if (r != APBF_OK) return r;
-    if (adaptive && !st.base_kernel_width_on_boundary_distance) {
+    if (spread) {
         r = spread_kernel_width(ctx, s);
         if (r != APBF_OK) return r;
     }
+    const bool converge = st.density_error_target > 0.0f;
+    if (converge) APBF_CUDA(cudaMemsetAsync(&ctx->status->converged, 0, sizeof(uint32_t), s));
     for (int it = 0; it < st.solver_iterations; ++it) {
-        r = box_collision(ctx, s);
-        if (r != APBF_OK) return r;
-        r = incompressibility(ctx, s);
+        if (it == 0 && !fuse_first) {
+            r = box_collision(ctx, s);
+            if (r != APBF_OK) return r;
+        }
+        r = incompressibility(ctx, s, it + 1 < st.solver_iterations, converge);
         if (r != APBF_OK) return r;
     }
     if (adaptive) {
@@ -397,11 +409,13 @@ apbf_status apbf_get_status(apbf_ctx *ctx, apbf_status_info *out, int clear, voi
     out->required_transfers = hs.required_transfers;
     out->required_particles = hs.required_particles;
     out->pairs = pairs;
+    out->density_passes = hs.density_passes;
     if (clear) {
         Status z = hs;
         z.flags = 0;
         z.required_neighbors = z.required_transfers = z.required_particles = 0;
         z.spin_where = 0;
+        z.density_passes = 0;
         APBF_CUDA(cudaMemcpyAsync(ctx->status, &z, sizeof(Status), cudaMemcpyHostToDevice, s));
         APBF_CUDA(cudaStreamSynchronize(s));
     }

@@ -40,56 +40,11 @@ __global__ void k_backup(FluidBufs f, const uint32_t *d_len) {
         f.pos_backup[i] = f.pos[i];
 }
 
-__device__ __forceinline__ float fractf(float x) { return x - floorf(x); }
-
-// box_collision.comp:19-25 (hash31 from shadertoy 4djSRW, MIT licence).
-__device__ __forceinline__ float3 hash31(float p) {
-    float3 p3 = make_float3(fractf(p * 0.1031f), fractf(p * 0.1030f), fractf(p * 0.0973f));
-    float t = p3.x * (p3.y + 33.33f);
-    t = t + p3.y * (p3.z + 33.33f);
-    t = t + p3.z * (p3.x + 33.33f);
-    p3.x += t;
-    p3.y += t;
-    p3.z += t;
-    return make_float3(fractf((p3.x + p3.y) * p3.z), fractf((p3.x + p3.z) * p3.y), fractf((p3.y + p3.z) * p3.x));
-}
-
-__device__ __forceinline__ float3 smallest_component(float3 v) {  // box_collision.comp:27-33
-    bool b1 = v.x <= v.y, b2 = v.x <= v.z, b3 = v.y <= v.z;
-    return make_float3((b1 && b2) ? 1.0f : 0.0f, (!b1 && b3) ? 1.0f : 0.0f, (!b2 && !b3) ? 1.0f : 0.0f);
-}
-
 __global__ void k_box_collision(int4 *pos, const float *radius, const uint32_t *d_len, const float4 *bmin,
                                 const float4 *bmax, uint32_t nb) {
     const uint32_t n = d_len[kLenParticles];
-    for (uint32_t id = blockIdx.x * blockDim.x + threadIdx.x; id < n; id += gridDim.x * blockDim.x) {
-        const int4 ip = pos[id];
-        float3 p = make_float3((float)ip.x / 262144.0f, (float)ip.y / 262144.0f, (float)ip.z / 262144.0f);
-        const float r = radius[id];
-        for (uint32_t k = 0; k < nb; ++k) {
-            const float fid = (float)id;
-            const float3 h1 = hash31((fid * p.x - p.y) - p.z);
-            const float3 h2 = hash31((fid * p.y + p.x) + p.z);
-            const float4 lo = bmin[k], hi = bmax[k];
-            float3 tmin = make_float3(((lo.x - r) - h1.x * 0.05f) - p.x, ((lo.y - r) - h1.y * 0.05f) - p.y,
-                                      ((lo.z - r) - h1.z * 0.05f) - p.z);
-            float3 tmax = make_float3(((hi.x + r) + h2.x * 0.05f) - p.x, ((hi.y + r) + h2.y * 0.05f) - p.y,
-                                      ((hi.z + r) + h2.z * 0.05f) - p.z);
-            const float3 m1 = smallest_component(make_float3(-tmin.x, -tmin.y, -tmin.z));
-            const float3 m2 = smallest_component(tmax);
-            tmin = make_float3(tmin.x * m1.x, tmin.y * m1.y, tmin.z * m1.z);
-            tmax = make_float3(tmax.x * m2.x, tmax.y * m2.y, tmax.z * m2.z);
-            const float dmin = -((tmin.x + tmin.y) + tmin.z);
-            const float dmax = (tmax.x + tmax.y) + tmax.z;
-            if (dmin <= 0.0f || dmax <= 0.0f) continue;
-            if (dmin < dmax) {
-                p.x += tmin.x; p.y += tmin.y; p.z += tmin.z;
-            } else {
-                p.x += tmax.x; p.y += tmax.y; p.z += tmax.z;
-            }
-        }
-        pos[id] = make_int4(f2i(p.x * 262144.0f), f2i(p.y * 262144.0f), f2i(p.z * 262144.0f), ip.w);
-    }
+    for (uint32_t id = blockIdx.x * blockDim.x + threadIdx.x; id < n; id += gridDim.x * blockDim.x)
+        pos[id] = box_push(pos[id], radius[id], id, bmin, bmax, nb);
 }
 
 __device__ __forceinline__ float move_towards_geo(float old_v, float new_v, float step) {

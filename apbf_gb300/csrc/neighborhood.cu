@@ -51,7 +51,9 @@ __global__ void k_reorder(FluidBufs src, FluidBufs dst, const uint32_t *__restri
     uint32_t n = d_len[kLenParticles];
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         uint32_t o = perm[k];
-        dst.pos[k] = src.pos[o];
+        int4 p = src.pos[o];
+        p.w = __float_as_int(1.0f / src.inv_mass[o]);  // the solver's per-particle mass (position.w is reserved)
+        dst.pos[k] = p;
         dst.vel[k] = src.vel[o];
         dst.inv_mass[k] = src.inv_mass[o];
         dst.radius[k] = src.radius[o];
@@ -114,73 +116,135 @@ __device__ __forceinline__ bool within(int4 a, int4 b, long long R) {
     return s <= (unsigned long long)ur * ur;
 }
 
-// neighborhood_green.comp:49-87 with the canonical predicate; rows column-major.
-__global__ void __launch_bounds__(256) k_build_rows(const int4 *__restrict__ pos, const float *__restrict__ range,
-                                                    float scale, const uint32_t *d_len, Bounds b, uint32_t L,
-                                                    const uint32_t *__restrict__ cstart,
-                                                    const uint32_t *__restrict__ cend, uint32_t stride, uint32_t maxn,
-                                                    uint32_t *__restrict__ count, uint32_t *__restrict__ idx,
-                                                    unsigned long long *total, Status *st) {
-    uint32_t n = d_len[kLenParticles];
+// Exact 32-bit form of `within` for particles that both lie inside the grid
+// (coordinates differ by less than 2^31): the same predicate, half the
+// instructions.  R2 = R * R.
+__device__ __forceinline__ bool within32(int4 a, int4 b, uint32_t R, unsigned long long R2) {
+    const uint32_t ax = (uint32_t)abs(b.x - a.x), ay = (uint32_t)abs(b.y - a.y), az = (uint32_t)abs(b.z - a.z);
+    if (max(ax, max(ay, az)) > R) return false;
+    const unsigned long long s = (unsigned long long)ax * ax + (unsigned long long)ay * ay + (unsigned long long)az * az;
+    return s <= R2;
+}
+
+// Walks the cells [x0, x1] x [y0, y1] x [z0, z1] and appends every neighbour of
+// particle i.  The walk is a chain of dependent loads (cell range -> candidates),
+// so the ranges of up to four cells of one (z, y) row are loaded together and
+// candidates four at a time.
+template <bool FAST>
+__device__ __forceinline__ uint32_t walk_cells(uint32_t i, int4 p, long long R, uint32_t x0, uint32_t x1, uint32_t y0,
+                                               uint32_t y1, uint32_t z0, uint32_t z1,
+                                               const int4 *__restrict__ pos, const uint32_t *__restrict__ cstart,
+                                               const uint32_t *__restrict__ cend, uint32_t stride, uint32_t maxn,
+                                               uint32_t *__restrict__ idx) {
+    const uint32_t R32 = (uint32_t)R;
+    const unsigned long long R2 = (unsigned long long)R32 * R32;
+    uint32_t c = 0;
+    for (uint32_t cz = z0; cz <= z1; ++cz)
+        for (uint32_t cy = y0; cy <= y1; ++cy) {
+            const uint32_t yz = (spread3(cy) << 1) | (spread3(cz) << 2);
+            for (uint32_t cx0 = x0; cx0 <= x1; cx0 += 4) {
+                uint32_t cs[4], ce[4];
+#pragma unroll
+                for (int v = 0; v < 4; ++v) {
+                    const bool in = cx0 + v <= x1;
+                    const uint32_t key = yz | spread3(cx0 + v);
+                    cs[v] = in ? cstart[key] : 0u;
+                    ce[v] = in ? cend[key] : 0u;
+                }
+#pragma unroll
+                for (int v = 0; v < 4; ++v) {
+                    const uint32_t s = cs[v], e = ce[v];
+                    for (uint32_t j0 = s; j0 < e; j0 += 4) {
+                        int4 q[4];
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) q[u] = j0 + u < e ? pos[j0 + u] : p;
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            const uint32_t j = j0 + u;
+                            if (j >= e || j == i) continue;
+                            if (FAST ? !within32(p, q[u], R32, R2) : !within(p, q[u], R)) continue;
+                            if (c < maxn) idx[(size_t)c * stride + i] = j;
+                            ++c;
+                        }
+                    }
+                }
+            }
+        }
+    return c;
+}
+
+struct BuildArgs {
+    const int4 *pos;
+    int4 *pos_box;  // when non-null: receives box_collision(pos) (the first Jacobi iteration's box pass)
+    const float *range;
+    const float *radius;
+    const float4 *bmin, *bmax;
+    uint32_t nboxes;
+    float scale;
+    const uint32_t *d_len;
+    Bounds b;
+    uint32_t L;
+    int fast_ok;  // the grid spans less than 2^31 units on every axis
+    const uint32_t *cstart, *cend;
+    uint32_t stride, maxn;
+    uint32_t *count, *idx;
+    unsigned long long *total;
+    Status *st;
+};
+
+// neighborhood_green.comp:49-87 with the canonical predicate (C2), one thread per
+// particle.  A box that touches no edge cell of the grid only meets particles
+// inside the grid (edge cells also hold the clamped outsiders), so it uses the
+// 32-bit predicate.
+__global__ void __launch_bounds__(256, 3) k_build_rows(BuildArgs a) {
+    const uint32_t n = a.d_len[kLenParticles];
+    const uint32_t last = (1u << a.L) - 1u;
     unsigned long long local = 0;
     long long rmin = 0x7fffffffffffffffll, rmax = -1;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        int4 p = pos[i];
-        long long R = range_fixed(range[i], scale);
+        const int4 p = a.pos[i];
+        const long long R = range_fixed(a.range[i], a.scale);
+        uint32_t c = 0;
         if (R < 0) {
-            set_flag(st, APBF_FLAG_NONFINITE);  // NaN or negative kernel width: no neighbours
+            set_flag(a.st, APBF_FLAG_NONFINITE);  // NaN or negative kernel width: no neighbours
         } else {
             rmin = R < rmin ? R : rmin;
             rmax = R > rmax ? R : rmax;
+            const Bounds &b = a.b;
+            const uint32_t x0 = cell_coord((long long)p.x - R, b.lo[0], b.hi[0], a.L);
+            const uint32_t x1 = cell_coord((long long)p.x + R, b.lo[0], b.hi[0], a.L);
+            const uint32_t y0 = cell_coord((long long)p.y - R, b.lo[1], b.hi[1], a.L);
+            const uint32_t y1 = cell_coord((long long)p.y + R, b.lo[1], b.hi[1], a.L);
+            const uint32_t z0 = cell_coord((long long)p.z - R, b.lo[2], b.hi[2], a.L);
+            const uint32_t z1 = cell_coord((long long)p.z + R, b.lo[2], b.hi[2], a.L);
+            const bool fast = a.fast_ok && x0 > 0 && y0 > 0 && z0 > 0 && x1 < last && y1 < last && z1 < last;
+            if (fast)
+                c = walk_cells<true>(i, p, R, x0, x1, y0, y1, z0, z1, a.pos, a.cstart, a.cend, a.stride, a.maxn, a.idx);
+            else
+                c = walk_cells<false>(i, p, R, x0, x1, y0, y1, z0, z1, a.pos, a.cstart, a.cend, a.stride, a.maxn,
+                                      a.idx);
         }
-        uint32_t c = 0;
-        if (R >= 0) {
-            uint32_t x0 = cell_coord((long long)p.x - R, b.lo[0], b.hi[0], L);
-            uint32_t x1 = cell_coord((long long)p.x + R, b.lo[0], b.hi[0], L);
-            uint32_t y0 = cell_coord((long long)p.y - R, b.lo[1], b.hi[1], L);
-            uint32_t y1 = cell_coord((long long)p.y + R, b.lo[1], b.hi[1], L);
-            uint32_t z0 = cell_coord((long long)p.z - R, b.lo[2], b.hi[2], L);
-            uint32_t z1 = cell_coord((long long)p.z + R, b.lo[2], b.hi[2], L);
-            for (uint32_t cz = z0; cz <= z1; ++cz)
-                for (uint32_t cy = y0; cy <= y1; ++cy)
-                    for (uint32_t cx = x0; cx <= x1; ++cx) {
-                        const uint32_t key = morton3(cx, cy, cz);
-                        const uint32_t s = cstart[key], e = cend[key];
-                        // candidates in batches of 4 loads
-                        for (uint32_t j0 = s; j0 < e; j0 += 4) {
-                            int4 q[4];
-#pragma unroll
-                            for (int u = 0; u < 4; ++u) q[u] = j0 + u < e ? pos[j0 + u] : p;
-#pragma unroll
-                            for (int u = 0; u < 4; ++u) {
-                                const uint32_t j = j0 + u;
-                                if (j >= e || j == i || !within(p, q[u], R)) continue;
-                                if (c < maxn) idx[(size_t)c * stride + i] = j;
-                                ++c;
-                            }
-                        }
-                    }
+        if (c > a.maxn) {
+            set_flag(a.st, APBF_FLAG_NEIGHBOR_OVERFLOW);
+            atomicMax(&a.st->required_neighbors, c);
         }
-        if (c > maxn) {
-            set_flag(st, APBF_FLAG_NEIGHBOR_OVERFLOW);
-            atomicMax(&st->required_neighbors, c);
-        }
-        count[i] = c < maxn ? c : maxn;
-        local += c < maxn ? c : maxn;
+        a.count[i] = c < a.maxn ? c : a.maxn;
+        local += c < a.maxn ? c : a.maxn;
+        if (a.pos_box) a.pos_box[i] = box_push(p, a.radius[i], i, a.bmin, a.bmax, a.nboxes);
     }
     // block reduction of the pair count and of the radius range
     for (int off = 16; off > 0; off >>= 1) {
         local += __shfl_down_sync(0xffffffffu, local, off);
-        long long a = __shfl_down_sync(0xffffffffu, rmin, off);
+        long long a2 = __shfl_down_sync(0xffffffffu, rmin, off);
         long long c2 = __shfl_down_sync(0xffffffffu, rmax, off);
-        rmin = a < rmin ? a : rmin;
+        rmin = a2 < rmin ? a2 : rmin;
         rmax = c2 > rmax ? c2 : rmax;
     }
     if ((threadIdx.x & 31) == 0) {
-        if (local) atomicAdd(total, local);
+        if (local) atomicAdd(a.total, local);
         if (rmax >= 0) {
-            atomicMin(&st->range_min, (unsigned long long)rmin);
-            atomicMax(&st->range_max, (unsigned long long)rmax);
+            atomicMin(&a.st->range_min, (unsigned long long)rmin);
+            atomicMax(&a.st->range_max, (unsigned long long)rmax);
         }
     }
 }
@@ -241,8 +305,11 @@ void swap_all(apbf_ctx *ctx) { ctx->fcur ^= 1; }
 }  // namespace
 
 apbf_status neighborhood_green(apbf_ctx *ctx, float range_scale, const float minp[3], const float maxp[3],
-                               uint32_t L, cudaStream_t s) {
-    if (L < 1 || L > ctx->cfg.max_log2res || L > 10) return APBF_ERR_INVALID_ARG;
+                               uint32_t L, cudaStream_t s, bool fuse_box) {
+    if (L < 1 || L > ctx->cfg.max_log2res || L > 10) {
+        set_error("neighborhood_green: log2res must be in [1, max_log2res of apbf_create]");
+        return APBF_ERR_INVALID_ARG;
+    }
     const uint32_t cap = ctx->cfg.particle_capacity;
     Bounds b = fixed_bounds(minp, maxp);
     FluidBufs &cur = ctx->fl[ctx->fcur];
@@ -274,10 +341,37 @@ apbf_status neighborhood_green(apbf_ctx *ctx, float range_scale, const float min
     k_reset_search<<<1, 1, 0, s>>>(ctx->status, ctx->d_pairs);
     APBF_AFTER_LAUNCH(ctx, s, "k_reset_search");
     APBF_BEFORE_LAUNCH(ctx, s, "k_build_rows");
-    k_build_rows<<<grid_for(ctx, cap, kBlock, 16), kBlock, 0, s>>>(
-        f.pos, f.kernel_width, range_scale, ctx->d_len, b, L, ctx->cell_start, ctx->cell_end, ctx->row_stride,
-        ctx->cfg.max_neighbors, ctx->nb_count, ctx->nb_idx, ctx->d_pairs, ctx->status);
+    BuildArgs ba;
+    ba.pos = f.pos;
+    FluidBufs &spare = ctx->fl[ctx->fcur ^ 1];
+    ba.pos_box = fuse_box ? spare.pos : nullptr;
+    ba.range = f.kernel_width;
+    ba.radius = f.radius;
+    ba.bmin = ctx->box_min;
+    ba.bmax = ctx->box_max;
+    ba.nboxes = ctx->n_boxes;
+    ba.scale = range_scale;
+    ba.d_len = ctx->d_len;
+    ba.b = b;
+    ba.L = L;
+    ba.fast_ok = 1;
+    for (int d = 0; d < 3; ++d)
+        if (b.hi[d] - b.lo[d] >= (1ll << 31)) ba.fast_ok = 0;
+    ba.cstart = ctx->cell_start;
+    ba.cend = ctx->cell_end;
+    ba.stride = ctx->row_stride;
+    ba.maxn = ctx->cfg.max_neighbors;
+    ba.count = ctx->nb_count;
+    ba.idx = ctx->nb_idx;
+    ba.total = ctx->d_pairs;
+    ba.st = ctx->status;
+    k_build_rows<<<grid_for(ctx, cap, kBlock, 8), kBlock, 0, s>>>(ba);
     APBF_AFTER_LAUNCH(ctx, s, "k_build_rows");
+    if (fuse_box) {  // the box-collided positions are the current ones now
+        int4 *t = f.pos;
+        f.pos = spare.pos;
+        spare.pos = t;
+    }
     return build_reverse_rows(ctx, s);
 }
 

@@ -38,13 +38,16 @@ struct PassA {
     uint32_t stride;
     float *lambda;
     int4 *shift;
-    KConst *kc;
+    float4 *rec;  // per particle: lambda, Gauss ivd, Gauss norm, kernel width (read by k_delta)
     uint32_t *dbg_dens;
     int4 *dbg_grad;
     uint32_t *dbg_sq;
     double *partials;
     const uint32_t *d_len;
     Status *st;
+    double *red_out;     // [2], [3]: mean compression / absolute error of this pass
+    float target;        // > 0: set st->converged when the error is at most this
+    int early_exit;      // skip the pass when st->converged is set
     float rmin3;  // pow(2 * smallestTargetRadius, 3)
     int hk, gk, method, update_b;
     float b_speed, b_sgl_factor, b_up_factor;
@@ -63,17 +66,40 @@ __device__ __forceinline__ void pair_terms(int hk, int gk, float3 d, float kw, K
     }
 }
 
+// Fixed-order (deterministic) sum of per-block partial pairs with one block of
+// 256 threads: thread t sums partials t, t+256, ... in order, then a fixed tree.
+__device__ __forceinline__ void block_sum2(const double *partials, int blocks, double &t1, double &t2) {
+    __shared__ double s1[256], s2[256];
+    double a = 0.0, b = 0.0;
+    for (int k = threadIdx.x; k < blocks; k += 256) {
+        a += ((volatile const double *)partials)[2 * k];
+        b += ((volatile const double *)partials)[2 * k + 1];
+    }
+    s1[threadIdx.x] = a;
+    s2[threadIdx.x] = b;
+    __syncthreads();
+    for (int off = 128; off > 0; off >>= 1) {
+        if ((int)threadIdx.x < off) {
+            s1[threadIdx.x] += s1[threadIdx.x + off];
+            s2[threadIdx.x] += s2[threadIdx.x + off];
+        }
+        __syncthreads();
+    }
+    t1 = s1[0];
+    t2 = s2[0];
+}
+
 constexpr int kUnroll = 4;
 
 template <bool GAUSS>
 __global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) {
+    if (a.early_exit && *(volatile uint32_t *)&a.st->converged) return;  // uniform over the grid
     const uint32_t n = a.d_len[kLenParticles];
     double e1 = 0.0, e2 = 0.0;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int4 p = a.pos[i];
         const float kw = a.kw[i], im = a.inv_mass[i], radius = a.radius[i];
         const KConst c = gauss_consts(kw);
-        a.kc[i] = c;
         float W0 = GAUSS ? c.norm : kernel_height(a.hk, 0.0f, kw, c);
         uint32_t dens = f2u(W0 / im * APBF_FIX);
         int32_t gx = 0, gy = 0, gz = 0;
@@ -86,34 +112,31 @@ __global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) 
         for (uint32_t k0 = 0; k0 < cnt; k0 += kUnroll) {
             uint32_t jj[kUnroll];
             int4 qq[kUnroll];
-            float mm[kUnroll];
 #pragma unroll
             for (int u = 0; u < kUnroll; ++u) jj[u] = k0 + u < cnt ? row[(size_t)(k0 + u) * a.stride] : i;
 #pragma unroll
-            for (int u = 0; u < kUnroll; ++u) {
-                qq[u] = a.pos[jj[u]];
-                mm[u] = a.inv_mass[jj[u]];
-            }
+            for (int u = 0; u < kUnroll; ++u) qq[u] = a.pos[jj[u]];
 #pragma unroll
             for (int u = 0; u < kUnroll; ++u) {
                 if (k0 + u >= cnt) break;
                 const int4 q = qq[u];
-                const float mj = __frcp_rn(mm[u]);  // mass of the neighbour (x / invMassN = x * mj)
+                // the neighbour's mass rides in position.w (x / invMassN = x * mass)
+                const float mjf = __int_as_float(q.w) * APBF_FIX;  // neighbour mass x 2^18
                 const float3 d = fdiff(p, q);
                 float W;
                 float3 g;
                 pair_terms<GAUSS>(a.hk, a.gk, d, kw, c, W, g);
-                dens += f2u(W * mj * APBF_FIX);
-                gx = wadd(gx, f2i(g.x * mj * APBF_FIX));
-                gy = wadd(gy, f2i(g.y * mj * APBF_FIX));
-                gz = wadd(gz, f2i(g.z * mj * APBF_FIX));
-                sq += f2u(dot3x(g, g) * mj * APBF_FIX);
+                dens += f2u(W * mjf);
+                gx = wadd(gx, f2i(g.x * mjf));
+                gy = wadd(gy, f2i(g.y * mjf));
+                gz = wadd(gz, f2i(g.z * mjf));
+                sq += f2u(dot3x(g, g) * mjf);
                 if (a.method == 1) {  // incompressibility_1.comp:62-68
-                    const float den = mm[u] * kw;
+                    const float den = kw * APBF_FIX / mjf;
                     cx = wadd(cx, f2i((float)wadd(q.x, -p.x) / den));
                     cy = wadd(cy, f2i((float)wadd(q.y, -p.y) / den));
                     cz = wadd(cz, f2i((float)wadd(q.z, -p.z) / den));
-                    cw = wadd(cw, f2i(APBF_FIX * mj));
+                    cw = wadd(cw, f2i(mjf));
                 }
             }
         }
@@ -145,6 +168,7 @@ __global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) 
         float lam = under / (ird * ird * (sqs + 0.01f));
         lam /= a.rmin3 / ird * im;
         a.lambda[i] = lam;
+        a.rec[i] = make_float4(lam, c.ivd, c.norm, kw);
         int4 sh = make_int4(0, 0, 0, 0);
         if (lam < 0.0f) {
             const float sc = lam * im * APBF_FIX;
@@ -164,15 +188,25 @@ __global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) 
                 for (uint32_t k = 0; k < cnt; ++k) {
                     const uint32_t j = a.idx[(size_t)k * a.stride + i];
                     const float3 d = fdiff(p, a.pos[j]);
-                    float W;
-                    float3 g;
-                    pair_terms<GAUSS>(a.hk, a.gk, d, kw, c, W, g);
-                    float l = sqrtf(dot3x(g, g));
-                    if (!(l > 0.0f)) continue;
-                    float dd = ed.x * (g.x / l) + ed.y * (g.y / l) + ed.z * (g.z / l);
-                    if (dd > 0.6f) {
-                        b = 0.0f;
-                        break;
+                    if (GAUSS) {
+                        // the Gauss gradient points along -d: normalize(gradW) = -d / |d|
+                        const float r2 = dot3x(d, d);
+                        if (r2 < 1.0e-8f) continue;  // zero gradient: normalize() gives NaN, no filter
+                        if (-(ed.x * d.x + ed.y * d.y + ed.z * d.z) > 0.6f * sqrtf(r2)) {
+                            b = 0.0f;
+                            break;
+                        }
+                    } else {
+                        float W;
+                        float3 g;
+                        pair_terms<GAUSS>(a.hk, a.gk, d, kw, c, W, g);
+                        float l = sqrtf(dot3x(g, g));
+                        if (!(l > 0.0f)) continue;
+                        float dd = ed.x * (g.x / l) + ed.y * (g.y / l) + ed.z * (g.z / l);
+                        if (dd > 0.6f) {
+                            b = 0.0f;
+                            break;
+                        }
                     }
                 }
             }
@@ -199,6 +233,7 @@ __global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) 
         s2[w] = e2;
     }
     __syncthreads();
+    __shared__ bool s_last;
     if (threadIdx.x == 0) {
         double t1 = 0.0, t2 = 0.0;
         for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
@@ -207,16 +242,34 @@ __global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) 
         }
         a.partials[2 * blockIdx.x] = t1;
         a.partials[2 * blockIdx.x + 1] = t2;
+        __threadfence();
+        s_last = atomicAdd(&a.st->done_blocks, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!s_last) return;
+    // the last block: fixed-order sum of all partials (deterministic), error and
+    // convergence flag for the passes that follow
+    __threadfence();
+    double t1, t2;
+    block_sum2(a.partials, gridDim.x, t1, t2);
+    if (threadIdx.x == 0) {
+        const double m1 = n ? t1 / n : 0.0, m2 = n ? t2 / n : 0.0;
+        a.red_out[2] = m1;
+        a.red_out[3] = m2;
+        a.st->density_passes += 1u;
+        a.st->done_blocks = 0u;
+        if (a.target > 0.0f && m1 <= (double)a.target) a.st->converged = 1u;
     }
 }
 
 struct PassB {
     const int4 *pos;
     int4 *pos_out;
-    const float *kw;
-    const float *lambda;
+    const float4 *rec;
     const int4 *shift;
-    const KConst *kc;
+    const float *radius;
+    const float4 *bmin, *bmax;
+    uint32_t nboxes;  // > 0: box collision of the next iteration applied to the output
     const uint32_t *count;
     const uint32_t *idx;
     const uint32_t *rcount;
@@ -225,11 +278,17 @@ struct PassB {
     const uint32_t *d_len;
     const Status *st;
     int gk;
+    int early_exit;  // converged: copy the positions unchanged (the buffers swap regardless)
 };
 
 template <bool GAUSS>
 __global__ void __launch_bounds__(256, GAUSS ? 5 : 4) k_delta(PassB a) {
     const uint32_t n = a.d_len[kLenParticles];
+    if (a.early_exit && *(volatile const uint32_t *)&a.st->converged) {
+        for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+            a.pos_out[j] = a.pos[j];
+        return;
+    }
     const bool sym = a.st->range_min == a.st->range_max;
     const uint32_t *cnt_arr = sym ? a.count : a.rcount;
     const uint32_t *idx_arr = sym ? a.idx : a.ridx;
@@ -241,30 +300,29 @@ __global__ void __launch_bounds__(256, GAUSS ? 5 : 4) k_delta(PassB a) {
         const uint32_t *row = idx_arr + j;
         for (uint32_t k0 = 0; k0 < cnt; k0 += kUnroll) {
             uint32_t ii[kUnroll];
-            float ll[kUnroll];
+            float4 rr[kUnroll];
             int4 qq[kUnroll];
-            KConst cc[kUnroll];
-            float hh[kUnroll];
 #pragma unroll
             for (int u = 0; u < kUnroll; ++u) ii[u] = k0 + u < cnt ? row[(size_t)(k0 + u) * a.stride] : j;
 #pragma unroll
             for (int u = 0; u < kUnroll; ++u) {
-                ll[u] = k0 + u < cnt ? a.lambda[ii[u]] : 0.0f;
+                rr[u] = a.rec[ii[u]];
                 qq[u] = a.pos[ii[u]];
-                cc[u] = a.kc[ii[u]];
-                hh[u] = GAUSS ? 0.0f : a.kw[ii[u]];
             }
 #pragma unroll
             for (int u = 0; u < kUnroll; ++u) {
-                const float lam = ll[u];
+                const float lam = k0 + u < cnt ? rr[u].x : 0.0f;
                 if (!(lam < 0.0f)) continue;  // incompressibility_3.comp:63 (also the padding lanes)
+                KConst c;
+                c.ivd = rr[u].y;
+                c.norm = rr[u].z;
                 const float3 d = fdiff(qq[u], p);
                 const float r2 = dot3x(d, d);
                 float3 g;
                 if (GAUSS) {
-                    g = kernel_gradient(1, d, r2, 0.0f, cc[u], gauss_height(r2, cc[u]));
+                    g = kernel_gradient(1, d, r2, 0.0f, c, gauss_height(r2, c));
                 } else {
-                    g = kernel_gradient(a.gk, d, r2, hh[u], cc[u], a.gk == 1 ? gauss_height(r2, cc[u]) : 0.0f);
+                    g = kernel_gradient(a.gk, d, r2, rr[u].w, c, a.gk == 1 ? gauss_height(r2, c) : 0.0f);
                 }
                 const float sc = lam * APBF_FIX;
                 ax = wadd(ax, f2i(g.x * sc));
@@ -272,41 +330,9 @@ __global__ void __launch_bounds__(256, GAUSS ? 5 : 4) k_delta(PassB a) {
                 az = wadd(az, f2i(g.z * sc));
             }
         }
-        a.pos_out[j] = make_int4(wadd(p.x, ax), wadd(p.y, ay), wadd(p.z, az), p.w);
-    }
-}
-
-// Fixed-order (deterministic) sum of per-block partial pairs with one block of
-// 256 threads: thread t sums partials t, t+256, ... in order, then a fixed tree.
-__device__ __forceinline__ void block_sum2(const double *partials, int blocks, double &t1, double &t2) {
-    __shared__ double s1[256], s2[256];
-    double a = 0.0, b = 0.0;
-    for (int k = threadIdx.x; k < blocks; k += 256) {
-        a += partials[2 * k];
-        b += partials[2 * k + 1];
-    }
-    s1[threadIdx.x] = a;
-    s2[threadIdx.x] = b;
-    __syncthreads();
-    for (int off = 128; off > 0; off >>= 1) {
-        if ((int)threadIdx.x < off) {
-            s1[threadIdx.x] += s1[threadIdx.x + off];
-            s2[threadIdx.x] += s2[threadIdx.x + off];
-        }
-        __syncthreads();
-    }
-    t1 = s1[0];
-    t2 = s2[0];
-}
-
-__global__ void __launch_bounds__(256) k_finalize_error(const double *partials, int blocks, const uint32_t *d_len,
-                                                        double *out) {
-    double t1, t2;
-    block_sum2(partials, blocks, t1, t2);
-    if (threadIdx.x == 0) {
-        uint32_t n = d_len[kLenParticles];
-        out[2] = n ? t1 / n : 0.0;
-        out[3] = n ? t2 / n : 0.0;
+        int4 out = make_int4(wadd(p.x, ax), wadd(p.y, ay), wadd(p.z, az), p.w);
+        if (a.nboxes) out = box_push(out, a.radius[j], j, a.bmin, a.bmax, a.nboxes);
+        a.pos_out[j] = out;
     }
 }
 
@@ -350,7 +376,7 @@ __global__ void __launch_bounds__(256) k_finalize_mass(const double *partials, i
 
 }  // namespace
 
-apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s) {
+apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s, bool box_after, bool converge) {
     const uint32_t cap = ctx->cfg.particle_capacity;
     FluidBufs &f = ctx->fl[ctx->fcur];
     FluidBufs &alt = ctx->fl[ctx->fcur ^ 1];
@@ -367,13 +393,16 @@ apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s) {
     a.stride = ctx->row_stride;
     a.lambda = ctx->lambda;
     a.shift = ctx->shift;
-    a.kc = ctx->kconst;
+    a.rec = ctx->solve_rec;
     a.dbg_dens = ctx->debug ? ctx->dbg_density : nullptr;
     a.dbg_grad = ctx->dbg_grad;
     a.dbg_sq = ctx->dbg_sq;
     a.partials = ctx->red_partials;
     a.d_len = ctx->d_len;
     a.st = ctx->status;
+    a.red_out = ctx->red_out;
+    a.target = converge ? st.density_error_target : 0.0f;
+    a.early_exit = converge ? 1 : 0;
     const float rm2 = 2.0f * st.smallest_target_radius;
     a.rmin3 = rm2 * rm2 * rm2;
     a.hk = st.height_kernel_id;
@@ -390,17 +419,16 @@ apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s) {
     else
         k_density_lambda<false><<<g, kBlock, 0, s>>>(a);
     APBF_AFTER_LAUNCH(ctx, s, "k_density_lambda");
-    APBF_BEFORE_LAUNCH(ctx, s, "k_finalize_error");
-    k_finalize_error<<<1, 256, 0, s>>>(ctx->red_partials, g, ctx->d_len, ctx->red_out);
-    APBF_AFTER_LAUNCH(ctx, s, "k_finalize_error");
 
     PassB b;
     b.pos = f.pos;
     b.pos_out = alt.pos;
-    b.kw = f.kernel_width;
-    b.lambda = ctx->lambda;
+    b.rec = ctx->solve_rec;
     b.shift = ctx->shift;
-    b.kc = ctx->kconst;
+    b.radius = f.radius;
+    b.bmin = ctx->box_min;
+    b.bmax = ctx->box_max;
+    b.nboxes = box_after ? ctx->n_boxes : 0u;
     b.count = ctx->nb_count;
     b.idx = ctx->nb_idx;
     b.rcount = ctx->rev_count;
@@ -409,6 +437,7 @@ apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s) {
     b.d_len = ctx->d_len;
     b.st = ctx->status;
     b.gk = st.gradient_kernel_id;
+    b.early_exit = converge ? 1 : 0;
     APBF_BEFORE_LAUNCH(ctx, s, "k_delta");
     if (gauss)
         k_delta<true><<<grid_for(ctx, cap), kBlock, 0, s>>>(b);
@@ -425,7 +454,7 @@ apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s) {
 apbf_status reduce_fp64(apbf_ctx *ctx, double out[4], cudaStream_t s) {
     FluidBufs &f = ctx->fl[ctx->fcur];
     const int g = ctx->red_blocks;
-    // the error partials of the last density pass are already reduced into red_out[2..3]
+    // red_out[2..3] hold the error of the last density pass (its last block wrote them)
     APBF_BEFORE_LAUNCH(ctx, s, "k_mass_volume");
     k_mass_volume<<<g, kBlock, 0, s>>>(f.inv_mass, f.radius, ctx->d_len, ctx->red_partials + 2 * g);
     APBF_AFTER_LAUNCH(ctx, s, "k_mass_volume");

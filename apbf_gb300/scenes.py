@@ -157,8 +157,12 @@ def water_drop(total: int = 250_000, seed: int = 0, substeps: int = 500, iterati
     bmin, bmax = wall_boxes([0, 0, 0], box, lid=False)
     hi = np.maximum(box, centre + R + 2)
     gmin, gmax, L = _grid_for([0, 0, 0], hi)
+    # free fall of the drop onto the pool surface: (1.0 m - 0.3 m - fill) / (g/2) -> ~90 substeps at 250k
+    fall = max(centre[1] - R - 2.0 * (layers + 1), 0.0) * r_m
+    impact = int(np.sqrt(2.0 * fall / 9.81) * 240.0)
     return SceneSpec("water_drop", st, bmin, bmax, gmin, gmax, L, (0.0, -9.81 / r_m, 0.0), 1.0 / 240.0, iterations,
-                     substeps, basic_pbf, {"r_m": r_m, "box": box.tolist(), "sphere": int(sp.shape[0])})
+                     substeps, basic_pbf, {"r_m": r_m, "box": box.tolist(), "sphere": int(sp.shape[0]),
+                                           "presteps": impact + 20})
 
 
 def block(n: int, seed: int = 0, iterations: int = 4, dt: float = 1.0 / 120.0) -> SceneSpec:

@@ -61,7 +61,8 @@ def settings_dict(spec) -> dict:
 
     s = default_settings()
     s.basic_pbf = 1 if spec.basic_pbf else 0
-    s.solver_iterations = spec.iterations
+    s.solver_iterations = 20
+    s.density_error_target = 0.001
     return {f: getattr(s, f) for f, _ in s._fields_ if not f.startswith("pad")}
 
 
@@ -247,12 +248,17 @@ def run_ours(args) -> None:
     cap = int(n * 1.25) + 1024
     ctx = Context(particle_capacity=cap, max_neighbors=args.max_neighbors, max_log2res=max(spec.log2res, 3),
                   device=local)
-    ctx.set_settings(basic_pbf=1 if spec.basic_pbf else 0, solver_iterations=args.iterations or spec.iterations)
+    # iterate every substep until the mean compression error is at most the target
+    ctx.set_settings(basic_pbf=1 if spec.basic_pbf else 0, solver_iterations=args.max_iterations,
+                     density_error_target=args.error_target)
     ctx.set_scene(spec.grid_min, spec.grid_max, spec.log2res, spec.acceleration)
     ctx.set_boxes(spec.box_min, spec.box_max)
     ctx.upload(spec.state)
     stream = torch.cuda.current_stream()
 
+    presteps = args.presteps if args.presteps >= 0 else spec.meta.get("presteps", 0)
+    for _ in range(presteps):  # untimed: bring the scene into its violent regime (after impact)
+        ctx.substep(spec.dt)
     for _ in range(args.warmup):
         ctx.substep(spec.dt)
     ctx.check_status()
@@ -263,6 +269,7 @@ def run_ours(args) -> None:
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     ctx.profile_enable(True, 65536)
     ctx.profile_read()  # clear
+    ctx.check_status()  # clears the status block (density pass counter)
     launches0 = ctx.launch_count()
     clocks = ClockSampler(local)
     clocks.start()
@@ -285,6 +292,7 @@ def run_ours(args) -> None:
     ctx.profile_enable(False, 0)
     step_ms = [a.elapsed_time(b) for a, b in ev]
     info = ctx.check_status()
+    passes_per_step = info.density_passes / args.steps
     n_end, _ = ctx.lengths()
     red = ctx.reduce_fp64()
     total_ms = float(np.sum(step_ms))
@@ -327,7 +335,8 @@ def run_ours(args) -> None:
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 (int32 fixed-point positions and sums)",
             "data": "synthetic (seeded scene generator)",
             "config": {"workload": args.workload, "particles": n, "particles_after": int(n_end),
-                       "iterations": int(ctx.settings.solver_iterations), "dt": spec.dt,
+                       "iterations": f"until mean compression error <= {args.error_target} (max {args.max_iterations})",
+                       "density_passes_per_substep": passes_per_step, "presteps": presteps, "dt": spec.dt,
                        "adaptive": not spec.basic_pbf, "pairs": int(info.pairs),
                        "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas x{world}",
                        "density_error_last_iteration": float(red[2]), "abs_density_error": float(red[3])},
@@ -378,7 +387,9 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
-    ap.add_argument("--iterations", type=int, default=0)
+    ap.add_argument("--max-iterations", type=int, default=20)
+    ap.add_argument("--error-target", type=float, default=0.001)
+    ap.add_argument("--presteps", type=int, default=-1, help="untimed substeps before warm-up (-1: scene default)")
     ap.add_argument("--max-neighbors", type=int, default=192)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

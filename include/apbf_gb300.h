@@ -86,7 +86,11 @@ typedef struct apbf_settings {
     float smallest_target_radius;
     float target_radius_offset;
     float target_radius_scale_factor;
-    float pad1[3];
+    /* Not in the reference: when > 0, the Jacobi iterations of apbf_substep stop as
+     * soon as the mean compression error max(0, rho/rho0 - 1) measured by a density
+     * pass is at most this value; solver_iterations is then the maximum. */
+    float density_error_target;
+    float pad1[2];
 } apbf_settings;
 
 /* Capacities (the reference's requested lengths, source/pool.cpp:7-15). */
@@ -113,7 +117,8 @@ typedef struct apbf_scene {
 typedef struct apbf_fluid_view {
     uint32_t capacity;
     uint32_t *d_length;
-    int32_t *position;     /* int4 */
+    int32_t *position;     /* int4; w is reserved: the neighbourhood search stores the particle's
+                              mass there for the incompressibility passes */
     float *velocity;       /* float4 */
     float *inverse_mass;
     float *radius;
@@ -152,6 +157,8 @@ typedef struct apbf_status_info {
     uint32_t required_transfers;
     uint32_t required_particles;
     unsigned long long pairs;    /* pairs of the last neighbourhood search */
+    uint32_t density_passes;     /* density passes executed since the status was last cleared */
+    uint32_t pad;
 } apbf_status_info;
 
 typedef struct apbf_ctx apbf_ctx;

@@ -1005,6 +1005,13 @@ uint64_t or_substep(or_fluid *f, or_transfers *t, or_neighbors *nb, const or_box
     if (!s->basic_pbf && !s->base_kernel_width_on_boundary_distance) or_spread_kernel_width(f, nb, s);
     for (int it = 0; it < s->solver_iterations; ++it) {
         or_box_collision(f, b);
+        if (s->density_error_target > 0.0f) {
+            /* the device measures the error in each density pass and stops before
+             * correcting once it is at most the target */
+            double e[2];
+            or_density_error(f, nb, s, e);
+            if (e[0] <= (double)s->density_error_target) break;
+        }
         or_incompressibility_apply(f, nb, s, NULL);
     }
     if (!s->basic_pbf) or_update_transfers(f, nb, t, s, sc->max_transfers);

@@ -71,7 +71,8 @@ typedef struct or_settings {
     float smallest_target_radius;
     float target_radius_offset;
     float target_radius_scale_factor;
-    float pad1[3];
+    float density_error_target; /* > 0: stop the iterations once the error is at most this */
+    float pad1[2];
 } or_settings;
 
 /* Particle + fluid state, structure of arrays.  pos / pos_backup are ivec4

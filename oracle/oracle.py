@@ -46,7 +46,8 @@ class OrSettings(C.Structure):
         ("smallest_target_radius", C.c_float),
         ("target_radius_offset", C.c_float),
         ("target_radius_scale_factor", C.c_float),
-        ("pad1", C.c_float * 3),
+        ("density_error_target", C.c_float),
+        ("pad1", C.c_float * 2),
     ]
 
 
@@ -136,7 +137,7 @@ def settings_from(src) -> OrSettings:
     for name, _ in OrSettings._fields_:
         if name.startswith("pad"):
             continue
-        v = src[name] if isinstance(src, dict) else getattr(src, name)
+        v = src.get(name, 0) if isinstance(src, dict) else getattr(src, name)
         setattr(s, name, v)
     return s
 

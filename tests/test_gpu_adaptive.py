@@ -18,7 +18,7 @@ pytestmark = pytest.mark.gpu
 GRID = ((-4.0, -4.0, -4.0), (60.0, 60.0, 60.0))
 
 
-def _ctx(cap, maxn=384, tcap=10000):
+def _ctx(cap, maxn=1024, tcap=10000):
     from apbf_gb300.api import Context
 
     return Context(particle_capacity=cap, max_neighbors=maxn, transfer_capacity=tcap, max_log2res=5)

@@ -104,7 +104,7 @@ def test_neighbor_overflow_reports_required(orc):
     from apbf_gb300.api import neighborhood_green
 
     spec = scenes.dam_break(n_side=10)
-    ctx = _ctx(1000, maxn=8, L=5)
+    ctx = _ctx(1000, maxn=8, L=max(5, spec.log2res))
     ctx.upload(spec.state)
     neighborhood_green().set_data(ctx).set_position_range(spec.grid_min, spec.grid_max, spec.log2res).apply()
     info = ctx.status()

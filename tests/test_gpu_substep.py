@@ -125,3 +125,41 @@ def test_dam_break_config0_runs_and_stays_incompressible():
     assert 0.0 <= red[2] < 0.05  # mean compression error of the last iteration
     assert info.pairs > 20 * spec.n
     ctx.close()
+
+
+def test_iterations_stop_at_error_target(orc):
+    """density_error_target: the device stops the Jacobi iterations at the first
+    density pass whose mean compression error is at most the target, like the
+    oracle's or_substep.  The target is put between two consecutive errors of the
+    oracle's own sequence so that FP32 and FP64 agree on where to stop."""
+    spec = _free_block(n_side=12)
+    ctx = _setup(spec)
+    s = orc.settings_from(ctx.settings)
+    # the oracle's error sequence for this substep
+    fs = orc.FluidState(spec.state)
+    orc.velocity_handling(fs, np.float32(spec.dt), np.float32(1.0), spec.acceleration)
+    orc.neighborhood_green(fs, 1.0, spec.grid_min, spec.grid_max, spec.log2res, 1 << 22)
+    errs = []
+    for _ in range(6):
+        errs.append(orc.density_error(fs, s)[0])
+        orc.incompressibility(fs, s)
+    assert errs[2] > 1.05 * errs[3] > 0, errs
+    target = float(np.sqrt(errs[2] * errs[3]))
+
+    ctx.set_settings(solver_iterations=10, density_error_target=target)
+    ctx.check_status()  # clear the pass counter
+    ctx.substep(spec.dt)
+    info = ctx.check_status()
+    assert info.density_passes == 4  # three corrections, then the pass that meets the target
+    g, _ = ctx.download()
+    s2 = orc.settings_from(ctx.settings)
+    fs2 = orc.FluidState(spec.state)
+    sc = orc.make_scene(s2, spec.grid_min, spec.grid_max, spec.log2res, spec.acceleration)
+    orc.substep(fs2, sc, (spec.box_min, spec.box_max), np.float32(spec.dt), 1 << 22)
+    o = fs2.state()
+    x = g["position"][:, :3].astype(np.int64)
+    xo = o["position"][:, :3].astype(np.int64)
+    assert np.all(np.abs(x - xo) <= 1e-5 * np.abs(xo) + 64), np.abs(x - xo).max()
+    red = ctx.reduce_fp64()
+    assert red[2] <= target < errs[2]
+    ctx.close()
