@@ -27,6 +27,9 @@ FLAG_SPIN_LIMIT = 0x8
 FLAG_NONFINITE = 0x10
 MAX_BOXES = 64
 MAX_TRANSFERS = 10000
+MLP_PARAMS = 4824  # apbf_mlp_param_count()
+WARM_LEARNED = 1    # APBF_WARM_LEARNED
+WARM_PROJECTED = 2  # APBF_WARM_PROJECTED
 
 
 class ApbfError(RuntimeError):
@@ -174,6 +177,14 @@ SIGNATURES = {
     "apbf_profile_read": (_ST, [_P, C.POINTER(KernelTime), C.c_uint32, C.POINTER(C.c_uint32),
                                 C.POINTER(C.c_ulonglong), _P]),
     "apbf_launch_count": (_ST, [_P, C.POINTER(C.c_ulonglong)]),
+    "apbf_mlp_param_count": (_ST, [C.POINTER(C.c_uint32)]),
+    "apbf_mlp_partials_size": (_ST, [C.c_uint32, C.POINTER(C.c_uint32)]),
+    "apbf_mlp_load": (_ST, [_P, _P, _P]),
+    "apbf_set_warm_start": (_ST, [_P, C.c_int]),
+    "apbf_record_samples": (_ST, [_P, C.c_uint32, _P, _P, C.c_uint32, _P]),
+    "apbf_mlp_forward": (_ST, [_P, _P, C.c_uint32, _P, _P]),
+    "apbf_mlp_train_step": (_ST, [_P, _P, _P, _P, _P, _P, C.c_uint32, C.c_float, C.c_float, C.c_uint32, _P, _P,
+                                  _P]),
     "apbf_sort_pairs": (_ST, [_P, _P, _P, _P, C.c_uint32, C.c_uint32, _P, _P, _P]),
     "apbf_sort_pairs_noalloc": (_ST, [_P, _P, _P, C.c_uint32, C.c_uint32, _P, _P, _P]),
     "apbf_prefix_sum": (_ST, [_P, _P, _P, C.c_uint32, _P]),

@@ -260,6 +260,30 @@ class Context:
     def substep(self, dt: float, stream=None) -> None:
         N.check(self.lib.apbf_substep(self.handle, C.c_float(dt), _stream_handle(stream)), "apbf_substep")
 
+    # ---- learned warm start (no reference counterpart) ----
+    def mlp_load(self, params: torch.Tensor, stream=None) -> None:
+        """Copies a device parameter vector (apbf_mlp_param_count() floats) into the context."""
+        if params.dtype != torch.float32 or not params.is_cuda or params.numel() != N.MLP_PARAMS:
+            raise ValueError("params must be a CUDA float32 tensor of %d floats" % N.MLP_PARAMS)
+        N.check(self.lib.apbf_mlp_load(self.handle, C.c_void_p(params.data_ptr()), _stream_handle(stream)),
+                "apbf_mlp_load")
+
+    def set_warm_start(self, mode: int | bool) -> None:
+        """N.WARM_LEARNED | N.WARM_PROJECTED bits (True = both); 0 / False = the reference's solve."""
+        m = (N.WARM_LEARNED | N.WARM_PROJECTED) if mode is True else int(mode)
+        N.check(self.lib.apbf_set_warm_start(self.handle, m), "apbf_set_warm_start")
+
+    def record_samples(self, iterations: int, features: torch.Tensor, targets: torch.Tensor,
+                       count: torch.Tensor) -> None:
+        """Arms the next substep to append (features, sum of min(0, lambda) over its first
+        `iterations` plain iterations) of every particle to the device buffers."""
+        cap = targets.numel()
+        if features.numel() < cap * 8 or count.dtype != torch.int32:
+            raise ValueError("features needs 8 floats per sample and count one int32")
+        N.check(self.lib.apbf_record_samples(self.handle, iterations, C.c_void_p(features.data_ptr()),
+                                             C.c_void_p(targets.data_ptr()), cap, C.c_void_p(count.data_ptr())),
+                "apbf_record_samples")
+
     def debug_incompressibility(self, stream=None) -> dict:
         n, _ = self.lengths(stream)
         d = torch.empty(self.capacity, dtype=torch.int32, device=f"cuda:{self.device}")

@@ -309,6 +309,7 @@ __global__ void k_split(FluidBufs f, const uint32_t *splits, uint32_t *d_len) {
         f.target_radius[d] = f.target_radius[s];
         f.kernel_width[d] = f.kernel_width[s];
         f.boundariness[d] = f.boundariness[s];
+        f.lambda_prev[d] = f.lambda_prev[s];
         f.boundary_distance[d] = f.boundary_distance[s];
     }
 }
@@ -367,6 +368,7 @@ __global__ void k_compact_particles(FluidBufs src, FluidBufs dst, const uint32_t
         dst.target_radius[k] = src.target_radius[i];
         dst.kernel_width[k] = src.kernel_width[i];
         dst.boundariness[k] = src.boundariness[i];
+        dst.lambda_prev[k] = src.lambda_prev[i];
         dst.boundary_distance[k] = src.boundary_distance[i];
     }
 }

@@ -39,6 +39,7 @@ struct FluidBufs {
     float *kernel_width;
     float *boundariness;
     uint32_t *boundary_distance;
+    float *lambda_prev;  // sum of the lambdas applied in the particle's last substep (warm-start feature)
 };
 
 struct TransferBufs {
@@ -135,6 +136,20 @@ struct apbf_ctx {
     float *lambda = nullptr;
     int4 *shift = nullptr;
     float4 *solve_rec = nullptr;   // per particle: lambda, Gauss constants (ivd, norm), kernel width
+    // learned warm start
+    float *mlp_params = nullptr;   // FP32 parameter vector (mlp.cu)
+    float *features = nullptr;     // per particle: 8 features of the first density pass
+    float4 *selfdir = nullptr;     // per particle: self-shift direction (xyz), inverse mass (w)
+    float *lam_acc = nullptr;      // per particle: sum of min(0, lambda) over the recorded iterations
+    int warm_start = 0;            // APBF_WARM_* bits: learned first update, projected later passes
+    int track_lambda = 0;          // 1: keep lambda_prev (set once recording or the warm start is used)
+    int mlp_loaded = 0;
+    // recording of training samples (armed for one apbf_substep)
+    uint32_t rec_iterations = 0;
+    float *rec_features = nullptr;
+    float *rec_targets = nullptr;
+    uint32_t rec_capacity = 0;
+    uint32_t *rec_count = nullptr;
     uint32_t *dbg_density = nullptr;
     int4 *dbg_grad = nullptr;
     uint32_t *dbg_sq = nullptr;
@@ -236,7 +251,25 @@ apbf_status neighborhood_green(apbf_ctx *ctx, float range_scale, const float min
                                uint32_t log2res, cudaStream_t s, bool fuse_box = false);
 apbf_status velocity_handling(apbf_ctx *ctx, float dt, const float accel[3], cudaStream_t s);
 apbf_status box_collision(apbf_ctx *ctx, cudaStream_t s);
-apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s, bool box_after = false, bool converge = false);
+// feature_mode: 0 none, 1 write features + self-shift direction; acc_mode: 0 none,
+// 1 lam_acc = min(0, lambda), 2 lam_acc += min(0, lambda); learned: the first
+// position update takes lambda from the network.
+// feature_mode 1: write the warm-start features of this pass; learned: the
+// network's lambda replaces the computed one in this pass's update; prev_mode /
+// acc_mode (0 off, 1 reset, 2 add): accumulate the applied min(0, lambda) into
+// lambda_prev (all passes) / lam_acc (recorded passes); projected: with
+// prev_mode 2, a pull-back lambda up to the substep's accumulated push is applied.
+apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s, bool box_after = false, bool converge = false,
+                              int feature_mode = 0, int acc_mode = 0, bool learned = false, int prev_mode = 0,
+                              bool projected = false);
+constexpr int kMlpParams = 4824;  // floats of the warm-start parameter vector (mlp.cu)
+apbf_status mlp_forward(const float *P, const float *X, uint32_t nrows, float *out, cudaStream_t s);
+apbf_status mlp_train_step(float *P, float *m, float *v, float *partials, const float *X, const float *T,
+                           uint32_t nrows, float lr, float over_weight, uint32_t step, float *grad_out,
+                           float *loss_out, cudaStream_t s);
+uint32_t mlp_partials_floats(uint32_t nrows);
+apbf_status mlp_lambda(apbf_ctx *ctx, cudaStream_t s, bool early_exit);
+apbf_status record_samples(apbf_ctx *ctx, cudaStream_t s);
 apbf_status kw_from_boundary_distance(apbf_ctx *ctx, cudaStream_t s);
 apbf_status spread_kernel_width(apbf_ctx *ctx, cudaStream_t s);
 apbf_status update_transfers(apbf_ctx *ctx, cudaStream_t s);

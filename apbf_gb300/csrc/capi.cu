@@ -127,6 +127,7 @@ apbf_status apbf_create(const apbf_config *cfg, apbf_ctx **out) {
         A(f.kernel_width, cap);
         A(f.boundariness, cap);
         A(f.boundary_distance, cap);
+        A(f.lambda_prev, cap);
         TransferBufs &t = ctx->tr[k];
         A(t.source, tcap);
         A(t.target, tcap);
@@ -159,6 +160,10 @@ apbf_status apbf_create(const apbf_config *cfg, apbf_ctx **out) {
     A(ctx->lambda, cap);
     A(ctx->shift, cap);
     A(ctx->solve_rec, cap);
+    A(ctx->mlp_params, kMlpParams);
+    A(ctx->features, (size_t)cap * 8);
+    A(ctx->selfdir, cap);
+    A(ctx->lam_acc, cap);
     A(ctx->dbg_density, cap);
     A(ctx->dbg_grad, cap);
     A(ctx->dbg_sq, cap);
@@ -189,6 +194,7 @@ apbf_status apbf_create(const apbf_config *cfg, apbf_ctx **out) {
         cudaMemset(ctx->fl[k].pos, 0, (size_t)cap * sizeof(int4));
         cudaMemset(ctx->fl[k].pos_backup, 0, (size_t)cap * sizeof(int4));
         cudaMemset(ctx->fl[k].vel, 0, (size_t)cap * sizeof(float4));
+        cudaMemset(ctx->fl[k].lambda_prev, 0, (size_t)cap * sizeof(float));
         cudaMemset(ctx->fl[k].transferring, 0, (size_t)cap * sizeof(uint32_t));
     }
     e = cudaDeviceSynchronize();
@@ -285,6 +291,8 @@ apbf_status apbf_set_lengths(apbf_ctx *ctx, uint32_t np, uint32_t nt, void *stre
     uint32_t v[2] = {np, nt};
     cudaStream_t s = (cudaStream_t)stream;
     APBF_CUDA(cudaMemcpyAsync(ctx->d_len, v, sizeof(v), cudaMemcpyHostToDevice, s));
+    // a new state has no lambda history (the warm start's previous-substep feature)
+    APBF_CUDA(cudaMemsetAsync(ctx->fl[ctx->fcur].lambda_prev, 0, (size_t)ctx->cfg.particle_capacity * sizeof(float), s));
     APBF_CUDA(cudaStreamSynchronize(s));
     return APBF_OK;
 }
@@ -376,13 +384,28 @@ apbf_status apbf_substep(apbf_ctx *ctx, float dt, void *stream) {
     }
     const bool converge = st.density_error_target > 0.0f;
     if (converge) APBF_CUDA(cudaMemsetAsync(&ctx->status->converged, 0, sizeof(uint32_t), s));
+    const bool recording = ctx->rec_iterations > 0;
+    const bool learned = (ctx->warm_start & APBF_WARM_LEARNED) && ctx->mlp_loaded;
+    const bool projected = (ctx->warm_start & APBF_WARM_PROJECTED) != 0;
+    const bool track = ctx->track_lambda != 0;
     for (int it = 0; it < st.solver_iterations; ++it) {
         if (it == 0 && !fuse_first) {
             r = box_collision(ctx, s);
             if (r != APBF_OK) return r;
         }
-        r = incompressibility(ctx, s, it + 1 < st.solver_iterations, converge);
+        const int feature_mode = it == 0 && (learned || recording) ? 1 : 0;
+        const int acc_mode = recording && (uint32_t)it < ctx->rec_iterations ? (it == 0 ? 1 : 2) : 0;
+        const int prev_mode = track ? (it == 0 ? 1 : 2) : 0;
+        r = incompressibility(ctx, s, it + 1 < st.solver_iterations, converge, feature_mode, acc_mode,
+                              learned && it == 0, prev_mode, projected);
         if (r != APBF_OK) return r;
+    }
+    if (recording) {
+        if (st.solver_iterations > 0) {
+            r = record_samples(ctx, s);
+            if (r != APBF_OK) return r;
+        }
+        ctx->rec_iterations = 0;  // armed for one substep
     }
     if (adaptive) {
         r = update_transfers(ctx, s);
@@ -505,6 +528,65 @@ apbf_status apbf_launch_count(apbf_ctx *ctx, unsigned long long *out) {
     if (!ctx || !out) return APBF_ERR_INVALID_ARG;
     *out = ctx->launches;
     return APBF_OK;
+}
+
+apbf_status apbf_mlp_param_count(uint32_t *out) {
+    if (!out) return APBF_ERR_INVALID_ARG;
+    *out = (uint32_t)kMlpParams;
+    return APBF_OK;
+}
+
+apbf_status apbf_mlp_partials_size(uint32_t n_samples, uint32_t *out_floats) {
+    if (!out_floats) return APBF_ERR_INVALID_ARG;
+    *out_floats = mlp_partials_floats(n_samples);
+    return APBF_OK;
+}
+
+apbf_status apbf_mlp_load(apbf_ctx *ctx, const float *d_params, void *stream) {
+    if (!ctx || !d_params) return APBF_ERR_INVALID_ARG;
+    APBF_CUDA(cudaMemcpyAsync(ctx->mlp_params, d_params, kMlpParams * sizeof(float), cudaMemcpyDeviceToDevice,
+                              (cudaStream_t)stream));
+    ctx->mlp_loaded = 1;
+    return APBF_OK;
+}
+
+apbf_status apbf_set_warm_start(apbf_ctx *ctx, int mode) {
+    if (!ctx || (mode & ~(APBF_WARM_LEARNED | APBF_WARM_PROJECTED))) return APBF_ERR_INVALID_ARG;
+    if ((mode & APBF_WARM_LEARNED) && !ctx->mlp_loaded) {
+        set_error("apbf_set_warm_start: load the network with apbf_mlp_load first");
+        return APBF_ERR_INVALID_ARG;
+    }
+    ctx->warm_start = mode;
+    if (mode) ctx->track_lambda = 1;
+    return APBF_OK;
+}
+
+apbf_status apbf_record_samples(apbf_ctx *ctx, uint32_t iterations, float *d_features, float *d_targets,
+                                uint32_t capacity, uint32_t *d_count) {
+    if (!ctx || !iterations || !d_features || !d_targets || !d_count) return APBF_ERR_INVALID_ARG;
+    ctx->rec_iterations = iterations;
+    ctx->rec_features = d_features;
+    ctx->rec_targets = d_targets;
+    ctx->rec_capacity = capacity;
+    ctx->rec_count = d_count;
+    ctx->track_lambda = 1;
+    return APBF_OK;
+}
+
+apbf_status apbf_mlp_forward(const float *d_params, const float *d_features, uint32_t n, float *d_out, void *stream) {
+    if (!d_params || (n && (!d_features || !d_out))) return APBF_ERR_INVALID_ARG;
+    return mlp_forward(d_params, d_features, n, d_out, (cudaStream_t)stream);
+}
+
+apbf_status apbf_mlp_train_step(float *d_params, float *d_m, float *d_v, float *d_partials, const float *d_features,
+                                const float *d_targets, uint32_t n, float lr, float over_weight, uint32_t step,
+                                float *d_grad, float *d_loss, void *stream) {
+    if (!d_params || !d_m || !d_v || !d_partials || (n && (!d_features || !d_targets)) || !(over_weight > 0.0f)) {
+        set_error("apbf_mlp_train_step: null buffer or over_weight <= 0");
+        return APBF_ERR_INVALID_ARG;
+    }
+    return mlp_train_step(d_params, d_m, d_v, d_partials, d_features, d_targets, n, lr, over_weight, step, d_grad,
+                          d_loss, (cudaStream_t)stream);
 }
 
 static uint32_t bit_length(uint32_t v) {

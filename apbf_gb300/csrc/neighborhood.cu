@@ -62,6 +62,7 @@ __global__ void k_reorder(FluidBufs src, FluidBufs dst, const uint32_t *__restri
         dst.target_radius[k] = src.target_radius[o];
         dst.kernel_width[k] = src.kernel_width[o];
         dst.boundariness[k] = src.boundariness[o];
+        dst.lambda_prev[k] = src.lambda_prev[o];
         dst.boundary_distance[k] = src.boundary_distance[o];
         inv_perm[o] = k;
     }

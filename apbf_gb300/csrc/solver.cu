@@ -46,6 +46,11 @@ struct PassA {
     const uint32_t *d_len;
     Status *st;
     double *red_out;     // [2], [3]: mean compression / absolute error of this pass
+    float *features;     // non-null: the 8 features of this pass (first pass of a substep)
+    float4 *selfdir;     // non-null with features: self-shift direction and inverse mass
+    const float4 *vel;   // velocities, for the divergence feature
+    const float *lam_prev;  // lambda_prev: the previous substep's sum at pass 0, this substep's after
+    int projected;          // 1: pull-back allowed (passes after the first of a warm-started substep)
     float target;        // > 0: set st->converged when the error is at most this
     int early_exit;      // skip the pass when st->converged is set
     float rmin3;  // pow(2 * smallestTargetRadius, 3)
@@ -107,6 +112,9 @@ __global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) 
         int32_t cx = 0, cy = 0, cz = 0, cw = 0;
         const uint32_t cnt = a.count[i];
         const uint32_t *row = a.idx + i;
+        const bool feat = a.features != nullptr;
+        const float4 vi = feat ? a.vel[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        float div = 0.0f;  // sum_j m_j (v_j - v_i) . gradW_ij  (velocity divergence x density)
         // Batches of kUnroll pairs: all row entries, then all neighbour gathers, then
         // the arithmetic, so each thread keeps kUnroll loads in flight.
         for (uint32_t k0 = 0; k0 < cnt; k0 += kUnroll) {
@@ -131,6 +139,10 @@ __global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) 
                 gy = wadd(gy, f2i(g.y * mjf));
                 gz = wadd(gz, f2i(g.z * mjf));
                 sq += f2u(dot3x(g, g) * mjf);
+                if (feat) {
+                    const float4 vj = a.vel[jj[u]];
+                    div += __int_as_float(q.w) * ((vj.x - vi.x) * g.x + (vj.y - vi.y) * g.y + (vj.z - vi.z) * g.z);
+                }
                 if (a.method == 1) {  // incompressibility_1.comp:62-68
                     const float den = kw * APBF_FIX / mjf;
                     cx = wadd(cx, f2i((float)wadd(q.x, -p.x) / den));
@@ -168,10 +180,34 @@ __global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) 
         float lam = under / (ird * ird * (sqs + 0.01f));
         lam /= a.rmin3 / ird * im;
         a.lambda[i] = lam;
-        a.rec[i] = make_float4(lam, c.ivd, c.norm, kw);
+        // The lambda this pass applies: the reference applies only pushes (lambda < 0,
+        // incompressibility_2.comp:106, incompressibility_3.comp:63).  Projected mode
+        // (warm-started solve) also applies a pull-back lambda > 0 where earlier passes
+        // of this substep pushed, up to their sum, so that an over-push is undone; the
+        // density that pull-back would restore counts as error.
+        float applied = lam < 0.0f ? lam : 0.0f;
+        float pull = 0.0f;
+        if (a.projected && lam > 0.0f) {
+            applied = fminf(lam, -a.lam_prev[i]);  // lam_prev: the sum applied so far (<= 0)
+            if (applied > 0.0f) pull = under * (applied / lam);
+            else applied = 0.0f;
+        }
+        a.rec[i] = make_float4(applied, c.ivd, c.norm, kw);
+        if (feat) {
+            float *fo = a.features + (size_t)i * 8;
+            fo[0] = (float)cnt;
+            fo[1] = density * ird - 1.0f;
+            fo[2] = kw / radius;
+            fo[3] = lam;
+            fo[4] = density > 0.0f ? div / density : 0.0f;
+            fo[5] = a.lam_prev[i];
+            fo[6] = 0.0f;
+            fo[7] = 0.0f;
+            a.selfdir[i] = make_float4(-wgs.x * ird, -wgs.y * ird, -wgs.z * ird, im);
+        }
         int4 sh = make_int4(0, 0, 0, 0);
-        if (lam < 0.0f) {
-            const float sc = lam * im * APBF_FIX;
+        if (applied != 0.0f) {
+            const float sc = applied * im * APBF_FIX;
             sh.x = f2i(-wgs.x * ird * sc);
             sh.y = f2i(-wgs.y * ird * sc);
             sh.z = f2i(-wgs.z * ird * sc);
@@ -213,7 +249,7 @@ __global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) 
         }
         a.bness[i] = b;
         const double ratio = (double)density * (double)ird - 1.0;
-        e1 += ratio > 0.0 ? ratio : 0.0;
+        e1 += ratio > 0.0 ? ratio : (double)pull;
         e2 += fabs(ratio);
         if (a.dbg_dens) {
             a.dbg_dens[i] = dens;
@@ -279,14 +315,25 @@ struct PassB {
     const Status *st;
     int gk;
     int early_exit;  // converged: copy the positions unchanged (the buffers swap regardless)
+    float *lam_prev;  // prev_mode / acc_mode (0 off, 1 reset, 2 add): accumulate the lambda
+    float *lam_acc;   // this pass applied (rec.x: the learned one in a learned pass)
+    int prev_mode, acc_mode;
 };
+
+__device__ __forceinline__ void accumulate(float *dst, int mode, uint32_t j, float v) {
+    if (mode == 1) dst[j] = v;
+    else if (mode == 2) dst[j] += v;
+}
 
 template <bool GAUSS>
 __global__ void __launch_bounds__(256, GAUSS ? 5 : 4) k_delta(PassB a) {
     const uint32_t n = a.d_len[kLenParticles];
     if (a.early_exit && *(volatile const uint32_t *)&a.st->converged) {
-        for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+        for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
             a.pos_out[j] = a.pos[j];
+            accumulate(a.lam_prev, a.prev_mode, j, 0.0f);  // nothing applied in this pass
+            accumulate(a.lam_acc, a.acc_mode, j, 0.0f);
+        }
         return;
     }
     const bool sym = a.st->range_min == a.st->range_max;
@@ -312,7 +359,7 @@ __global__ void __launch_bounds__(256, GAUSS ? 5 : 4) k_delta(PassB a) {
 #pragma unroll
             for (int u = 0; u < kUnroll; ++u) {
                 const float lam = k0 + u < cnt ? rr[u].x : 0.0f;
-                if (!(lam < 0.0f)) continue;  // incompressibility_3.comp:63 (also the padding lanes)
+                if (lam == 0.0f) continue;  // the applied lambda (incompressibility_3.comp:63); padding lanes
                 KConst c;
                 c.ivd = rr[u].y;
                 c.norm = rr[u].z;
@@ -333,6 +380,11 @@ __global__ void __launch_bounds__(256, GAUSS ? 5 : 4) k_delta(PassB a) {
         int4 out = make_int4(wadd(p.x, ax), wadd(p.y, ay), wadd(p.z, az), p.w);
         if (a.nboxes) out = box_push(out, a.radius[j], j, a.bmin, a.bmax, a.nboxes);
         a.pos_out[j] = out;
+        if (a.prev_mode | a.acc_mode) {
+            const float lj = reinterpret_cast<const float *>(a.rec + j)[0];  // applied (learned) lambda
+            accumulate(a.lam_prev, a.prev_mode, j, lj);
+            accumulate(a.lam_acc, a.acc_mode, j, lj);
+        }
     }
 }
 
@@ -376,7 +428,8 @@ __global__ void __launch_bounds__(256) k_finalize_mass(const double *partials, i
 
 }  // namespace
 
-apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s, bool box_after, bool converge) {
+apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s, bool box_after, bool converge, int feature_mode,
+                              int acc_mode, bool learned, int prev_mode, bool projected) {
     const uint32_t cap = ctx->cfg.particle_capacity;
     FluidBufs &f = ctx->fl[ctx->fcur];
     FluidBufs &alt = ctx->fl[ctx->fcur ^ 1];
@@ -403,6 +456,11 @@ apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s, bool box_after, boo
     a.red_out = ctx->red_out;
     a.target = converge ? st.density_error_target : 0.0f;
     a.early_exit = converge ? 1 : 0;
+    a.features = feature_mode ? ctx->features : nullptr;
+    a.selfdir = ctx->selfdir;
+    a.vel = f.vel;
+    a.lam_prev = f.lambda_prev;
+    a.projected = projected && prev_mode == 2 ? 1 : 0;
     const float rm2 = 2.0f * st.smallest_target_radius;
     a.rmin3 = rm2 * rm2 * rm2;
     a.hk = st.height_kernel_id;
@@ -420,6 +478,10 @@ apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s, bool box_after, boo
         k_density_lambda<false><<<g, kBlock, 0, s>>>(a);
     APBF_AFTER_LAUNCH(ctx, s, "k_density_lambda");
 
+    if (learned) {  // the network's lambda replaces the plain one in this update
+        apbf_status r = mlp_lambda(ctx, s, converge);
+        if (r != APBF_OK) return r;
+    }
     PassB b;
     b.pos = f.pos;
     b.pos_out = alt.pos;
@@ -438,6 +500,10 @@ apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s, bool box_after, boo
     b.st = ctx->status;
     b.gk = st.gradient_kernel_id;
     b.early_exit = converge ? 1 : 0;
+    b.lam_prev = f.lambda_prev;
+    b.lam_acc = ctx->lam_acc;
+    b.prev_mode = prev_mode;
+    b.acc_mode = acc_mode;
     APBF_BEFORE_LAUNCH(ctx, s, "k_delta");
     if (gauss)
         k_delta<true><<<grid_for(ctx, cap), kBlock, 0, s>>>(b);
@@ -463,6 +529,38 @@ apbf_status reduce_fp64(apbf_ctx *ctx, double out[4], cudaStream_t s) {
     APBF_AFTER_LAUNCH(ctx, s, "k_finalize_mass");
     APBF_CUDA(cudaMemcpyAsync(out, ctx->red_out, 4 * sizeof(double), cudaMemcpyDeviceToHost, s));
     APBF_CUDA(cudaStreamSynchronize(s));
+    return APBF_OK;
+}
+
+namespace {
+// Appends (features, sum of min(0, lambda)) of the particles to the caller's
+// sample buffers, in particle order, up to their capacity.
+__global__ void k_record_append(const float *feat, const float *acc, const uint32_t *d_len, float *out_f,
+                                float *out_t, uint32_t cap, uint32_t *count) {
+    const uint32_t n = d_len[kLenParticles];
+    const uint32_t base = *count;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t r = base + i;
+        if (r >= cap) break;
+        for (int k = 0; k < 8; ++k) out_f[(size_t)r * 8 + k] = feat[(size_t)i * 8 + k];
+        out_t[r] = acc[i];
+    }
+}
+__global__ void k_record_count(const uint32_t *d_len, uint32_t cap, uint32_t *count) {
+    const uint32_t v = *count + d_len[kLenParticles];
+    *count = v < cap ? v : cap;
+}
+}  // namespace
+
+apbf_status record_samples(apbf_ctx *ctx, cudaStream_t s) {
+    const uint32_t cap = ctx->cfg.particle_capacity;
+    APBF_BEFORE_LAUNCH(ctx, s, "k_record_append");
+    k_record_append<<<grid_for(ctx, cap), kBlock, 0, s>>>(ctx->features, ctx->lam_acc, ctx->d_len, ctx->rec_features,
+                                                         ctx->rec_targets, ctx->rec_capacity, ctx->rec_count);
+    APBF_AFTER_LAUNCH(ctx, s, "k_record_append");
+    APBF_BEFORE_LAUNCH(ctx, s, "k_record_count");
+    k_record_count<<<1, 1, 0, s>>>(ctx->d_len, ctx->rec_capacity, ctx->rec_count);
+    APBF_AFTER_LAUNCH(ctx, s, "k_record_count");
     return APBF_OK;
 }
 

@@ -66,9 +66,14 @@ def make_state(pos: np.ndarray, radius: float = 1.0) -> dict:
     }
 
 
-def wall_boxes(a_min, a_max, radius: float = 1.0, lid: bool = True):
-    """pool.cpp:30-40: walls of thickness 4 around [a_min, a_max + (0, 2r, 0)]."""
-    t = 4.0
+def wall_boxes(a_min, a_max, radius: float = 1.0, lid: bool = True, thickness: float = 4.0):
+    """pool.cpp:30-40: walls of thickness 4 around [a_min, a_max + (0, 2r, 0)].
+
+    box_collision pushes a particle out through the nearest face of a box
+    (box_collision.comp:45-57), so a particle that moves more than half the wall
+    thickness into a wall in one substep leaves through the far side; scenes with
+    fast impacts pass a larger thickness."""
+    t = float(thickness)
     wmin = np.asarray(a_min, np.float64) - t
     wmax = np.asarray(a_max, np.float64) + t + np.array([0.0, 2.0 * radius, 0.0])
     boxes = [
@@ -119,7 +124,8 @@ def dam_break(n_side: int = 32, seed: int = 0, substeps: int = 200, iterations: 
     box = np.array([3.2, 1.6, 1.6]) / r_m  # 128 x 64 x 64
     pos = lattice([1.0, 1.0, 1.0], [n_side] * 3, 2.0, 0.005 / r_m, rng)
     st = make_state(pos)
-    bmin, bmax = wall_boxes([0, 0, 0], box)
+    # the front reaches ~2 radii per substep: 16-radius walls keep it inside
+    bmin, bmax = wall_boxes([0, 0, 0], box, thickness=16.0)
     gmin, gmax, L = _grid_for([0, 0, 0], box)
     return SceneSpec("dam_break", st, bmin, bmax, gmin, gmax, L, (0.0, -9.81 / r_m, 0.0), 1.0 / 120.0, iterations,
                      substeps, True, {"r_m": r_m, "box": box.tolist()})
@@ -154,8 +160,11 @@ def water_drop(total: int = 250_000, seed: int = 0, substeps: int = 500, iterati
         pool = np.concatenate([pool, top], axis=0)
     pos = np.concatenate([pool, sp], axis=0)
     st = make_state(pos)
-    bmin, bmax = wall_boxes([0, 0, 0], box, lid=False)
     hi = np.maximum(box, centre + R + 2)
+    # the drop hits the floor at ~3 radii per substep: 32-radius walls, as high as
+    # the drop's start and closed by a lid there, so that the splash stays inside the
+    # search grid (particles outside it are clamped into its border cells)
+    bmin, bmax = wall_boxes([0, 0, 0], [box[0], hi[1], box[2]], lid=True, thickness=32.0)
     gmin, gmax, L = _grid_for([0, 0, 0], hi)
     # free fall of the drop onto the pool surface: (1.0 m - 0.3 m - fill) / (g/2) -> ~90 substeps at 250k
     fall = max(centre[1] - R - 2.0 * (layers + 1), 0.0) * r_m

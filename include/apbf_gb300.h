@@ -246,6 +246,55 @@ apbf_status apbf_profile_read(apbf_ctx *ctx, apbf_kernel_time *out, uint32_t cap
 /* Number of kernels this context has launched since creation. */
 apbf_status apbf_launch_count(apbf_ctx *ctx, unsigned long long *out);
 
+/* ---- learned warm start of the Jacobi solve (no reference counterpart) ----
+ * A 6 -> 64 -> 64 -> 1 ReLU network (BF16 weights, FP32 accumulation, tensor
+ * cores) maps per-particle features of the first density pass of a substep --
+ * neighbour count, rho/rho0 - 1, kernel width / radius, the plain Jacobi lambda,
+ * velocity divergence / density, the sum of the lambdas applied to the particle
+ * in the previous substep (8 slots, 6 used) -- to the lambda used by that
+ * substep's first position update.  Later iterations are the plain solve, which stays the judge of the
+ * density error (density_error_target).  Parameters are one FP32 vector of
+ * apbf_mlp_param_count() floats: mu[8], 1/sigma[8], W1[64][8], b1[64],
+ * W2[64][64], b2[64], w3[64], b3, y_scale, y_mean (lambda = y * y_scale + y_mean),
+ * omega_max (> 0: the learned lambda is clamped to [omega_max * lambda, lambda]
+ * where the plain lambda of the pass is negative and is 0 elsewhere),
+ * min_neighbors (a particle with fewer neighbours keeps the plain lambda), three
+ * reserved floats. */
+apbf_status apbf_mlp_param_count(uint32_t *out);
+/* Floats of scratch apbf_mlp_train_step needs for n_samples samples. */
+apbf_status apbf_mlp_partials_size(uint32_t n_samples, uint32_t *out_floats);
+/* Copies device parameters into the context. */
+apbf_status apbf_mlp_load(apbf_ctx *ctx, const float *d_params, void *stream);
+/* Warm-start mode of apbf_substep, a combination of:
+ *   APBF_WARM_LEARNED    the first position update uses the network's lambda;
+ *   APBF_WARM_PROJECTED  the later passes of the substep may apply a pull-back
+ *                        (lambda > 0) up to the lambda sum the particle was pushed
+ *                        with earlier in the substep, so an over-push is undone,
+ *                        and the density that pull-back would restore counts in
+ *                        the density error that density_error_target tests.
+ * 0 is the reference's solve. */
+#define APBF_WARM_LEARNED 1
+#define APBF_WARM_PROJECTED 2
+apbf_status apbf_set_warm_start(apbf_ctx *ctx, int mode);
+/* Arms the next apbf_substep to append one training sample per particle: its 8
+ * features (first density pass) and the sum of min(0, lambda) over the first
+ * `iterations` plain Jacobi iterations; d_count (device) is advanced, at most
+ * `capacity` samples are kept. */
+apbf_status apbf_record_samples(apbf_ctx *ctx, uint32_t iterations, float *d_features, float *d_targets,
+                                uint32_t capacity, uint32_t *d_count);
+/* Inference on n feature rows (8 floats each): d_out = lambda in physical units. */
+apbf_status apbf_mlp_forward(const float *d_params, const float *d_features, uint32_t n, float *d_out, void *stream);
+/* One Adam step (lr; step = number of earlier steps) on the weighted mean squared
+ * error between the normalised output y and d_targets t (already normalised):
+ * mean of w (y - t)^2 with w = over_weight (> 0) where y < t -- a larger push than
+ * the target -- and 1 elsewhere (over_weight = 1: plain least squares).
+ * d_partials holds apbf_mlp_partials_size(n) floats; d_grad (may be NULL)
+ * receives the gradient, d_loss (may be NULL) the loss.  lr = 0 leaves the
+ * parameters and moments unchanged. */
+apbf_status apbf_mlp_train_step(float *d_params, float *d_m, float *d_v, float *d_partials, const float *d_features,
+                                const float *d_targets, uint32_t n, float lr, float over_weight, uint32_t step,
+                                float *d_grad, float *d_loss, void *stream);
+
 /* ---- parallel primitives (source/algorithms.h:12-17) ---- */
 /* algorithms::sort (source/algorithms.cpp:59-91): stable sort of (key, value) pairs
  * by key; only key bits below the highest set bit of value_upper_bound are used.

@@ -493,6 +493,7 @@ void or_incompressibility_apply(or_fluid *f, const or_neighbors *nb, const or_se
     uint32_t *sq = (uint32_t *)calloc(n ? n : 1, sizeof(uint32_t));
     int32_t *com = (int32_t *)calloc(4 * (size_t)(n ? n : 1), sizeof(int32_t));
     double *lambda = (double *)calloc(n ? n : 1, sizeof(double));
+    double *div = (double *)calloc(n ? n : 1, sizeof(double));
     int32_t *shift = (int32_t *)calloc(3 * (size_t)(n ? n : 1), sizeof(int32_t));
     const double R = OR_POS_RESOLUTION;
 
@@ -515,6 +516,7 @@ void or_incompressibility_apply(or_fluid *f, const or_neighbors *nb, const or_se
             dens[i] += f2u(or_kernel_height(s->height_kernel_id, d, kw) / imn * R);
             for (int c = 0; c < 3; ++c) gsum[3 * i + c] = wrap_add(gsum[3 * i + c], f2i(g[c] / imn * R));
             sq[i] += f2u(dot3(g, g) / imn * R);
+            for (int c = 0; c < 3; ++c) div[i] += ((double)f->vel[4 * (size_t)j + c] - f->vel[4 * (size_t)i + c]) * g[c] / imn;
             if (s->boundariness_calculation_method == 1) {
                 for (int c = 0; c < 3; ++c)
                     com[4 * i + c] = wrap_add(com[4 * i + c],
@@ -552,9 +554,20 @@ void or_incompressibility_apply(or_fluid *f, const or_neighbors *nb, const or_se
         double lam = under / (ird * ird * (sqs + F32(0.01f)));
         double rmin2 = 2.0 * (double)s->smallest_target_radius;
         lam /= (rmin2 * rmin2 * rmin2) / ird * im;
-        lambda[i] = lam;
-        if (lam < 0.0) {
-            for (int c = 0; c < 3; ++c) shift[3 * i + c] = wrap_add(shift[3 * i + c], f2i(-wgs[c] * ird * (lam * im * R)));
+        /* the applied lambda: pushes only (incompressibility_2.comp:106) */
+        double applied = lam < 0.0 ? lam : 0.0;
+        if (out && out->lambda_in) {
+            if (out->lambda) out->lambda[i] = (float)lam;  /* the computed one, before the override */
+            applied = (double)out->lambda_in[i];
+        } else if (out && out->projected_acc && lam > 0.0) {
+            double a = fmin(lam, -(double)out->projected_acc[i]);
+            applied = a > 0.0 ? a : 0.0;
+        }
+        if (out && out->lambda && !out->lambda_in) out->lambda[i] = (float)lam;
+        if (out && out->applied) out->applied[i] = (float)applied;
+        lambda[i] = applied;
+        if (applied != 0.0) {
+            for (int c = 0; c < 3; ++c) shift[3 * i + c] = wrap_add(shift[3 * i + c], f2i(-wgs[c] * ird * (applied * im * R)));
         }
     }
     /* incompressibility_3.comp:48-67 */
@@ -577,7 +590,7 @@ void or_incompressibility_apply(or_fluid *f, const or_neighbors *nb, const or_se
                     if (dd > F32(0.6f)) f->boundariness[i] = 0.0f;
                 }
             }
-            if (!(lambda[i] < 0.0)) continue;
+            if (lambda[i] == 0.0) continue;
             for (int c = 0; c < 3; ++c) shift[3 * j + c] = wrap_add(shift[3 * j + c], f2i(g[c] * (lambda[i] * R)));
         }
     }
@@ -587,10 +600,10 @@ void or_incompressibility_apply(or_fluid *f, const or_neighbors *nb, const or_se
         if (out->density) memcpy(out->density, dens, n * sizeof(uint32_t));
         if (out->grad_sum) memcpy(out->grad_sum, gsum, 3 * (size_t)n * sizeof(int32_t));
         if (out->sq_grad_sum) memcpy(out->sq_grad_sum, sq, n * sizeof(uint32_t));
-        if (out->lambda)
-            for (uint32_t i = 0; i < n; ++i) out->lambda[i] = (float)lambda[i];
+        if (out->divergence)
+            for (uint32_t i = 0; i < n; ++i) out->divergence[i] = (float)div[i];
     }
-    free(dens); free(gsum); free(sq); free(com); free(lambda); free(shift);
+    free(dens); free(gsum); free(sq); free(com); free(lambda); free(shift); free(div);
 }
 
 /* ------------------------------------------------------------------ */

@@ -161,6 +161,18 @@ typedef struct or_incomp_out {
     int32_t *grad_sum;      /* 3n */
     uint32_t *sq_grad_sum;  /* n */
     float *lambda;          /* n */
+    /* Learned warm start (no reference counterpart): per-particle velocity
+     * divergence x density, sum_j m_j (v_j - v_i) . gradW_ij, of this pass (out);
+     * and, when non-NULL, the lambda that replaces the computed one in this
+     * pass's position update (in). */
+    float *divergence;      /* n */
+    const float *lambda_in; /* n */
+    /* Projected pass of a warm-started substep (no reference counterpart): when
+     * non-NULL, the sum of the lambdas applied to each particle earlier in the
+     * substep (<= 0); a positive lambda is then applied up to minus that sum
+     * (pull-back).  `applied` (out) receives the lambda each particle applied. */
+    const float *projected_acc; /* n */
+    float *applied;             /* n */
 } or_incomp_out;
 void or_incompressibility_apply(or_fluid *f, const or_neighbors *nb, const or_settings *s,
                                 or_incomp_out *out);

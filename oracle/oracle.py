@@ -81,7 +81,8 @@ class OrBoxes(C.Structure):
 
 
 class OrIncompOut(C.Structure):
-    _fields_ = [("density", _u32p), ("grad_sum", _i32p), ("sq_grad_sum", _u32p), ("lambda_", _f32p)]
+    _fields_ = [("density", _u32p), ("grad_sum", _i32p), ("sq_grad_sum", _u32p), ("lambda_", _f32p),
+                ("divergence", _f32p), ("lambda_in", _f32p), ("projected_acc", _f32p), ("applied", _f32p)]
 
 
 class OrScene(C.Structure):
@@ -288,12 +289,23 @@ def set_rows(fs: FluidState, rows: list) -> None:
 
 
 # ---------------------------------------------------------------- stages
-def incompressibility(fs: FluidState, settings: OrSettings) -> dict:
+def incompressibility(fs: FluidState, settings: OrSettings, lambda_in: np.ndarray | None = None,
+                      projected_acc: np.ndarray | None = None) -> dict:
+    """One Jacobi pass.  lambda_in (optional): the lambda that the position update
+    uses instead of the computed one (the learned warm start's first update);
+    projected_acc (optional): the lambdas applied earlier in the substep, enabling
+    the pull-back of a projected pass.  out["lambda"] is always the computed one,
+    out["applied"] the one the update used."""
     n = fs.n
     out = {"density": np.zeros(n, np.uint32), "grad_sum": np.zeros((n, 3), np.int32),
-           "sq_grad_sum": np.zeros(n, np.uint32), "lambda": np.zeros(n, np.float32)}
+           "sq_grad_sum": np.zeros(n, np.uint32), "lambda": np.zeros(n, np.float32),
+           "divergence": np.zeros(n, np.float32), "applied": np.zeros(n, np.float32)}
+    lin = None if lambda_in is None else np.ascontiguousarray(lambda_in, np.float32)
+    acc = None if projected_acc is None else np.ascontiguousarray(projected_acc, np.float32)
     o = OrIncompOut(_p(out["density"], _u32p), _p(out["grad_sum"], _i32p), _p(out["sq_grad_sum"], _u32p),
-                    _p(out["lambda"], _f32p))
+                    _p(out["lambda"], _f32p), _p(out["divergence"], _f32p),
+                    _p(lin, _f32p) if lin is not None else None, _p(acc, _f32p) if acc is not None else None,
+                    _p(out["applied"], _f32p))
     lib().or_incompressibility_apply(C.byref(fs.f), C.byref(fs.nb), C.byref(settings), C.byref(o))
     return out
 
