@@ -131,7 +131,7 @@ class StatusInfo(C.Structure):
         ("required_particles", C.c_uint32),
         ("pairs", C.c_ulonglong),
         ("density_passes", C.c_uint32),
-        ("pad", C.c_uint32),
+        ("converged_substeps", C.c_uint32),
     ]
 
 
@@ -181,6 +181,7 @@ SIGNATURES = {
     "apbf_mlp_partials_size": (_ST, [C.c_uint32, C.POINTER(C.c_uint32)]),
     "apbf_mlp_load": (_ST, [_P, _P, _P]),
     "apbf_set_warm_start": (_ST, [_P, C.c_int]),
+    "apbf_set_solve_graph": (_ST, [_P, C.c_int]),
     "apbf_record_samples": (_ST, [_P, C.c_uint32, _P, _P, C.c_uint32, _P]),
     "apbf_mlp_forward": (_ST, [_P, _P, C.c_uint32, _P, _P]),
     "apbf_mlp_train_step": (_ST, [_P, _P, _P, _P, _P, _P, C.c_uint32, C.c_float, C.c_float, C.c_uint32, _P, _P,

@@ -131,6 +131,10 @@ class Context:
     def set_debug(self, enable: bool) -> None:
         N.check(self.lib.apbf_set_debug(self.handle, 1 if enable else 0), "apbf_set_debug")
 
+    def set_solve_graph(self, enable: bool) -> None:
+        """Jacobi passes 1.. of a substep as one graph launch with a device-side loop (default on)."""
+        N.check(self.lib.apbf_set_solve_graph(self.handle, 1 if enable else 0), "apbf_set_solve_graph")
+
     # ---- lists ----
     def fluid_view(self) -> dict:
         v = N.FluidView()

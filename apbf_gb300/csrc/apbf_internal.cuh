@@ -61,7 +61,9 @@ struct Status {
     uint32_t density_passes;       // density passes executed (not skipped after convergence)
     uint32_t converged;            // set by a density pass whose error met the target
     uint32_t done_blocks;          // last-block counter of the density pass reduction
-    uint32_t pad[3];
+    uint32_t converged_substeps;   // substeps in which a density pass met the target
+    uint32_t pass_index;           // solve loop graph: index of the first pass of the current body run
+    uint32_t loop_iters;           // solve loop graph: body runs since the context was created
 };
 
 // Device length block.
@@ -98,6 +100,15 @@ struct ProfSlot {
     const char *name;
     cudaEvent_t a, b;
 };
+
+// One instantiated solve loop (graph.cu): a while-conditional graph node whose
+// body runs two Jacobi passes and decides on the device whether to go on.
+struct SolveGraph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    unsigned long long key[4] = {0, 0, 0, 0};
+};
+constexpr int kSolveGraphs = 4;
 }  // namespace apbf
 
 struct apbf_ctx {
@@ -190,6 +201,15 @@ struct apbf_ctx {
     unsigned long long prof_dropped = 0;
     unsigned long long launches = 0;
     apbf::ProfSlot *prof_open = nullptr;
+    bool capturing = false;        // launches go into a graph being built: not counted
+
+    // solve loop graphs (graph.cu)
+    int use_graphs = 1;
+    unsigned long long graph_version = 1;  // bumped by every change captured by value
+    apbf::SolveGraph solve_graphs[apbf::kSolveGraphs];
+    int solve_graph_next = 0;
+    cudaStream_t capture_stream = nullptr;
+    unsigned long long loop_launches_per_iter = 0;  // kernel nodes per body run
 };
 
 namespace apbf {
@@ -210,6 +230,7 @@ apbf_status cuda_check(cudaError_t e, const char *what);
 // Kernel-launch bookkeeping: every launch is counted; when tracing is on, a
 // pair of events is recorded around it on the launching stream.
 inline void before_launch(apbf_ctx *c, cudaStream_t s, const char *name) {
+    if (c->capturing) return;
     ++c->launches;
     c->prof_open = nullptr;
     if (!c->prof_on) return;
@@ -223,6 +244,7 @@ inline void before_launch(apbf_ctx *c, cudaStream_t s, const char *name) {
     c->prof_open = slot;
 }
 inline void after_launch(apbf_ctx *c, cudaStream_t s) {
+    if (c->capturing) return;
     if (c->prof_open) cudaEventRecord(c->prof_open->b, s);
     c->prof_open = nullptr;
 }
@@ -254,14 +276,22 @@ apbf_status box_collision(apbf_ctx *ctx, cudaStream_t s);
 // feature_mode: 0 none, 1 write features + self-shift direction; acc_mode: 0 none,
 // 1 lam_acc = min(0, lambda), 2 lam_acc += min(0, lambda); learned: the first
 // position update takes lambda from the network.
-// feature_mode 1: write the warm-start features of this pass; learned: the
-// network's lambda replaces the computed one in this pass's update; prev_mode /
-// acc_mode (0 off, 1 reset, 2 add): accumulate the applied min(0, lambda) into
-// lambda_prev (all passes) / lam_acc (recorded passes); projected: with
-// prev_mode 2, a pull-back lambda up to the substep's accumulated push is applied.
-apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s, bool box_after = false, bool converge = false,
-                              int feature_mode = 0, int acc_mode = 0, bool learned = false, int prev_mode = 0,
-                              bool projected = false);
+// Options of one Jacobi pass (density + lambda, then position update).
+struct SolveOpts {
+    bool box_after = false;   // box collision of the next iteration applied to this pass's output
+    bool converge = false;    // density_error_target > 0: skip the pass once a pass met it
+    int feature_mode = 0;     // 1: write the warm-start features (first pass of a substep)
+    int acc_mode = 0;         // lam_acc: 0 off, 1 reset, 2 add the applied lambda (recorded passes)
+    bool learned = false;     // the network's lambda replaces the computed one in this update
+    int prev_mode = 0;        // lambda_prev: 0 off, 1 reset, 2 add the applied lambda
+    bool projected = false;   // with prev_mode 2: pull-back up to the substep's accumulated push
+    int loop_offset = -1;     // >= 0: a pass of the solve loop graph, number = pass_index + offset;
+    uint32_t max_passes = 0;  //   skipped from max_passes on, box after it unless it is the last
+};
+apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s, const SolveOpts &o = SolveOpts());
+// Passes 1.. of a substep as one graph launch (a device-side while loop).
+apbf_status solve_loop(apbf_ctx *ctx, cudaStream_t s, const SolveOpts &o);
+void destroy_solve_graphs(apbf_ctx *ctx);
 constexpr int kMlpParams = 4824;  // floats of the warm-start parameter vector (mlp.cu)
 apbf_status mlp_forward(const float *P, const float *X, uint32_t nrows, float *out, cudaStream_t s);
 apbf_status mlp_train_step(float *P, float *m, float *v, float *partials, const float *X, const float *T,

@@ -76,6 +76,8 @@ apbf_status apbf_destroy(apbf_ctx *ctx) {
         cudaEventDestroy(p.a);
         cudaEventDestroy(p.b);
     }
+    destroy_solve_graphs(ctx);
+    if (ctx->capture_stream) cudaStreamDestroy(ctx->capture_stream);
     for (void *p : ctx->owned) cudaFree(p);
     delete ctx;
     return APBF_OK;
@@ -214,6 +216,7 @@ apbf_status apbf_set_settings(apbf_ctx *ctx, const apbf_settings *s) {
         return APBF_ERR_INVALID_ARG;
     }
     ctx->settings = *s;
+    ctx->graph_version++;  // solve loop graphs hold settings by value
     return APBF_OK;
 }
 
@@ -235,12 +238,21 @@ apbf_status apbf_set_boxes(apbf_ctx *ctx, const float *bmin, const float *bmax, 
         APBF_CUDA(cudaMemcpy(ctx->box_max, bmax, n * sizeof(float4), cudaMemcpyHostToDevice));
     }
     ctx->n_boxes = n;
+    ctx->graph_version++;
     return APBF_OK;
 }
 
 apbf_status apbf_set_debug(apbf_ctx *ctx, int enable) {
     if (!ctx) return APBF_ERR_INVALID_ARG;
     ctx->debug = enable ? 1 : 0;
+    ctx->graph_version++;
+    return APBF_OK;
+}
+
+apbf_status apbf_set_solve_graph(apbf_ctx *ctx, int enable) {
+    if (!ctx) return APBF_ERR_INVALID_ARG;
+    ctx->use_graphs = enable ? 1 : 0;
+    if (!enable) destroy_solve_graphs(ctx);
     return APBF_OK;
 }
 
@@ -388,16 +400,31 @@ apbf_status apbf_substep(apbf_ctx *ctx, float dt, void *stream) {
     const bool learned = (ctx->warm_start & APBF_WARM_LEARNED) && ctx->mlp_loaded;
     const bool projected = (ctx->warm_start & APBF_WARM_PROJECTED) != 0;
     const bool track = ctx->track_lambda != 0;
+    // Passes 1.. as one graph launch whose while loop stops on the device (at
+    // convergence or after solver_iterations passes), instead of one launch pair per
+    // possible pass; not while tracing, debugging or recording.
+    const bool loop_graph = ctx->use_graphs && !ctx->prof_on && !ctx->debug && !recording &&
+                            st.solver_iterations >= 2;
     for (int it = 0; it < st.solver_iterations; ++it) {
         if (it == 0 && !fuse_first) {
             r = box_collision(ctx, s);
             if (r != APBF_OK) return r;
         }
-        const int feature_mode = it == 0 && (learned || recording) ? 1 : 0;
-        const int acc_mode = recording && (uint32_t)it < ctx->rec_iterations ? (it == 0 ? 1 : 2) : 0;
-        const int prev_mode = track ? (it == 0 ? 1 : 2) : 0;
-        r = incompressibility(ctx, s, it + 1 < st.solver_iterations, converge, feature_mode, acc_mode,
-                              learned && it == 0, prev_mode, projected);
+        SolveOpts o;
+        o.box_after = it + 1 < st.solver_iterations;
+        o.converge = converge;
+        o.feature_mode = it == 0 && (learned || recording) ? 1 : 0;
+        o.acc_mode = recording && (uint32_t)it < ctx->rec_iterations ? (it == 0 ? 1 : 2) : 0;
+        o.learned = learned && it == 0;
+        o.prev_mode = track ? (it == 0 ? 1 : 2) : 0;
+        o.projected = projected;
+        if (it == 1 && loop_graph) {
+            o.max_passes = (uint32_t)st.solver_iterations;
+            r = solve_loop(ctx, s, o);
+            if (r != APBF_OK) return r;
+            break;
+        }
+        r = incompressibility(ctx, s, o);
         if (r != APBF_OK) return r;
     }
     if (recording) {
@@ -433,12 +460,14 @@ apbf_status apbf_get_status(apbf_ctx *ctx, apbf_status_info *out, int clear, voi
     out->required_particles = hs.required_particles;
     out->pairs = pairs;
     out->density_passes = hs.density_passes;
+    out->converged_substeps = hs.converged_substeps;
     if (clear) {
         Status z = hs;
         z.flags = 0;
         z.required_neighbors = z.required_transfers = z.required_particles = 0;
         z.spin_where = 0;
         z.density_passes = 0;
+        z.converged_substeps = 0;
         APBF_CUDA(cudaMemcpyAsync(ctx->status, &z, sizeof(Status), cudaMemcpyHostToDevice, s));
         APBF_CUDA(cudaStreamSynchronize(s));
     }
@@ -526,7 +555,11 @@ apbf_status apbf_profile_read(apbf_ctx *ctx, apbf_kernel_time *out, uint32_t cap
 
 apbf_status apbf_launch_count(apbf_ctx *ctx, unsigned long long *out) {
     if (!ctx || !out) return APBF_ERR_INVALID_ARG;
-    *out = ctx->launches;
+    // kernels run by solve loop graphs: the body's kernel nodes per loop iteration
+    uint32_t iters = 0;
+    cudaSetDevice(ctx->device);
+    APBF_CUDA(cudaMemcpy(&iters, &ctx->status->loop_iters, sizeof(iters), cudaMemcpyDeviceToHost));
+    *out = ctx->launches + (unsigned long long)iters * ctx->loop_launches_per_iter;
     return APBF_OK;
 }
 

@@ -51,6 +51,8 @@ struct PassA {
     const float4 *vel;   // velocities, for the divergence feature
     const float *lam_prev;  // lambda_prev: the previous substep's sum at pass 0, this substep's after
     int projected;          // 1: pull-back allowed (passes after the first of a warm-started substep)
+    int loop_offset;        // >= 0: solve loop pass number = st->pass_index + loop_offset
+    uint32_t max_passes;    // loop passes from this number on are skipped
     float target;        // > 0: set st->converged when the error is at most this
     int early_exit;      // skip the pass when st->converged is set
     float rmin3;  // pow(2 * smallestTargetRadius, 3)
@@ -99,6 +101,7 @@ constexpr int kUnroll = 4;
 template <bool GAUSS>
 __global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) {
     if (a.early_exit && *(volatile uint32_t *)&a.st->converged) return;  // uniform over the grid
+    if (a.loop_offset >= 0 && a.st->pass_index + (uint32_t)a.loop_offset >= a.max_passes) return;
     const uint32_t n = a.d_len[kLenParticles];
     double e1 = 0.0, e2 = 0.0;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -294,7 +297,10 @@ __global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) 
         a.red_out[3] = m2;
         a.st->density_passes += 1u;
         a.st->done_blocks = 0u;
-        if (a.target > 0.0f && m1 <= (double)a.target) a.st->converged = 1u;
+        if (a.target > 0.0f && m1 <= (double)a.target) {
+            a.st->converged = 1u;  // the remaining passes of the substep are skipped
+            a.st->converged_substeps += 1u;
+        }
     }
 }
 
@@ -318,6 +324,8 @@ struct PassB {
     float *lam_prev;  // prev_mode / acc_mode (0 off, 1 reset, 2 add): accumulate the lambda
     float *lam_acc;   // this pass applied (rec.x: the learned one in a learned pass)
     int prev_mode, acc_mode;
+    int loop_offset;      // >= 0: solve loop pass number = st->pass_index + loop_offset
+    uint32_t max_passes;  // loop passes from this number on copy through; box after all but the last
 };
 
 __device__ __forceinline__ void accumulate(float *dst, int mode, uint32_t j, float v) {
@@ -328,7 +336,14 @@ __device__ __forceinline__ void accumulate(float *dst, int mode, uint32_t j, flo
 template <bool GAUSS>
 __global__ void __launch_bounds__(256, GAUSS ? 5 : 4) k_delta(PassB a) {
     const uint32_t n = a.d_len[kLenParticles];
-    if (a.early_exit && *(volatile const uint32_t *)&a.st->converged) {
+    bool skip = a.early_exit && *(volatile const uint32_t *)&a.st->converged;
+    uint32_t nboxes = a.nboxes;
+    if (a.loop_offset >= 0) {
+        const uint32_t pass = a.st->pass_index + (uint32_t)a.loop_offset;
+        skip = skip || pass >= a.max_passes;
+        if (pass + 1u >= a.max_passes) nboxes = 0u;  // no box collision after the last iteration
+    }
+    if (skip) {
         for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
             a.pos_out[j] = a.pos[j];
             accumulate(a.lam_prev, a.prev_mode, j, 0.0f);  // nothing applied in this pass
@@ -378,7 +393,7 @@ __global__ void __launch_bounds__(256, GAUSS ? 5 : 4) k_delta(PassB a) {
             }
         }
         int4 out = make_int4(wadd(p.x, ax), wadd(p.y, ay), wadd(p.z, az), p.w);
-        if (a.nboxes) out = box_push(out, a.radius[j], j, a.bmin, a.bmax, a.nboxes);
+        if (nboxes) out = box_push(out, a.radius[j], j, a.bmin, a.bmax, nboxes);
         a.pos_out[j] = out;
         if (a.prev_mode | a.acc_mode) {
             const float lj = reinterpret_cast<const float *>(a.rec + j)[0];  // applied (learned) lambda
@@ -428,8 +443,9 @@ __global__ void __launch_bounds__(256) k_finalize_mass(const double *partials, i
 
 }  // namespace
 
-apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s, bool box_after, bool converge, int feature_mode,
-                              int acc_mode, bool learned, int prev_mode, bool projected) {
+apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s, const SolveOpts &o) {
+    const bool box_after = o.box_after, converge = o.converge, learned = o.learned, projected = o.projected;
+    const int feature_mode = o.feature_mode, acc_mode = o.acc_mode, prev_mode = o.prev_mode;
     const uint32_t cap = ctx->cfg.particle_capacity;
     FluidBufs &f = ctx->fl[ctx->fcur];
     FluidBufs &alt = ctx->fl[ctx->fcur ^ 1];
@@ -461,6 +477,8 @@ apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s, bool box_after, boo
     a.vel = f.vel;
     a.lam_prev = f.lambda_prev;
     a.projected = projected && prev_mode == 2 ? 1 : 0;
+    a.loop_offset = o.loop_offset;
+    a.max_passes = o.max_passes;
     const float rm2 = 2.0f * st.smallest_target_radius;
     a.rmin3 = rm2 * rm2 * rm2;
     a.hk = st.height_kernel_id;
@@ -504,6 +522,8 @@ apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s, bool box_after, boo
     b.lam_acc = ctx->lam_acc;
     b.prev_mode = prev_mode;
     b.acc_mode = acc_mode;
+    b.loop_offset = o.loop_offset;
+    b.max_passes = o.max_passes;
     APBF_BEFORE_LAUNCH(ctx, s, "k_delta");
     if (gauss)
         k_delta<true><<<grid_for(ctx, cap), kBlock, 0, s>>>(b);

@@ -61,7 +61,7 @@ def settings_dict(spec) -> dict:
 
     s = default_settings()
     s.basic_pbf = 1 if spec.basic_pbf else 0
-    s.solver_iterations = 20
+    s.solver_iterations = 100
     s.density_error_target = 0.001
     return {f: getattr(s, f) for f, _ in s._fields_ if not f.startswith("pad")}
 
@@ -229,6 +229,136 @@ def run_reference(args) -> None:
 
 
 # ----------------------------------------------------------------------------- ours
+def _make_ctx(spec, args, local, mode: int = 0, net=None):
+    from apbf_gb300.api import Context
+
+    cap = int(spec.n * 1.25) + 1024
+    ctx = Context(particle_capacity=cap, max_neighbors=args.max_neighbors, max_log2res=max(spec.log2res, 3),
+                  device=local)
+    # iterate every substep until the mean density error is at most the target
+    ctx.set_settings(basic_pbf=1 if spec.basic_pbf else 0, solver_iterations=args.max_iterations,
+                     density_error_target=args.error_target)
+    ctx.set_scene(spec.grid_min, spec.grid_max, spec.log2res, spec.acceleration)
+    ctx.set_boxes(spec.box_min, spec.box_max)
+    ctx.upload(spec.state)
+    if net is not None:
+        ctx.mlp_load(net.params)
+    if mode:
+        ctx.set_warm_start(mode)
+    return ctx
+
+
+def train_warm_start(args, local: int, rank: int) -> tuple[object, dict]:
+    """Untimed: samples from projected-rule rollouts of two scenes with seeds that the
+    timed scene does not use, then minibatch Adam with the project's kernels."""
+    import torch
+
+    from apbf_gb300 import _native as N
+    from apbf_gb300.warmstart import SampleBuffer, WarmStartNet, record_rollout
+
+    t0 = time.perf_counter()
+    seeds = [1000 + 10 * rank + k for k in (1, 2)]
+    specs = [make_spec(args.workload, seed=s) for s in seeds]
+    per = [sp.meta.get("presteps", 0) + 60 for sp in specs]
+    cap = sum(int(sp.n * 1.3) * ((p + 2) // 3 + 1) for sp, p in zip(specs, per))
+    buf = SampleBuffer.allocate(cap, device=local)
+    for sp, p in zip(specs, per):
+        ctx = _make_ctx(sp, args, local, N.WARM_PROJECTED)
+        record_rollout(ctx, sp.dt, p, buf, iterations=args.max_iterations, every=3)
+        ctx.check_status()
+        ctx.close()
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    X, T = buf.view()
+    net = WarmStartNet(device=local, seed=0)
+    net.set_normalization(X, T)
+    hist = net.fit(X, T, epochs=args.ws_epochs, batch=32768, lr=2e-3, lr_final=2e-4)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    net.min_neighbors = args.ws_min_neighbors
+    net.omega_max = args.ws_omega
+    info = {"samples": int(X.shape[0]), "rollout_seeds": seeds, "substeps_per_rollout": per,
+            "target": "sum of the lambdas applied over all passes of a projected-rule substep",
+            "epochs": args.ws_epochs, "loss_per_epoch": [round(h, 5) for h in hist],
+            "collect_s": round(t1 - t0, 3), "train_s": round(t2 - t1, 3),
+            "guards": {"min_neighbors": args.ws_min_neighbors, "omega_max": args.ws_omega}}
+    del buf
+    return net, info
+
+
+def _state_summary(ctx) -> dict:
+    g, _ = ctx.download()
+    v = g["velocity"][:, :3].astype(np.float64)
+    y = g["position"][:, 1].astype(np.float64) / 262144.0
+    red = ctx.reduce_fp64()
+    return {"mean_v2": round(float(np.mean(np.sum(v * v, axis=1))), 1), "y_p99": round(float(np.percentile(y, 99)), 1),
+            "mean_abs_density_error": round(float(red[3]), 4), "last_density_error": float(red[2])}
+
+
+def run_arm(spec, args, local, mode: int, net, dist, headline: bool) -> tuple[dict, object]:
+    """Presteps and warm-up untimed, then `steps` substeps timed with CUDA events on
+    the launching stream, L2 flushed (256 MB write) before each."""
+    import torch
+
+    ctx = _make_ctx(spec, args, local, mode, net)
+    stream = torch.cuda.current_stream()
+    presteps = args.presteps if args.presteps >= 0 else spec.meta.get("presteps", 0)
+    for _ in range(presteps):  # untimed: bring the scene into its violent regime (after impact)
+        ctx.substep(spec.dt)
+    for _ in range(args.warmup):
+        ctx.substep(spec.dt)
+    ctx.check_status()
+    torch.cuda.synchronize()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    ctx.check_status()  # clears the pass and convergence counters
+    launches0 = ctx.launch_count()
+    clocks = ClockSampler(local) if headline else None
+    if clocks:
+        clocks.start()
+        time.sleep(0.3)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    for k in range(args.steps):
+        flush.zero_()
+        ev[k][0].record(stream)
+        ctx.substep(spec.dt)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop() if clocks else None
+    launches = ctx.launch_count() - launches0
+    total_ms = float(np.sum([a.elapsed_time(b) for a, b in ev]))
+    info = ctx.check_status()
+    n_end, _ = ctx.lengths()
+    prof, dropped = {}, 0
+    if headline and args.prof_steps > 0:
+        # per-kernel CUDA events on a few more substeps with the same pass count and
+        # no early stop (every launch a full pass), for the kernel shares and the
+        # roofline of the dominant kernel; tracing uses one launch pair per pass
+        passes = max(2, int(round(info.density_passes / args.steps)))
+        ctx.set_settings(solver_iterations=passes, density_error_target=0.0)
+        ctx.profile_enable(True, 65536)
+        ctx.profile_read()
+        for _ in range(args.prof_steps):
+            flush.zero_()
+            ctx.substep(spec.dt)
+        prof, dropped = ctx.profile_read()
+        ctx.profile_enable(False, 0)
+        ctx.set_settings(solver_iterations=args.max_iterations, density_error_target=args.error_target)
+        ctx.check_status()
+    r = {"ms_per_step": total_ms / args.steps, "value": spec.n * args.steps / (total_ms / 1000.0),
+         "density_passes_per_substep": info.density_passes / args.steps,
+         "converged_substeps": f"{info.converged_substeps}/{args.steps}", "pairs": int(info.pairs),
+         "particles_after": int(n_end), "presteps": presteps, "total_ms": total_ms, "gpu_launches": int(launches),
+         "state_after": _state_summary(ctx)}
+    if headline:
+        r["_prof"], r["_dropped"], r["_clocks"] = prof, dropped, clk
+    return r, ctx
+
+
 def run_ours(args) -> None:
     import torch
 
@@ -241,61 +371,23 @@ def run_ours(args) -> None:
         import torch.distributed as dist
 
         dist.init_process_group("nccl", device_id=torch.device(f"cuda:{local}"))
-    from apbf_gb300.api import Context
+    from apbf_gb300 import _native as N
 
     spec = make_spec(args.workload, seed=rank)
     n = spec.n
-    cap = int(n * 1.25) + 1024
-    ctx = Context(particle_capacity=cap, max_neighbors=args.max_neighbors, max_log2res=max(spec.log2res, 3),
-                  device=local)
-    # iterate every substep until the mean compression error is at most the target
-    ctx.set_settings(basic_pbf=1 if spec.basic_pbf else 0, solver_iterations=args.max_iterations,
-                     density_error_target=args.error_target)
-    ctx.set_scene(spec.grid_min, spec.grid_max, spec.log2res, spec.acceleration)
-    ctx.set_boxes(spec.box_min, spec.box_max)
-    ctx.upload(spec.state)
-    stream = torch.cuda.current_stream()
+    learned = not args.no_warm_start
+    net, train_info = train_warm_start(args, local, rank) if learned else (None, None)
+    head_mode = (N.WARM_LEARNED | N.WARM_PROJECTED) if learned else 0
 
-    presteps = args.presteps if args.presteps >= 0 else spec.meta.get("presteps", 0)
-    for _ in range(presteps):  # untimed: bring the scene into its violent regime (after impact)
-        ctx.substep(spec.dt)
-    for _ in range(args.warmup):
-        ctx.substep(spec.dt)
-    ctx.check_status()
-    torch.cuda.synchronize()
-
-    # L2 (129 MB) flush between timed steps: the working set of a 250k scene fits in L2
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    ctx.profile_enable(True, 65536)
-    ctx.profile_read()  # clear
-    ctx.check_status()  # clears the status block (density pass counter)
-    launches0 = ctx.launch_count()
-    clocks = ClockSampler(local)
-    clocks.start()
-    time.sleep(0.3)
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    n_now = []
-    for k in range(args.steps):
-        flush.zero_()
-        ev[k][0].record(stream)
-        ctx.substep(spec.dt)
-        ev[k][1].record(stream)
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    clk = clocks.stop()
-    launches = ctx.launch_count() - launches0
-    prof, dropped = ctx.profile_read()
-    ctx.profile_enable(False, 0)
-    step_ms = [a.elapsed_time(b) for a, b in ev]
-    info = ctx.check_status()
-    passes_per_step = info.density_passes / args.steps
-    n_end, _ = ctx.lengths()
-    red = ctx.reduce_fp64()
-    total_ms = float(np.sum(step_ms))
+    # the plain forms first (same scene, same seed), then the headline form
+    plain = {}
+    if learned and not args.no_plain:
+        for name, mode in (("reference_rule", 0), ("projected_rule", N.WARM_PROJECTED)):
+            r, c = run_arm(spec, args, local, mode, None, dist, headline=False)
+            c.close()
+            plain[name] = {k: v for k, v in r.items() if not k.startswith("_")}
+    head, ctx = run_arm(spec, args, local, head_mode, net, dist, headline=True)
+    total_ms = head["total_ms"]
     particles_processed = n * args.steps
     if dist:
         t = torch.tensor([total_ms, particles_processed], dtype=torch.float64, device=f"cuda:{local}")
@@ -306,18 +398,21 @@ def run_ours(args) -> None:
     value = particles_processed / (total_ms / 1000.0)
 
     # roofline of the dominant kernel (largest share of the timed kernel time)
+    prof = head.pop("_prof")
+    dropped = head.pop("_dropped")
+    clk = head.pop("_clocks")
     dom = max(prof.items(), key=lambda kv: kv[1][1]) if prof else None
     roof = None
     if dom:
         name, (cnt, ms) = dom
         per_launch_s = ms / cnt / 1000.0
-        alg = algorithmic_bytes(name, n, int(info.pairs))
+        alg = algorithmic_bytes(name, n, head["pairs"])
         peak, peak_kind = measured_peak()
         if alg:
             ach = alg / per_launch_s / 1e9
             roof = {"kernel": name, "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
                     "frac": ach / peak, "peak_source": peak_kind,
-                    "traffic": traffic_from_profiles(name, n, int(info.pairs)),
+                    "traffic": traffic_from_profiles(name, n, head["pairs"]),
                     "algorithmic_bytes": alg, "launch_us": per_launch_s * 1e6}
     kernel_share = {k: round(v[1] / max(sum(x[1] for x in prof.values()), 1e-9), 4) for k, v in prof.items()}
 
@@ -329,18 +424,24 @@ def run_ours(args) -> None:
         cpu = cpu_baseline(spec)
 
     if rank == 0:
+        solver = ("learned warm start (BF16 MLP first update) + projected Jacobi passes" if learned
+                  else "reference Jacobi rule")
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (int32 fixed-point positions and sums)",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (int32 fixed-point positions and sums; bf16 MLP)",
             "data": "synthetic (seeded scene generator)",
-            "config": {"workload": args.workload, "particles": n, "particles_after": int(n_end),
-                       "iterations": f"until mean compression error <= {args.error_target} (max {args.max_iterations})",
-                       "density_passes_per_substep": passes_per_step, "presteps": presteps, "dt": spec.dt,
-                       "adaptive": not spec.basic_pbf, "pairs": int(info.pairs),
-                       "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas x{world}",
-                       "density_error_last_iteration": float(red[2]), "abs_density_error": float(red[3])},
-            "roofline": roof, "kernel_share": kernel_share, "gpu_launches": int(launches),
+            "config": {"workload": args.workload, "particles": n, "particles_after": head["particles_after"],
+                       "solver": solver,
+                       "iterations": f"until mean density error <= {args.error_target} (max {args.max_iterations})",
+                       "density_passes_per_substep": head["density_passes_per_substep"],
+                       "converged_substeps": head["converged_substeps"], "presteps": head["presteps"],
+                       "dt": spec.dt, "adaptive": not spec.basic_pbf, "pairs": head["pairs"],
+                       "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas x{world}"},
+            "state_after": head["state_after"],
+            "plain": plain or None,
+            "warm_start_training": train_info,
+            "roofline": roof, "kernel_share": kernel_share, "gpu_launches": head["gpu_launches"],
             "profiler_dropped": int(dropped), "clocks": clk, "e2e": e2e, "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)
@@ -383,15 +484,21 @@ def run_e2e(ctx, spec, args, local) -> dict:
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
-    ap.add_argument("--max-iterations", type=int, default=20)
+    ap.add_argument("--max-iterations", type=int, default=100)
     ap.add_argument("--error-target", type=float, default=0.001)
     ap.add_argument("--presteps", type=int, default=-1, help="untimed substeps before warm-up (-1: scene default)")
     ap.add_argument("--max-neighbors", type=int, default=192)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-warm-start", action="store_true", help="headline = the reference Jacobi rule")
+    ap.add_argument("--no-plain", action="store_true", help="skip the two plain-solver comparison runs")
+    ap.add_argument("--ws-epochs", type=int, default=3)
+    ap.add_argument("--prof-steps", type=int, default=8, help="traced substeps after the timed ones (kernel shares)")
+    ap.add_argument("--ws-min-neighbors", type=float, default=16.0)
+    ap.add_argument("--ws-omega", type=float, default=2.0)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

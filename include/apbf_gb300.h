@@ -158,7 +158,7 @@ typedef struct apbf_status_info {
     uint32_t required_particles;
     unsigned long long pairs;    /* pairs of the last neighbourhood search */
     uint32_t density_passes;     /* density passes executed since the status was last cleared */
-    uint32_t pad;
+    uint32_t converged_substeps; /* substeps whose density error met density_error_target, same period */
 } apbf_status_info;
 
 typedef struct apbf_ctx apbf_ctx;
@@ -221,6 +221,11 @@ apbf_status apbf_export_pairs(apbf_ctx *ctx, uint32_t *d_pairs, uint32_t capacit
  * intermediates read by apbf_debug_incompressibility (costs 24 bytes per particle
  * of extra writes per iteration). */
 apbf_status apbf_set_debug(apbf_ctx *ctx, int enable);
+/* 1 (default): apbf_substep runs Jacobi passes 1.. as one CUDA graph launch whose
+ * while loop ends on the device at convergence or after solver_iterations
+ * passes; 0: one launch pair per pass (the form tracing and debugging use).
+ * Both give the same results.  No counterpart in the reference. */
+apbf_status apbf_set_solve_graph(apbf_ctx *ctx, int enable);
 /* Per-particle intermediates of the last incompressibility iteration (debug):
  * density and squared-gradient sums (2^18 fixed point), weighted gradient sums
  * (int4), lambda.  Any pointer may be NULL. */

@@ -1,0 +1,70 @@
+"""The solve loop graph (Jacobi passes 1.. of a substep as one graph launch with a
+device-side while loop) against the per-pass launches: bit-identical states,
+pass counts and convergence counts, fewer host launches."""
+import numpy as np
+import pytest
+
+from apbf_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(spec, graph: bool, substeps: int, iterations: int, target: float, warm=None, maxn=128):
+    import torch
+
+    from apbf_gb300.api import Context
+
+    ctx = Context(particle_capacity=spec.n, max_neighbors=maxn, max_log2res=max(spec.log2res, 3))
+    ctx.set_settings(basic_pbf=1 if spec.basic_pbf else 0, solver_iterations=iterations,
+                     density_error_target=target)
+    ctx.set_scene(spec.grid_min, spec.grid_max, spec.log2res, spec.acceleration)
+    ctx.set_boxes(spec.box_min, spec.box_max)
+    ctx.upload(spec.state)
+    ctx.set_solve_graph(graph)
+    if warm is not None:
+        ctx.mlp_load(torch.from_numpy(warm).cuda())
+        ctx.set_warm_start(True)
+    ctx.check_status()
+    l0 = ctx.launch_count()
+    for _ in range(substeps):
+        ctx.substep(spec.dt)
+    info = ctx.check_status()
+    launches = ctx.launch_count() - l0
+    st, _ = ctx.download()
+    ctx.close()
+    return st, info.density_passes, info.converged_substeps, launches
+
+
+def _same(a, b):
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+
+
+@pytest.mark.parametrize("iterations,target", [(30, 1e-3), (5, 0.0), (4, 0.0), (7, 2e-3)])
+def test_graph_matches_launches_dam_break(iterations, target):
+    spec = scenes.dam_break(n_side=16)
+    a = _run(spec, True, 12, iterations, target)
+    b = _run(spec, False, 12, iterations, target)
+    _same(a[0], b[0])
+    assert a[1] == b[1] and a[2] == b[2], (a[1:], b[1:])
+    if target > 0:
+        assert a[3] < b[3], (a[3], b[3])
+
+
+def test_graph_matches_launches_with_warm_start():
+    from oracle import mlp_oracle as M
+
+    rng = np.random.default_rng(0)
+    p = np.zeros(M.P_N, np.float32)
+    p[M.P_IS:M.P_IS + 6] = 0.1
+    p[M.P_W1:M.P_B1] = rng.normal(size=M.H * M.F) * 0.3
+    p[M.P_W2:M.P_B2] = rng.normal(size=M.H * M.H) * 0.1
+    p[M.P_W3:M.P_B3] = rng.normal(size=M.H) * 0.05
+    p[M.P_YS] = 0.2
+    p[M.P_YM] = -0.3
+    spec = scenes.water_drop(total=20_000, seed=3, basic_pbf=True)
+    a = _run(spec, True, 30, 40, 1e-3, warm=p, maxn=160)
+    b = _run(spec, False, 30, 40, 1e-3, warm=p, maxn=160)
+    _same(a[0], b[0])
+    assert a[1] == b[1] and a[2] == b[2], (a[1:], b[1:])
+    assert a[3] < b[3]
