@@ -135,6 +135,10 @@ class StatusInfo(C.Structure):
     ]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("gather_lanes", C.c_uint32), ("reserved0", C.c_uint32), ("reserved", C.c_uint32 * 6)]
+
+
 class KernelTime(C.Structure):
     _fields_ = [("name", C.c_char * 48), ("launches", C.c_uint32), ("pad", C.c_uint32), ("total_ms", C.c_double)]
 
@@ -182,6 +186,9 @@ SIGNATURES = {
     "apbf_mlp_load": (_ST, [_P, _P, _P]),
     "apbf_set_warm_start": (_ST, [_P, C.c_int]),
     "apbf_set_solve_graph": (_ST, [_P, C.c_int]),
+    "apbf_set_tuning": (_ST, [_P, _P]),
+    "apbf_get_tuning": (_ST, [_P, _P]),
+    "apbf_autotune": (_ST, [_P, _P, _P, _P]),
     "apbf_record_samples": (_ST, [_P, C.c_uint32, _P, _P, C.c_uint32, _P]),
     "apbf_mlp_forward": (_ST, [_P, _P, C.c_uint32, _P, _P]),
     "apbf_mlp_train_step": (_ST, [_P, _P, _P, _P, _P, _P, C.c_uint32, C.c_float, C.c_float, C.c_uint32, _P, _P,

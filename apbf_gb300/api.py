@@ -131,6 +131,26 @@ class Context:
     def set_debug(self, enable: bool) -> None:
         N.check(self.lib.apbf_set_debug(self.handle, 1 if enable else 0), "apbf_set_debug")
 
+    def tuning(self) -> dict:
+        t = N.Tuning()
+        N.check(self.lib.apbf_get_tuning(self.handle, C.byref(t)), "apbf_get_tuning")
+        return {"gather_lanes": t.gather_lanes}
+
+    def set_tuning(self, gather_lanes: int) -> None:
+        t = N.Tuning()
+        N.check(self.lib.apbf_get_tuning(self.handle, C.byref(t)), "apbf_get_tuning")
+        t.gather_lanes = gather_lanes
+        N.check(self.lib.apbf_set_tuning(self.handle, C.byref(t)), "apbf_set_tuning")
+
+    def autotune(self, stream=None) -> dict:
+        """Times every launch-shape candidate on the current state (restored afterwards)
+        and keeps the fastest; returns the choice and the per-pass times (ms)."""
+        t = N.Tuning()
+        ms = (C.c_float * 4)()
+        N.check(self.lib.apbf_autotune(self.handle, _stream_handle(stream), C.byref(t), ms), "apbf_autotune")
+        return {"gather_lanes": t.gather_lanes,
+                "pass_ms": {str(l): round(float(v), 5) for l, v in zip((1, 2, 4, 8), ms)}}
+
     def set_solve_graph(self, enable: bool) -> None:
         """Jacobi passes 1.. of a substep as one graph launch with a device-side loop (default on)."""
         N.check(self.lib.apbf_set_solve_graph(self.handle, 1 if enable else 0), "apbf_set_solve_graph")

@@ -203,6 +203,8 @@ struct apbf_ctx {
     apbf::ProfSlot *prof_open = nullptr;
     bool capturing = false;        // launches go into a graph being built: not counted
 
+    apbf_tuning tuning = {1u, 0u, {0u, 0u, 0u, 0u, 0u, 0u}};  // launch shapes (apbf_set_tuning / apbf_autotune)
+
     // solve loop graphs (graph.cu)
     int use_graphs = 1;
     unsigned long long graph_version = 1;  // bumped by every change captured by value

@@ -16,6 +16,9 @@
 // as the scatter form, and integer addition is associative, so the gather is
 // bit-identical to the atomic scatter.  Gradients are recomputed in k_delta
 // rather than stored (the reference writes 16 bytes per pair).
+#include <algorithm>
+#include <type_traits>
+
 #include "apbf_internal.cuh"
 
 namespace apbf {
@@ -98,38 +101,62 @@ __device__ __forceinline__ void block_sum2(const double *partials, int blocks, d
 
 constexpr int kUnroll = 4;
 
-template <bool GAUSS>
+// L threads per particle ("lanes"): lane s of a particle's group takes row
+// entries s, s + L, ...; the group's integer sums are then combined by shuffles.
+// Wrapping integer sums are order-free, so every L gives the same density,
+// gradient and squared-gradient sums bit for bit.
+template <int L, typename T>
+__device__ __forceinline__ T group_sum(T v) {
+#pragma unroll
+    for (int off = L / 2; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
+}
+template <int L>
+__device__ __forceinline__ int32_t group_wsum(int32_t v) {
+#pragma unroll
+    for (int off = L / 2; off > 0; off >>= 1) v = wadd(v, __shfl_xor_sync(0xffffffffu, v, off));
+    return v;
+}
+
+template <bool GAUSS, int L>
 __global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) {
     if (a.early_exit && *(volatile uint32_t *)&a.st->converged) return;  // uniform over the grid
     if (a.loop_offset >= 0 && a.st->pass_index + (uint32_t)a.loop_offset >= a.max_passes) return;
     const uint32_t n = a.d_len[kLenParticles];
+    const uint32_t sub = threadIdx.x % L, gpb = blockDim.x / L;
     double e1 = 0.0, e2 = 0.0;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    // the block iterates as a whole (uniform trip count: the group shuffles need every lane)
+    for (uint32_t base = blockIdx.x * gpb; base < n; base += gridDim.x * gpb) {
+        const uint32_t i_raw = base + threadIdx.x / L;
+        const bool valid = i_raw < n;
+        const uint32_t i = valid ? i_raw : 0u;
         const int4 p = a.pos[i];
-        const float kw = a.kw[i], im = a.inv_mass[i], radius = a.radius[i];
+        const float kw = a.kw[i];
         const KConst c = gauss_consts(kw);
-        float W0 = GAUSS ? c.norm : kernel_height(a.hk, 0.0f, kw, c);
-        uint32_t dens = f2u(W0 / im * APBF_FIX);
+        uint32_t dens = 0u;
         int32_t gx = 0, gy = 0, gz = 0;
         uint32_t sq = 0;
         int32_t cx = 0, cy = 0, cz = 0, cw = 0;
-        const uint32_t cnt = a.count[i];
+        const uint32_t cnt = valid ? a.count[i] : 0u;
         const uint32_t *row = a.idx + i;
         const bool feat = a.features != nullptr;
         const float4 vi = feat ? a.vel[i] : make_float4(0.f, 0.f, 0.f, 0.f);
         float div = 0.0f;  // sum_j m_j (v_j - v_i) . gradW_ij  (velocity divergence x density)
-        // Batches of kUnroll pairs: all row entries, then all neighbour gathers, then
-        // the arithmetic, so each thread keeps kUnroll loads in flight.
-        for (uint32_t k0 = 0; k0 < cnt; k0 += kUnroll) {
+        // Batches of kUnroll pairs per lane: all row entries, then all neighbour
+        // gathers, then the arithmetic, so each lane keeps kUnroll loads in flight.
+        for (uint32_t k0 = sub; k0 < cnt; k0 += L * kUnroll) {
             uint32_t jj[kUnroll];
             int4 qq[kUnroll];
 #pragma unroll
-            for (int u = 0; u < kUnroll; ++u) jj[u] = k0 + u < cnt ? row[(size_t)(k0 + u) * a.stride] : i;
+            for (int u = 0; u < kUnroll; ++u) {
+                const uint32_t k = k0 + u * L;
+                jj[u] = k < cnt ? row[(size_t)k * a.stride] : i;
+            }
 #pragma unroll
             for (int u = 0; u < kUnroll; ++u) qq[u] = a.pos[jj[u]];
 #pragma unroll
             for (int u = 0; u < kUnroll; ++u) {
-                if (k0 + u >= cnt) break;
+                if (k0 + u * L >= cnt) break;
                 const int4 q = qq[u];
                 // the neighbour's mass rides in position.w (x / invMassN = x * mass)
                 const float mjf = __int_as_float(q.w) * APBF_FIX;  // neighbour mass x 2^18
@@ -155,6 +182,24 @@ __global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) 
                 }
             }
         }
+        if (L > 1) {
+            dens = group_sum<L>(dens);
+            sq = group_sum<L>(sq);
+            gx = group_wsum<L>(gx);
+            gy = group_wsum<L>(gy);
+            gz = group_wsum<L>(gz);
+            if (feat) div = group_sum<L>(div);
+            if (a.method == 1) {
+                cx = group_wsum<L>(cx);
+                cy = group_wsum<L>(cy);
+                cz = group_wsum<L>(cz);
+                cw = group_wsum<L>(cw);
+            }
+        }
+        if (!valid || sub != 0) continue;
+        const float im = a.inv_mass[i], radius = a.radius[i];
+        const float W0 = GAUSS ? c.norm : kernel_height(a.hk, 0.0f, kw, c);
+        dens += f2u(W0 / im * APBF_FIX);  // incompressibility_0.comp:32-45 (the self term)
         // incompressibility_2.comp:77-109
         const float r2x = 2.0f * radius;
         const float ird = (r2x * r2x * r2x) * im;
@@ -333,8 +378,8 @@ __device__ __forceinline__ void accumulate(float *dst, int mode, uint32_t j, flo
     else if (mode == 2) dst[j] += v;
 }
 
-template <bool GAUSS>
-__global__ void __launch_bounds__(256, GAUSS ? 5 : 4) k_delta(PassB a) {
+template <bool GAUSS, int L>
+__global__ void __launch_bounds__(256, GAUSS && L == 1 ? 5 : 4) k_delta(PassB a) {
     const uint32_t n = a.d_len[kLenParticles];
     bool skip = a.early_exit && *(volatile const uint32_t *)&a.st->converged;
     uint32_t nboxes = a.nboxes;
@@ -354,18 +399,24 @@ __global__ void __launch_bounds__(256, GAUSS ? 5 : 4) k_delta(PassB a) {
     const bool sym = a.st->range_min == a.st->range_max;
     const uint32_t *cnt_arr = sym ? a.count : a.rcount;
     const uint32_t *idx_arr = sym ? a.idx : a.ridx;
-    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    const uint32_t sub = threadIdx.x % L, gpb = blockDim.x / L;
+    for (uint32_t base = blockIdx.x * gpb; base < n; base += gridDim.x * gpb) {
+        const uint32_t j_raw = base + threadIdx.x / L;
+        const bool valid = j_raw < n;
+        const uint32_t j = valid ? j_raw : 0u;
         const int4 p = a.pos[j];
-        const int4 sh = a.shift[j];
-        int32_t ax = sh.x, ay = sh.y, az = sh.z;
-        const uint32_t cnt = cnt_arr[j];
+        int32_t ax = 0, ay = 0, az = 0;
+        const uint32_t cnt = valid ? cnt_arr[j] : 0u;
         const uint32_t *row = idx_arr + j;
-        for (uint32_t k0 = 0; k0 < cnt; k0 += kUnroll) {
+        for (uint32_t k0 = sub; k0 < cnt; k0 += L * kUnroll) {
             uint32_t ii[kUnroll];
             float4 rr[kUnroll];
             int4 qq[kUnroll];
 #pragma unroll
-            for (int u = 0; u < kUnroll; ++u) ii[u] = k0 + u < cnt ? row[(size_t)(k0 + u) * a.stride] : j;
+            for (int u = 0; u < kUnroll; ++u) {
+                const uint32_t k = k0 + u * L;
+                ii[u] = k < cnt ? row[(size_t)k * a.stride] : j;
+            }
 #pragma unroll
             for (int u = 0; u < kUnroll; ++u) {
                 rr[u] = a.rec[ii[u]];
@@ -373,7 +424,7 @@ __global__ void __launch_bounds__(256, GAUSS ? 5 : 4) k_delta(PassB a) {
             }
 #pragma unroll
             for (int u = 0; u < kUnroll; ++u) {
-                const float lam = k0 + u < cnt ? rr[u].x : 0.0f;
+                const float lam = k0 + u * L < cnt ? rr[u].x : 0.0f;
                 if (lam == 0.0f) continue;  // the applied lambda (incompressibility_3.comp:63); padding lanes
                 KConst c;
                 c.ivd = rr[u].y;
@@ -392,6 +443,16 @@ __global__ void __launch_bounds__(256, GAUSS ? 5 : 4) k_delta(PassB a) {
                 az = wadd(az, f2i(g.z * sc));
             }
         }
+        if (L > 1) {
+            ax = group_wsum<L>(ax);
+            ay = group_wsum<L>(ay);
+            az = group_wsum<L>(az);
+        }
+        if (!valid || sub != 0) continue;
+        const int4 sh = a.shift[j];  // the self shift (incompressibility_2.comp:106-109)
+        ax = wadd(ax, sh.x);
+        ay = wadd(ay, sh.y);
+        az = wadd(az, sh.z);
         int4 out = make_int4(wadd(p.x, ax), wadd(p.y, ay), wadd(p.z, az), p.w);
         if (nboxes) out = box_push(out, a.radius[j], j, a.bmin, a.bmax, nboxes);
         a.pos_out[j] = out;
@@ -443,6 +504,17 @@ __global__ void __launch_bounds__(256) k_finalize_mass(const double *partials, i
 
 }  // namespace
 
+// Calls f with std::integral_constant<int, L> for the tuned lanes per particle.
+template <typename F>
+void launch_lanes(int lanes, F &&f) {
+    switch (lanes) {
+        case 2: f(std::integral_constant<int, 2>()); break;
+        case 4: f(std::integral_constant<int, 4>()); break;
+        case 8: f(std::integral_constant<int, 8>()); break;
+        default: f(std::integral_constant<int, 1>()); break;
+    }
+}
+
 apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s, const SolveOpts &o) {
     const bool box_after = o.box_after, converge = o.converge, learned = o.learned, projected = o.projected;
     const int feature_mode = o.feature_mode, acc_mode = o.acc_mode, prev_mode = o.prev_mode;
@@ -489,11 +561,15 @@ apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s, const SolveOpts &o)
     a.b_sgl_factor = st.boundariness_self_grad_length_factor;
     a.b_up_factor = st.boundariness_underpressure_factor;
     const int g = ctx->red_blocks;
+    const int lanes = ctx->tuning.gather_lanes;
     APBF_BEFORE_LAUNCH(ctx, s, "k_density_lambda");
-    if (gauss)
-        k_density_lambda<true><<<g, kBlock, 0, s>>>(a);
-    else
-        k_density_lambda<false><<<g, kBlock, 0, s>>>(a);
+    launch_lanes(lanes, [&](auto lc) {
+        constexpr int Lc = decltype(lc)::value;
+        if (gauss)
+            k_density_lambda<true, Lc><<<g, kBlock, 0, s>>>(a);
+        else
+            k_density_lambda<false, Lc><<<g, kBlock, 0, s>>>(a);
+    });
     APBF_AFTER_LAUNCH(ctx, s, "k_density_lambda");
 
     if (learned) {  // the network's lambda replaces the plain one in this update
@@ -525,10 +601,14 @@ apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s, const SolveOpts &o)
     b.loop_offset = o.loop_offset;
     b.max_passes = o.max_passes;
     APBF_BEFORE_LAUNCH(ctx, s, "k_delta");
-    if (gauss)
-        k_delta<true><<<grid_for(ctx, cap), kBlock, 0, s>>>(b);
-    else
-        k_delta<false><<<grid_for(ctx, cap), kBlock, 0, s>>>(b);
+    const int gd = grid_for(ctx, (uint32_t)std::min<uint64_t>((uint64_t)cap * lanes, 0xffffffffu));
+    launch_lanes(lanes, [&](auto lc) {
+        constexpr int Lc = decltype(lc)::value;
+        if (gauss)
+            k_delta<true, Lc><<<gd, kBlock, 0, s>>>(b);
+        else
+            k_delta<false, Lc><<<gd, kBlock, 0, s>>>(b);
+    });
     APBF_AFTER_LAUNCH(ctx, s, "k_delta");
     // the updated positions now live in the alternate buffer: swap position buffers
     int4 *tmp = f.pos;

@@ -282,7 +282,8 @@ def train_warm_start(args, local: int, rank: int) -> tuple[object, dict]:
             "epochs": args.ws_epochs, "loss_per_epoch": [round(h, 5) for h in hist],
             "collect_s": round(t1 - t0, 3), "train_s": round(t2 - t1, 3),
             "guards": {"min_neighbors": args.ws_min_neighbors, "omega_max": args.ws_omega}}
-    del buf
+    del buf, X, T
+    torch.cuda.empty_cache()
     return net, info
 
 
@@ -305,6 +306,7 @@ def run_arm(spec, args, local, mode: int, net, dist, headline: bool) -> tuple[di
     presteps = args.presteps if args.presteps >= 0 else spec.meta.get("presteps", 0)
     for _ in range(presteps):  # untimed: bring the scene into its violent regime (after impact)
         ctx.substep(spec.dt)
+    tuning = ctx.autotune() if not args.no_autotune else ctx.tuning()  # untimed, state restored
     for _ in range(args.warmup):
         ctx.substep(spec.dt)
     ctx.check_status()
@@ -320,12 +322,16 @@ def run_arm(spec, args, local, mode: int, net, dist, headline: bool) -> tuple[di
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
+    if headline:
+        torch.cuda.nvtx.range_push("timed")  # lets ncu select the timed substeps (--nvtx-include timed/)
     for k in range(args.steps):
         flush.zero_()
         ev[k][0].record(stream)
         ctx.substep(spec.dt)
         ev[k][1].record(stream)
     torch.cuda.synchronize()
+    if headline:
+        torch.cuda.nvtx.range_pop()
     if dist:
         dist.barrier()
     clk = clocks.stop() if clocks else None
@@ -353,6 +359,7 @@ def run_arm(spec, args, local, mode: int, net, dist, headline: bool) -> tuple[di
          "density_passes_per_substep": info.density_passes / args.steps,
          "converged_substeps": f"{info.converged_substeps}/{args.steps}", "pairs": int(info.pairs),
          "particles_after": int(n_end), "presteps": presteps, "total_ms": total_ms, "gpu_launches": int(launches),
+         "tuning": tuning,
          "state_after": _state_summary(ctx)}
     if headline:
         r["_prof"], r["_dropped"], r["_clocks"] = prof, dropped, clk
@@ -437,7 +444,8 @@ def run_ours(args) -> None:
                        "density_passes_per_substep": head["density_passes_per_substep"],
                        "converged_substeps": head["converged_substeps"], "presteps": head["presteps"],
                        "dt": spec.dt, "adaptive": not spec.basic_pbf, "pairs": head["pairs"],
-                       "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas x{world}"},
+                       "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas x{world}",
+                       "tuning": head["tuning"]},
             "state_after": head["state_after"],
             "plain": plain or None,
             "warm_start_training": train_info,
@@ -496,6 +504,7 @@ def main() -> None:
     ap.add_argument("--no-warm-start", action="store_true", help="headline = the reference Jacobi rule")
     ap.add_argument("--no-plain", action="store_true", help="skip the two plain-solver comparison runs")
     ap.add_argument("--ws-epochs", type=int, default=3)
+    ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--prof-steps", type=int, default=8, help="traced substeps after the timed ones (kernel shares)")
     ap.add_argument("--ws-min-neighbors", type=float, default=16.0)
     ap.add_argument("--ws-omega", type=float, default=2.0)

@@ -161,6 +161,15 @@ typedef struct apbf_status_info {
     uint32_t converged_substeps; /* substeps whose density error met density_error_target, same period */
 } apbf_status_info;
 
+/* Launch shapes of the context's kernels (no reference counterpart: the
+ * reference's workgroup sizes are fixed in its shaders).  Results do not depend
+ * on them. */
+typedef struct apbf_tuning {
+    uint32_t gather_lanes;   /* threads per particle in the density and position passes: 1, 2, 4 or 8 */
+    uint32_t reserved0;
+    uint32_t reserved[6];
+} apbf_tuning;
+
 typedef struct apbf_ctx apbf_ctx;
 
 /* ---- lifetime and configuration ---- */
@@ -226,6 +235,15 @@ apbf_status apbf_set_debug(apbf_ctx *ctx, int enable);
  * passes; 0: one launch pair per pass (the form tracing and debugging use).
  * Both give the same results.  No counterpart in the reference. */
 apbf_status apbf_set_solve_graph(apbf_ctx *ctx, int enable);
+
+/* Launch shapes (no counterpart in the reference).  apbf_autotune times every
+ * gather_lanes candidate on the context's current particle state and neighbour
+ * rows (call it after a substep or a neighbourhood search), keeps the fastest and
+ * restores the state it ran on; pass_ms (may be NULL) receives the time of one
+ * Jacobi pass for gather_lanes 1, 2, 4, 8. */
+apbf_status apbf_set_tuning(apbf_ctx *ctx, const apbf_tuning *t);
+apbf_status apbf_get_tuning(apbf_ctx *ctx, apbf_tuning *t);
+apbf_status apbf_autotune(apbf_ctx *ctx, void *stream, apbf_tuning *chosen, float *pass_ms);
 /* Per-particle intermediates of the last incompressibility iteration (debug):
  * density and squared-gradient sums (2^18 fixed point), weighted gradient sums
  * (int4), lambda.  Any pointer may be NULL. */
