@@ -151,9 +151,10 @@ class Context:
         return {"gather_lanes": t.gather_lanes,
                 "pass_ms": {str(l): round(float(v), 5) for l, v in zip((1, 2, 4, 8), ms)}}
 
-    def set_solve_graph(self, enable: bool) -> None:
-        """Jacobi passes 1.. of a substep as one graph launch with a device-side loop (default on)."""
-        N.check(self.lib.apbf_set_solve_graph(self.handle, 1 if enable else 0), "apbf_set_solve_graph")
+    def set_solve_graph(self, mode: int | bool) -> None:
+        """0: per-kernel launches; 1 (default): the Jacobi passes 1.. as one graph launch with a
+        device-side loop; 2: the whole substep as one graph launch."""
+        N.check(self.lib.apbf_set_solve_graph(self.handle, int(mode)), "apbf_set_solve_graph")
 
     # ---- lists ----
     def fluid_view(self) -> dict:
@@ -478,6 +479,35 @@ class algorithms:
     def prefix_sum(ctx: Context, values: torch.Tensor, count: torch.Tensor, max_count: int, stream=None) -> None:
         N.check(ctx.lib.apbf_prefix_sum(ctx.handle, C.c_void_p(values.data_ptr()), C.c_void_p(count.data_ptr()),
                                         max_count, _stream_handle(stream)), "algorithms.prefix_sum")
+
+
+class Batch:
+    """Independent scenes (contexts) advanced together: one graph launch per substep
+    whose parallel branches are the contexts' substeps."""
+
+    def __init__(self, contexts: list):
+        self.contexts = list(contexts)
+        self.lib = N.load()
+        arr = (C.c_void_p * len(self.contexts))(*[c.handle.value for c in self.contexts])
+        h = C.c_void_p()
+        N.check(self.lib.apbf_batch_create(arr, len(self.contexts), C.byref(h)), "apbf_batch_create")
+        self.handle = h
+
+    def substep(self, dt: float, stream=None) -> None:
+        N.check(self.lib.apbf_batch_substep(self.handle, C.c_float(dt), _stream_handle(stream)),
+                "apbf_batch_substep")
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            torch.cuda.synchronize()
+            self.lib.apbf_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 @dataclass

@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cstring>
 #include <string>
 #include <vector>
 
@@ -109,6 +110,31 @@ struct SolveGraph {
     unsigned long long key[4] = {0, 0, 0, 0};
 };
 constexpr int kSolveGraphs = 4;
+
+// Host-side roles of the context's buffers; a substep moves them from one value to
+// the next, and a captured substep graph is valid for one starting value.
+struct HostState {
+    FluidBufs fl[2];
+    TransferBufs tr[2];
+    uint32_t *old_bd = nullptr;
+    int fcur = 0, tcur = 0;
+    float last_dt = 0.0f;
+    bool operator==(const HostState &o) const {
+        return std::memcmp(fl, o.fl, sizeof(fl)) == 0 && std::memcmp(tr, o.tr, sizeof(tr)) == 0 &&
+               old_bd == o.old_bd && fcur == o.fcur && tcur == o.tcur && last_dt == o.last_dt;
+    }
+};
+
+// One instantiated whole-substep graph (graph.cu).
+struct SubstepGraph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    HostState before, after;
+    float dt = 0.0f;
+    unsigned long long version = 0, mode = 0;
+    unsigned long long kernels = 0;  // kernel nodes outside the solve loop body
+};
+constexpr int kSubstepGraphs = 8;  // the buffer roles of an adaptive scene cycle with a period of up to 6
 }  // namespace apbf
 
 struct apbf_ctx {
@@ -211,7 +237,10 @@ struct apbf_ctx {
     apbf::SolveGraph solve_graphs[apbf::kSolveGraphs];
     int solve_graph_next = 0;
     cudaStream_t capture_stream = nullptr;
+    cudaStream_t capture_stream2 = nullptr;  // solve loop bodies captured inside a substep capture
     unsigned long long loop_launches_per_iter = 0;  // kernel nodes per body run
+    apbf::SubstepGraph substep_graphs[apbf::kSubstepGraphs];
+    int substep_graph_next = 0;
 };
 
 namespace apbf {
@@ -293,7 +322,18 @@ struct SolveOpts {
 apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s, const SolveOpts &o = SolveOpts());
 // Passes 1.. of a substep as one graph launch (a device-side while loop).
 apbf_status solve_loop(apbf_ctx *ctx, cudaStream_t s, const SolveOpts &o);
+// The same loop as a conditional node of the graph that stream s is capturing.
+apbf_status solve_loop_captured(apbf_ctx *ctx, cudaStream_t s, const SolveOpts &o);
 void destroy_solve_graphs(apbf_ctx *ctx);
+void destroy_substep_graphs(apbf_ctx *ctx);
+// Whole substeps as graphs (graph.cu): one context, or a batch of contexts as the
+// parallel branches of one graph.
+apbf_status substep_body(apbf_ctx *ctx, float dt, cudaStream_t s, bool capture);
+bool substep_graph_eligible(const apbf_ctx *ctx);
+apbf_status substep_graph(apbf_ctx *ctx, float dt, cudaStream_t s);
+HostState host_state(const apbf_ctx *ctx);
+void set_host_state(apbf_ctx *ctx, const HostState &h);
+unsigned long long substep_mode_bits(const apbf_ctx *ctx);
 constexpr int kMlpParams = 4824;  // floats of the warm-start parameter vector (mlp.cu)
 apbf_status mlp_forward(const float *P, const float *X, uint32_t nrows, float *out, cudaStream_t s);
 apbf_status mlp_train_step(float *P, float *m, float *v, float *partials, const float *X, const float *T,

@@ -77,7 +77,9 @@ apbf_status apbf_destroy(apbf_ctx *ctx) {
         cudaEventDestroy(p.b);
     }
     destroy_solve_graphs(ctx);
+    destroy_substep_graphs(ctx);
     if (ctx->capture_stream) cudaStreamDestroy(ctx->capture_stream);
+    if (ctx->capture_stream2) cudaStreamDestroy(ctx->capture_stream2);
     for (void *p : ctx->owned) cudaFree(p);
     delete ctx;
     return APBF_OK;
@@ -249,10 +251,11 @@ apbf_status apbf_set_debug(apbf_ctx *ctx, int enable) {
     return APBF_OK;
 }
 
-apbf_status apbf_set_solve_graph(apbf_ctx *ctx, int enable) {
-    if (!ctx) return APBF_ERR_INVALID_ARG;
-    ctx->use_graphs = enable ? 1 : 0;
-    if (!enable) destroy_solve_graphs(ctx);
+apbf_status apbf_set_solve_graph(apbf_ctx *ctx, int mode) {
+    if (!ctx || mode < 0 || mode > 2) return APBF_ERR_INVALID_ARG;
+    ctx->use_graphs = mode;
+    destroy_solve_graphs(ctx);
+    destroy_substep_graphs(ctx);
     return APBF_OK;
 }
 
@@ -362,13 +365,13 @@ apbf_status apbf_particle_transfer_apply(apbf_ctx *ctx, float dt, void *stream) 
 }
 
 // pool::update (source/pool.cpp:67-106).
-apbf_status apbf_substep(apbf_ctx *ctx, float dt, void *stream) {
-    if (!ctx) return APBF_ERR_INVALID_ARG;
-    if (ctx->scene.log2res < 1) {
-        set_error("apbf_substep: call apbf_set_scene first");
-        return APBF_ERR_INVALID_ARG;
-    }
-    cudaStream_t s = (cudaStream_t)stream;
+}  // extern "C"
+
+namespace apbf {
+// The body of pool::update (pool.cpp:67-106) on stream s.  capture: s is being
+// captured into a substep graph, so the solve loop becomes a conditional node of
+// that graph instead of a launch of its own.
+apbf_status substep_body(apbf_ctx *ctx, float dt, cudaStream_t s, bool capture) {
     const apbf_settings &st = ctx->settings;
     apbf_status r = velocity_handling(ctx, dt, ctx->scene.acceleration, s);
     if (r != APBF_OK) return r;
@@ -420,7 +423,7 @@ apbf_status apbf_substep(apbf_ctx *ctx, float dt, void *stream) {
         o.projected = projected;
         if (it == 1 && loop_graph) {
             o.max_passes = (uint32_t)st.solver_iterations;
-            r = solve_loop(ctx, s, o);
+            r = capture ? solve_loop_captured(ctx, s, o) : solve_loop(ctx, s, o);
             if (r != APBF_OK) return r;
             break;
         }
@@ -439,6 +442,25 @@ apbf_status apbf_substep(apbf_ctx *ctx, float dt, void *stream) {
         if (r != APBF_OK) return r;
     }
     return APBF_OK;
+}
+
+bool substep_graph_eligible(const apbf_ctx *ctx) {
+    return ctx->use_graphs == 2 && !ctx->prof_on && !ctx->debug && ctx->rec_iterations == 0 &&
+           ctx->settings.solver_iterations >= 2;
+}
+}  // namespace apbf
+
+extern "C" {
+
+apbf_status apbf_substep(apbf_ctx *ctx, float dt, void *stream) {
+    if (!ctx) return APBF_ERR_INVALID_ARG;
+    if (ctx->scene.log2res < 1) {
+        set_error("apbf_substep: call apbf_set_scene first");
+        return APBF_ERR_INVALID_ARG;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    if (substep_graph_eligible(ctx)) return substep_graph(ctx, dt, s);
+    return substep_body(ctx, dt, s, false);
 }
 
 apbf_status apbf_reduce_fp64(apbf_ctx *ctx, double out[4], void *stream) {

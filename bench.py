@@ -241,6 +241,7 @@ def _make_ctx(spec, args, local, mode: int = 0, net=None):
     ctx.set_scene(spec.grid_min, spec.grid_max, spec.log2res, spec.acceleration)
     ctx.set_boxes(spec.box_min, spec.box_max)
     ctx.upload(spec.state)
+    ctx.set_solve_graph(args.graph_mode)
     if net is not None:
         ctx.mlp_load(net.params)
     if mode:
@@ -445,6 +446,7 @@ def run_ours(args) -> None:
                        "converged_substeps": head["converged_substeps"], "presteps": head["presteps"],
                        "dt": spec.dt, "adaptive": not spec.basic_pbf, "pairs": head["pairs"],
                        "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas x{world}",
+                       "graph_mode": args.graph_mode,
                        "tuning": head["tuning"]},
             "state_after": head["state_after"],
             "plain": plain or None,
@@ -505,6 +507,8 @@ def main() -> None:
     ap.add_argument("--no-plain", action="store_true", help="skip the two plain-solver comparison runs")
     ap.add_argument("--ws-epochs", type=int, default=3)
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--graph-mode", type=int, default=2, choices=(0, 1, 2),
+                    help="0 per-kernel launches, 1 solve loop as a graph, 2 whole substep as a graph")
     ap.add_argument("--prof-steps", type=int, default=8, help="traced substeps after the timed ones (kernel shares)")
     ap.add_argument("--ws-min-neighbors", type=float, default=16.0)
     ap.add_argument("--ws-omega", type=float, default=2.0)

@@ -230,11 +230,26 @@ apbf_status apbf_export_pairs(apbf_ctx *ctx, uint32_t *d_pairs, uint32_t capacit
  * intermediates read by apbf_debug_incompressibility (costs 24 bytes per particle
  * of extra writes per iteration). */
 apbf_status apbf_set_debug(apbf_ctx *ctx, int enable);
-/* 1 (default): apbf_substep runs Jacobi passes 1.. as one CUDA graph launch whose
- * while loop ends on the device at convergence or after solver_iterations
- * passes; 0: one launch pair per pass (the form tracing and debugging use).
- * Both give the same results.  No counterpart in the reference. */
-apbf_status apbf_set_solve_graph(apbf_ctx *ctx, int enable);
+/* Graph use of apbf_substep (no counterpart in the reference):
+ *   0  one launch per kernel, one launch pair per possible Jacobi pass;
+ *   1  (default) Jacobi passes 1.. as one CUDA graph launch whose while loop ends
+ *      on the device at convergence or after solver_iterations passes;
+ *   2  the whole substep as one CUDA graph launch (captured on first use, one
+ *      graph per buffer-role state and dt, replayed afterwards), the solve loop a
+ *      conditional node inside it.
+ * All modes give the same results.  Tracing, debugging and sample recording run
+ * a substep with per-kernel launches. */
+apbf_status apbf_set_solve_graph(apbf_ctx *ctx, int mode);
+
+/* A batch of contexts (independent scenes on one device) whose substeps run as the
+ * parallel branches of one CUDA graph: apbf_batch_substep advances every context
+ * by one substep with one graph launch (each scene keeps its own solve loop and
+ * convergence).  The contexts stay usable on their own; no context may be in two
+ * batches that run at the same time.  No counterpart in the reference. */
+typedef struct apbf_batch apbf_batch;
+apbf_status apbf_batch_create(apbf_ctx *const *ctxs, uint32_t n, apbf_batch **out);
+apbf_status apbf_batch_substep(apbf_batch *batch, float dt, void *stream);
+apbf_status apbf_batch_destroy(apbf_batch *batch);
 
 /* Launch shapes (no counterpart in the reference).  apbf_autotune times every
  * gather_lanes candidate on the context's current particle state and neighbour

@@ -68,3 +68,97 @@ def test_graph_matches_launches_with_warm_start():
     _same(a[0], b[0])
     assert a[1] == b[1] and a[2] == b[2], (a[1:], b[1:])
     assert a[3] < b[3]
+
+
+def _run_mode(spec, mode, substeps, iterations, target, maxn=128, warm=None):
+    import torch
+
+    from apbf_gb300.api import Context
+
+    ctx = Context(particle_capacity=int(spec.n * 1.3) + 64, max_neighbors=maxn, max_log2res=max(spec.log2res, 3))
+    ctx.set_settings(basic_pbf=1 if spec.basic_pbf else 0, solver_iterations=iterations,
+                     density_error_target=target)
+    ctx.set_scene(spec.grid_min, spec.grid_max, spec.log2res, spec.acceleration)
+    ctx.set_boxes(spec.box_min, spec.box_max)
+    ctx.upload(spec.state)
+    ctx.set_solve_graph(mode)
+    if warm is not None:
+        ctx.mlp_load(torch.from_numpy(warm).cuda())
+        ctx.set_warm_start(True)
+    ctx.check_status()
+    for _ in range(substeps):
+        ctx.substep(spec.dt)
+    info = ctx.check_status()
+    st, tr = ctx.download()
+    ctx.close()
+    return st, tr, info.density_passes, info.converged_substeps
+
+
+@pytest.mark.parametrize("scene", ["dam_break", "water_drop_adaptive"])
+def test_whole_substep_graph_matches_launches(scene):
+    if scene == "dam_break":
+        spec, maxn, it, tg = scenes.dam_break(n_side=16), 128, 30, 1e-3
+    else:
+        spec, maxn, it, tg = scenes.water_drop(total=20_000, seed=1, basic_pbf=False), 256, 8, 0.0
+    a = _run_mode(spec, 2, 10, it, tg, maxn)
+    b = _run_mode(spec, 0, 10, it, tg, maxn)
+    _same(a[0], b[0])
+    _same(a[1], b[1])
+    assert a[2:] == b[2:]
+
+
+def test_whole_substep_graph_with_warm_start():
+    from oracle import mlp_oracle as M
+
+    rng = np.random.default_rng(1)
+    p = np.zeros(M.P_N, np.float32)
+    p[M.P_IS:M.P_IS + 6] = 0.1
+    p[M.P_W1:M.P_B1] = rng.normal(size=M.H * M.F) * 0.3
+    p[M.P_W2:M.P_B2] = rng.normal(size=M.H * M.H) * 0.1
+    p[M.P_W3:M.P_B3] = rng.normal(size=M.H) * 0.05
+    p[M.P_YS] = 0.2
+    p[M.P_YM] = -0.3
+    spec = scenes.water_drop(total=20_000, seed=3, basic_pbf=True)
+    a = _run_mode(spec, 2, 25, 40, 1e-3, 160, warm=p)
+    b = _run_mode(spec, 1, 25, 40, 1e-3, 160, warm=p)
+    _same(a[0], b[0])
+    assert a[2:] == b[2:]
+
+
+def test_batch_matches_separate_contexts():
+    """Scenes of different sizes and kinds advanced by one graph launch per substep
+    end bit-identical to the same scenes advanced one context at a time."""
+    from apbf_gb300.api import Batch, Context
+
+    specs = [(scenes.dam_break(n_side=12), 128, 30, 1e-3), (scenes.dam_break(n_side=16, seed=2), 128, 30, 1e-3),
+             (scenes.water_drop(total=20_000, seed=4, basic_pbf=True), 160, 40, 1e-3),
+             (scenes.water_drop(total=15_000, seed=5, basic_pbf=False), 256, 8, 0.0)]
+
+    def make(spec, maxn, it, tg):
+        ctx = Context(particle_capacity=int(spec.n * 1.3) + 64, max_neighbors=maxn,
+                      max_log2res=max(spec.log2res, 3))
+        ctx.set_settings(basic_pbf=1 if spec.basic_pbf else 0, solver_iterations=it, density_error_target=tg)
+        ctx.set_scene(spec.grid_min, spec.grid_max, spec.log2res, spec.acceleration)
+        ctx.set_boxes(spec.box_min, spec.box_max)
+        ctx.upload(spec.state)
+        return ctx
+
+    dt = specs[0][0].dt
+    batched = [make(*s) for s in specs]
+    batch = Batch(batched)
+    for _ in range(8):
+        batch.substep(dt)
+    single = [make(*s) for s in specs]
+    for c in single:
+        for _ in range(8):
+            c.substep(dt)
+    for a, b in zip(batched, single):
+        ia, ib = a.check_status(), b.check_status()
+        assert (ia.density_passes, ia.converged_substeps) == (ib.density_passes, ib.converged_substeps)
+        sa, ta = a.download()
+        sb, tb = b.download()
+        _same(sa, sb)
+        _same(ta, tb)
+    batch.close()
+    for c in batched + single:
+        c.close()
