@@ -39,6 +39,8 @@ WORKLOADS = {
     "water_drop_250k": ("water_drop", dict(total=250_000, basic_pbf=False)),
     "water_drop_250k_plain": ("water_drop", dict(total=250_000, basic_pbf=True)),
     "dam_break_32k": ("dam_break", dict(n_side=32)),
+    # 64 independent scenes, log-uniform 4k-200k particles, one graph launch per substep
+    "batch64": ("batch", dict(scenes=64, lo=4_000, hi=200_000)),
 }
 DEFAULT_WORKLOAD = "water_drop_250k_plain"
 
@@ -159,9 +161,12 @@ def traffic_from_profiles(kernel: str, n: int, pairs: int) -> float | None:
 
 
 # ----------------------------------------------------------------------------- CPU baseline
-def cpu_baseline(spec, budget_s: float = 15.0) -> dict:
+def cpu_baseline(workload: str, budget_s: float = 15.0) -> dict:
+    """The single-threaded FP64 oracle on a bounded sample: the same scene at 1/8 of
+    the particle count (every length halved), substeps until the budget is spent."""
     from oracle import oracle as orc
 
+    spec = make_spec(workload, scale=1.0 / 8.0)
     fs = orc.FluidState(spec.state)
     sc = orc.make_scene(orc.settings_from(settings_dict(spec)), spec.grid_min, spec.grid_max, spec.log2res,
                         spec.acceleration)
@@ -169,11 +174,13 @@ def cpu_baseline(spec, budget_s: float = 15.0) -> dict:
     while True:
         orc.substep(fs, sc, (spec.box_min, spec.box_max), np.float32(spec.dt), int(spec.n * 64))
         steps += 1
-        if time.perf_counter() - t0 > budget_s or steps >= 3:
+        if time.perf_counter() - t0 > budget_s or steps >= 20:
             break
     el = time.perf_counter() - t0
     return {"value": spec.n * steps / el, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"{steps} substep(s) of the full {spec.n}-particle scene, single-threaded FP64 oracle, "
+            "sample": f"{steps} substep(s) from the start of the {spec.n}-particle (1/8 scale) version of the "
+                      f"scene, reference Jacobi rule until {settings_dict(spec)['density_error_target']} "
+                      f"(max {settings_dict(spec)['solver_iterations']} passes), single-threaded FP64 oracle, "
                       f"{el:.1f} s"}
 
 
@@ -429,7 +436,7 @@ def run_ours(args) -> None:
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(spec)
+        cpu = cpu_baseline(args.workload)
 
     if rank == 0:
         solver = ("learned warm start (BF16 MLP first update) + projected Jacobi passes" if learned
@@ -458,6 +465,215 @@ def run_ours(args) -> None:
     ctx.close()
     if dist:
         dist.destroy_process_group()
+
+
+# ----------------------------------------------------------------------------- batch
+def batch_specs(n_scenes: int, lo: int, hi: int, seed: int = 7) -> list:
+    """Seeded scene table: particle counts log-uniform in [lo, hi]; every other scene a
+    dam break (single kernel width), the rest water drops, half of them adaptive."""
+    from apbf_gb300 import scenes
+
+    rng = np.random.default_rng(seed)
+    counts = np.exp(rng.uniform(np.log(lo), np.log(hi), size=n_scenes)).astype(int)
+    out = []
+    for k, c in enumerate(counts):
+        if k % 2 == 0:
+            out.append(scenes.dam_break(n_side=max(8, int(round(c ** (1.0 / 3.0)))), seed=k))
+        else:
+            out.append(scenes.water_drop(total=int(c), seed=k, basic_pbf=(k % 4 == 1)))
+    return out
+
+
+def run_batch(args) -> None:
+    """Config-4 style throughput: many independent scenes of uneven sizes advanced by
+    one graph launch per substep (their substeps are the graph's parallel branches),
+    against the same scenes advanced one after the other."""
+    import torch
+
+    from apbf_gb300 import _native as N
+    from apbf_gb300.api import Batch, Context
+    from apbf_gb300.warmstart import SampleBuffer, WarmStartNet, record_rollout
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    torch.cuda.set_device(local)
+    _, kw = WORKLOADS[args.workload]
+    specs = batch_specs(kw["scenes"], kw["lo"], kw["hi"], seed=7 + rank)
+    dt = 1.0 / 240.0  # one time step for the whole batch
+
+    def make(spec, mode=0, net=None):
+        maxn = 128 if spec.basic_pbf and spec.name == "dam_break" else (192 if spec.basic_pbf else 256)
+        ctx = Context(particle_capacity=int(spec.n * 1.3) + 1024, max_neighbors=maxn,
+                      max_log2res=max(spec.log2res, 3), device=local)
+        ctx.set_settings(basic_pbf=1 if spec.basic_pbf else 0, solver_iterations=args.max_iterations,
+                         density_error_target=args.error_target)
+        ctx.set_scene(spec.grid_min, spec.grid_max, spec.log2res, spec.acceleration)
+        ctx.set_boxes(spec.box_min, spec.box_max)
+        ctx.upload(spec.state)
+        ctx.set_solve_graph(2)
+        if net is not None:
+            ctx.mlp_load(net.params)
+        if mode:
+            ctx.set_warm_start(mode)
+        return ctx
+
+    # warm start: one network for the mixture, trained on projected-rule rollouts of
+    # small scenes of each kind with seeds the batch does not use
+    t0 = time.perf_counter()
+    from apbf_gb300 import scenes as S
+
+    train = [S.dam_break(n_side=24, seed=901), S.water_drop(total=40_000, seed=902, basic_pbf=True),
+             S.water_drop(total=40_000, seed=903, basic_pbf=False)]
+    buf = SampleBuffer.allocate(12_000_000, device=local)
+    for sp in train:
+        c = make(sp, N.WARM_PROJECTED)
+        record_rollout(c, dt, 120, buf, iterations=args.max_iterations, every=2)
+        c.check_status()
+        c.close()
+    X, T = buf.view()
+    net = WarmStartNet(device=local, seed=0)
+    net.set_normalization(X, T)
+    net.fit(X, T, epochs=args.ws_epochs, batch=32768)
+    net.min_neighbors = args.ws_min_neighbors
+    net.omega_max = args.ws_omega
+    n_samples = int(X.shape[0])
+    del buf, X, T
+    torch.cuda.empty_cache()
+    train_s = time.perf_counter() - t0
+
+    mode = N.WARM_LEARNED | N.WARM_PROJECTED
+    ctxs = [make(sp, mode, net) for sp in specs]
+    batch = Batch(ctxs)
+    for _ in range(args.presteps if args.presteps >= 0 else 40):
+        batch.substep(dt)
+    for c in ctxs:
+        c.autotune()
+    for _ in range(args.warmup):
+        batch.substep(dt)
+    for c in ctxs:
+        c.check_status()
+    n_total = sum(sp.n for sp in specs)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    stream = torch.cuda.current_stream()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    l0 = sum(c.launch_count() for c in ctxs)
+    torch.cuda.synchronize()
+    for k in range(args.steps):
+        flush.zero_()
+        ev[k][0].record(stream)
+        batch.substep(dt)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = sum(c.launch_count() for c in ctxs) - l0
+    total_ms = float(np.sum([a.elapsed_time(b) for a, b in ev]))
+    infos = [c.check_status() for c in ctxs]
+    errs = [float(c.reduce_fp64()[2]) for c in ctxs]
+    passes = sum(i.density_passes for i in infos) / (len(ctxs) * args.steps)
+    conv = sum(i.converged_substeps for i in infos)
+    value = n_total * args.steps / (total_ms / 1000.0)
+
+    # the same scenes one after the other (each a whole-substep graph), same state
+    ev2 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    for k in range(args.steps):
+        flush.zero_()
+        ev2[k][0].record(stream)
+        for c in ctxs:
+            c.substep(dt)
+        ev2[k][1].record(stream)
+    torch.cuda.synchronize()
+    seq_ms = float(np.sum([a.elapsed_time(b) for a, b in ev2]))
+
+    # per-scene density error: the device's FP64 value against the oracle's FP64
+    # recomputation on the same (downloaded) state, for every 8th scene
+    e2e = run_batch_e2e(batch, ctxs, args, dt)
+    check = []
+    if rank == 0 and not args.no_cpu_baseline:
+        from apbf_gb300.api import incompressibility, neighborhood_green
+        from oracle import oracle as orc
+
+        # every 8th scene, alternating dam breaks, plain and adaptive water drops
+        for k in [8 * i + (0, 1, 3)[i % 3] for i in range(len(ctxs) // 8)]:
+            c, sp = ctxs[k], specs[k]
+            scale = 1.0 if sp.basic_pbf else 1.5
+            st, _ = c.download()
+            # device: neighbour search + one density pass on this state (FP32 sums, FP64 mean)
+            neighborhood_green().set_data(c).set_range_scale(scale).set_position_range(
+                sp.grid_min, sp.grid_max, sp.log2res).apply()
+            incompressibility().set_data(c).apply()
+            e_dev = float(c.reduce_fp64()[2])
+            # oracle: the same state in FP64
+            fs = orc.FluidState(st)
+            orc.neighborhood_green(fs, scale, sp.grid_min, sp.grid_max, sp.log2res, int(st["position"].shape[0] * 160))
+            e_or = float(orc.density_error(fs, orc.settings_from(c.settings))[0])
+            check.append({"scene": k, "particles": int(st["position"].shape[0]), "adaptive": not sp.basic_pbf,
+                          "device": e_dev, "oracle_fp64": e_or, "abs_diff": abs(e_dev - e_or)})
+    batch.close()
+    for c in ctxs:
+        c.close()
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (int32 fixed-point positions and sums; bf16 MLP)",
+            "data": "synthetic (seeded scene table)",
+            "config": {"workload": args.workload, "scenes": len(specs), "particles_total": int(n_total),
+                       "particles_min": int(min(sp.n for sp in specs)), "particles_max": int(max(sp.n for sp in specs)),
+                       "adaptive_scenes": int(sum(not sp.basic_pbf for sp in specs)), "dt": dt,
+                       "solver": "learned warm start + projected Jacobi passes, per-scene convergence",
+                       "iterations": f"until mean density error <= {args.error_target} (max {args.max_iterations})",
+                       "density_passes_per_scene_substep": passes,
+                       "converged_scene_substeps": f"{conv}/{len(ctxs) * args.steps}",
+                       "launch": "one CUDA graph per substep, scenes as parallel branches",
+                       "l2": "flushed between timed steps (256 MB write)"},
+            "sequential": {"ms_per_step": seq_ms / args.steps,
+                           "value": n_total * args.steps / (seq_ms / 1000.0),
+                           "note": "the same scenes, one whole-substep graph launch each, one after the other"},
+            "scene_density_error_last_pass": {"min": min(errs), "max": max(errs), "mean": float(np.mean(errs))},
+            "oracle_density_error_check": check,
+            "warm_start_training": {"samples": n_samples, "seconds": round(train_s, 2)},
+            "roofline": None, "gpu_launches": int(launches), "clocks": clk, "e2e": e2e,
+            "cpu_baseline": None,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def run_batch_e2e(batch, ctxs, args, dt) -> dict:
+    """Per step: H2D of every scene's positions and velocities from pinned host memory,
+    one batched substep, D2H of the resulting positions and velocities."""
+    import torch
+
+    hosts = []
+    for c in ctxs:
+        n, _ = c.lengths()
+        v = c.fluid_view()
+        hosts.append((n, v["position"][:n].cpu().pin_memory(), v["velocity"][:n].cpu().pin_memory()))
+    nbytes = sum(p.numel() * 4 + q.numel() * 4 for _, p, q in hosts)
+    steps = max(3, min(args.steps, 10))
+    stream = torch.cuda.current_stream()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    total = 0
+    for _ in range(steps):
+        for c, (n, p, q) in zip(ctxs, hosts):
+            v = c.fluid_view()
+            v["position"][:n].copy_(p, non_blocking=True)
+            v["velocity"][:n].copy_(q, non_blocking=True)
+        batch.substep(dt)
+        for c, (n, p, q) in zip(ctxs, hosts):
+            v = c.fluid_view()
+            p.copy_(v["position"][:n], non_blocking=True)
+            q.copy_(v["velocity"][:n], non_blocking=True)
+            total += n
+        stream.synchronize()
+    el = time.perf_counter() - t0
+    return {"value": total / el, "unit": UNIT, "h2d_bytes_per_step": int(nbytes), "d2h_bytes_per_step": int(nbytes),
+            "steps": steps}
 
 
 def run_e2e(ctx, spec, args, local) -> dict:
@@ -517,6 +733,8 @@ def main() -> None:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif WORKLOADS[args.workload][0] == "batch":
+        run_batch(args)
     else:
         run_ours(args)
 
