@@ -135,6 +135,12 @@ class StatusInfo(C.Structure):
     ]
 
 
+class Emitter(C.Structure):
+    _fields_ = [("origin", C.c_float * 3), ("radius", C.c_float), ("nx", C.c_uint32), ("nz", C.c_uint32),
+                ("speed", C.c_float), ("jitter", C.c_float), ("seed", C.c_uint32), ("max_particles", C.c_uint32),
+                ("enabled", C.c_uint32), ("pad", C.c_uint32)]
+
+
 class Tuning(C.Structure):
     _fields_ = [("gather_lanes", C.c_uint32), ("reserved0", C.c_uint32), ("reserved", C.c_uint32 * 6)]
 
@@ -156,6 +162,9 @@ SIGNATURES = {
     "apbf_destroy": (_ST, [_P]),
     "apbf_set_settings": (_ST, [_P, C.POINTER(Settings)]),
     "apbf_set_scene": (_ST, [_P, C.POINTER(Scene)]),
+    "apbf_set_emitter": (_ST, [_P, _P]),
+    "apbf_set_oriented_boxes": (_ST, [_P, _P, _P, _P, C.c_uint32]),
+    "apbf_get_box_rotations": (_ST, [_P, _P, C.c_uint32]),
     "apbf_set_boxes": (_ST, [_P, _F3, _F3, C.c_uint32]),
     "apbf_fluid_get_view": (_ST, [_P, C.POINTER(FluidView)]),
     "apbf_transfers_get_view": (_ST, [_P, C.POINTER(TransfersView)]),

@@ -128,6 +128,41 @@ class Context:
                 "apbf_set_boxes")
         return self
 
+    def load_scene(self, spec) -> "Context":
+        """Scene range, boxes (axis-aligned and oriented), emitter and particle state of a
+        scenes.SceneSpec."""
+        self.set_scene(spec.grid_min, spec.grid_max, spec.log2res, spec.acceleration)
+        self.set_boxes(spec.box_min, spec.box_max)
+        if spec.meta.get("oriented_boxes") is not None:
+            self.set_oriented_boxes(*spec.meta["oriented_boxes"])
+        if spec.meta.get("emitter"):
+            self.set_emitter(**spec.meta["emitter"])
+        self.upload(spec.state)
+        return self
+
+    def set_oriented_boxes(self, center: np.ndarray, half: np.ndarray, quat: np.ndarray) -> "Context":
+        """Oriented boxes after the axis-aligned ones (centre, half extents, quaternion x y z w)."""
+        c = np.ascontiguousarray(center, dtype=np.float32).reshape(-1, 4)
+        h = np.ascontiguousarray(half, dtype=np.float32).reshape(-1, 4)
+        q = np.ascontiguousarray(quat, dtype=np.float32).reshape(-1, 4)
+        N.check(self.lib.apbf_set_oriented_boxes(self.handle, c.ctypes.data_as(N._F3), h.ctypes.data_as(N._F3),
+                                                 q.ctypes.data_as(N._F3), c.shape[0]), "apbf_set_oriented_boxes")
+        return self
+
+    def box_rotations(self, n: int) -> np.ndarray:
+        """Rotation rows of the first n boxes as the device uses them (n x 3 x 4 floats)."""
+        out = np.zeros((n, 3, 4), np.float32)
+        N.check(self.lib.apbf_get_box_rotations(self.handle, out.ctypes.data_as(N._F3), n), "apbf_get_box_rotations")
+        return out
+
+    def set_emitter(self, origin, radius: float, nx: int, nz: int, speed: float, jitter: float = 0.2,
+                    seed: int = 0, max_particles: int = 0, enabled: bool = True) -> "Context":
+        e = N.Emitter((C.c_float * 3)(*origin), radius, nx, nz, speed, jitter, seed, max_particles,
+                      1 if enabled else 0, 0)
+        N.check(self.lib.apbf_set_emitter(self.handle, C.byref(e)), "apbf_set_emitter")
+        self.emitter = e
+        return self
+
     def set_debug(self, enable: bool) -> None:
         N.check(self.lib.apbf_set_debug(self.handle, 1 if enable else 0), "apbf_set_debug")
 

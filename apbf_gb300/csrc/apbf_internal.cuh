@@ -213,7 +213,12 @@ struct apbf_ctx {
 
     float4 *box_min = nullptr;
     float4 *box_max = nullptr;
+    float4 *box_rot = nullptr;  // 3 rows per box; row 0 .w != 0 marks an oriented box
     uint32_t n_boxes = 0;
+    uint32_t n_aabb = 0;        // boxes set by apbf_set_boxes (the oriented ones follow)
+    apbf_emitter emitter = {};  // emitter.enabled == 0: none
+    float emit_inv_mass = 0.0f;
+    double *emit_state = nullptr;  // device: [0] stream time T, [1] particles emitted, [2..3] this substep's plan
 
     apbf::Status *status = nullptr;
     uint32_t n_cells_log2_alloc = 0;
@@ -294,7 +299,16 @@ inline int grid_for(const apbf_ctx *ctx, uint32_t n, int block = kBlock, int per
     return (int)(need < cap ? need : cap);
 }
 
+// float -> int32 truncating toward zero, saturating, NaN -> 0 (rule C4), on the host
+inline int32_t f2i_host(float x) {
+    if (!(x == x)) return 0;
+    if (x >= 2147483647.0f) return 2147483647;
+    if (x <= -2147483648.0f) return (int32_t)(-2147483647 - 1);
+    return (int32_t)x;
+}
+
 // ---- host-side stage launchers (defined in the .cu files) ----
+apbf_status emit(apbf_ctx *ctx, float dt, cudaStream_t s);  // glue.cu
 apbf_status sort_pairs_device(apbf_ctx *ctx, const uint32_t *keys_in, const uint32_t *vals_in, const uint32_t *d_count,
                               uint32_t max_count, uint32_t key_bits, uint32_t *keys_out, uint32_t *vals_out,
                               cudaStream_t s);
@@ -499,9 +513,58 @@ __device__ __forceinline__ float3 hash31_rn(float p) {  // shadertoy 4djSRW hash
                        fract_rn(__fmul_rn(__fadd_rn(q.y, q.z), q.x)));
 }
 
-// Pushes one particle (sorted id `id`, radius r) out of every box.
+// box_collision.comp:35-57 on one box in the box's own frame: (qx, qy, qz) is the
+// particle position relative to the frame, [lo, hi] the box; the box is grown by the
+// radius and by the hash jitter h1 / h2, and the particle is moved out through the
+// nearest face of whichever corner is closer.  Returns whether it moved.
+__device__ __forceinline__ bool push_out(float &qx, float &qy, float &qz, float3 lo, float3 hi, float r, float3 h1,
+                                         float3 h2) {
+    float tx0 = __fsub_rn(__fsub_rn(__fsub_rn(lo.x, r), __fmul_rn(h1.x, 0.05f)), qx);
+    float ty0 = __fsub_rn(__fsub_rn(__fsub_rn(lo.y, r), __fmul_rn(h1.y, 0.05f)), qy);
+    float tz0 = __fsub_rn(__fsub_rn(__fsub_rn(lo.z, r), __fmul_rn(h1.z, 0.05f)), qz);
+    float tx1 = __fsub_rn(__fadd_rn(__fadd_rn(hi.x, r), __fmul_rn(h2.x, 0.05f)), qx);
+    float ty1 = __fsub_rn(__fadd_rn(__fadd_rn(hi.y, r), __fmul_rn(h2.y, 0.05f)), qy);
+    float tz1 = __fsub_rn(__fadd_rn(__fadd_rn(hi.z, r), __fmul_rn(h2.z, 0.05f)), qz);
+    // smallestComponent(-toMin) and smallestComponent(toMax), box_collision.comp:27-33
+    {
+        const float vx = -tx0, vy = -ty0, vz = -tz0;
+        const bool b1 = vx <= vy, b2 = vx <= vz, b3 = vy <= vz;
+        tx0 = __fmul_rn(tx0, (b1 && b2) ? 1.0f : 0.0f);
+        ty0 = __fmul_rn(ty0, (!b1 && b3) ? 1.0f : 0.0f);
+        tz0 = __fmul_rn(tz0, (!b2 && !b3) ? 1.0f : 0.0f);
+    }
+    {
+        const bool b1 = tx1 <= ty1, b2 = tx1 <= tz1, b3 = ty1 <= tz1;
+        tx1 = __fmul_rn(tx1, (b1 && b2) ? 1.0f : 0.0f);
+        ty1 = __fmul_rn(ty1, (!b1 && b3) ? 1.0f : 0.0f);
+        tz1 = __fmul_rn(tz1, (!b2 && !b3) ? 1.0f : 0.0f);
+    }
+    const float dmin = -__fadd_rn(__fadd_rn(tx0, ty0), tz0);
+    const float dmax = __fadd_rn(__fadd_rn(tx1, ty1), tz1);
+    if (dmin <= 0.0f || dmax <= 0.0f) return false;
+    if (dmin < dmax) {
+        qx = __fadd_rn(qx, tx0);
+        qy = __fadd_rn(qy, ty0);
+        qz = __fadd_rn(qz, tz0);
+    } else {
+        qx = __fadd_rn(qx, tx1);
+        qy = __fadd_rn(qy, ty1);
+        qz = __fadd_rn(qz, tz1);
+    }
+    return true;
+}
+
+__device__ __forceinline__ float dot3_rn(float4 a, float x, float y, float z) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(a.x, x), __fmul_rn(a.y, y)), __fmul_rn(a.z, z));
+}
+
+// Pushes one particle (sorted id `id`, radius r) out of every box.  Box k is
+// axis-aligned ([bmin, bmax], as in the reference) unless rot[3k].w != 0: then it
+// is oriented, bmin = its centre, bmax = its half extents and rot[3k..3k+2] the
+// rows of its rotation (local axis i = row i), and the same push runs in its frame.
 __device__ __forceinline__ int4 box_push(int4 ip, float r, uint32_t id, const float4 *__restrict__ bmin,
-                                         const float4 *__restrict__ bmax, uint32_t nb) {
+                                         const float4 *__restrict__ bmax, const float4 *__restrict__ rot,
+                                         uint32_t nb) {
     if (nb == 0) return ip;
     float px = __fdiv_rn((float)ip.x, 262144.0f), py = __fdiv_rn((float)ip.y, 262144.0f),
           pz = __fdiv_rn((float)ip.z, 262144.0f);
@@ -510,38 +573,20 @@ __device__ __forceinline__ int4 box_push(int4 ip, float r, uint32_t id, const fl
         const float3 h1 = hash31_rn(__fsub_rn(__fsub_rn(__fmul_rn(fid, px), py), pz));
         const float3 h2 = hash31_rn(__fadd_rn(__fadd_rn(__fmul_rn(fid, py), px), pz));
         const float4 lo = bmin[k], hi = bmax[k];
-        float tx0 = __fsub_rn(__fsub_rn(__fsub_rn(lo.x, r), __fmul_rn(h1.x, 0.05f)), px);
-        float ty0 = __fsub_rn(__fsub_rn(__fsub_rn(lo.y, r), __fmul_rn(h1.y, 0.05f)), py);
-        float tz0 = __fsub_rn(__fsub_rn(__fsub_rn(lo.z, r), __fmul_rn(h1.z, 0.05f)), pz);
-        float tx1 = __fsub_rn(__fadd_rn(__fadd_rn(hi.x, r), __fmul_rn(h2.x, 0.05f)), px);
-        float ty1 = __fsub_rn(__fadd_rn(__fadd_rn(hi.y, r), __fmul_rn(h2.y, 0.05f)), py);
-        float tz1 = __fsub_rn(__fadd_rn(__fadd_rn(hi.z, r), __fmul_rn(h2.z, 0.05f)), pz);
-        // smallestComponent(-toMin) and smallestComponent(toMax), box_collision.comp:27-33
-        {
-            const float vx = -tx0, vy = -ty0, vz = -tz0;
-            const bool b1 = vx <= vy, b2 = vx <= vz, b3 = vy <= vz;
-            tx0 = __fmul_rn(tx0, (b1 && b2) ? 1.0f : 0.0f);
-            ty0 = __fmul_rn(ty0, (!b1 && b3) ? 1.0f : 0.0f);
-            tz0 = __fmul_rn(tz0, (!b2 && !b3) ? 1.0f : 0.0f);
+        const float4 r0 = rot[3 * k];
+        if (r0.w == 0.0f) {
+            push_out(px, py, pz, make_float3(lo.x, lo.y, lo.z), make_float3(hi.x, hi.y, hi.z), r, h1, h2);
+            continue;
         }
-        {
-            const bool b1 = tx1 <= ty1, b2 = tx1 <= tz1, b3 = ty1 <= tz1;
-            tx1 = __fmul_rn(tx1, (b1 && b2) ? 1.0f : 0.0f);
-            ty1 = __fmul_rn(ty1, (!b1 && b3) ? 1.0f : 0.0f);
-            tz1 = __fmul_rn(tz1, (!b2 && !b3) ? 1.0f : 0.0f);
-        }
-        const float dmin = -__fadd_rn(__fadd_rn(tx0, ty0), tz0);
-        const float dmax = __fadd_rn(__fadd_rn(tx1, ty1), tz1);
-        if (dmin <= 0.0f || dmax <= 0.0f) continue;
-        if (dmin < dmax) {
-            px = __fadd_rn(px, tx0);
-            py = __fadd_rn(py, ty0);
-            pz = __fadd_rn(pz, tz0);
-        } else {
-            px = __fadd_rn(px, tx1);
-            py = __fadd_rn(py, ty1);
-            pz = __fadd_rn(pz, tz1);
-        }
+        const float4 r1 = rot[3 * k + 1], r2 = rot[3 * k + 2];
+        const float dx = __fsub_rn(px, lo.x), dy = __fsub_rn(py, lo.y), dz = __fsub_rn(pz, lo.z);
+        float qx = dot3_rn(r0, dx, dy, dz), qy = dot3_rn(r1, dx, dy, dz), qz = dot3_rn(r2, dx, dy, dz);
+        if (!push_out(qx, qy, qz, make_float3(-hi.x, -hi.y, -hi.z), make_float3(hi.x, hi.y, hi.z), r, h1, h2))
+            continue;
+        // back to the world frame: p = centre + R^T q
+        px = __fadd_rn(lo.x, __fadd_rn(__fadd_rn(__fmul_rn(r0.x, qx), __fmul_rn(r1.x, qy)), __fmul_rn(r2.x, qz)));
+        py = __fadd_rn(lo.y, __fadd_rn(__fadd_rn(__fmul_rn(r0.y, qx), __fmul_rn(r1.y, qy)), __fmul_rn(r2.y, qz)));
+        pz = __fadd_rn(lo.z, __fadd_rn(__fadd_rn(__fmul_rn(r0.z, qx), __fmul_rn(r1.z, qy)), __fmul_rn(r2.z, qz)));
     }
     return make_int4(f2i(__fmul_rn(px, 262144.0f)), f2i(__fmul_rn(py, 262144.0f)), f2i(__fmul_rn(pz, 262144.0f)), ip.w);
 }

@@ -187,6 +187,8 @@ apbf_status apbf_create(const apbf_config *cfg, apbf_ctx **out) {
     A(ctx->red_out, 4);
     A(ctx->box_min, APBF_MAX_BOXES);
     A(ctx->box_max, APBF_MAX_BOXES);
+    A(ctx->box_rot, 3 * APBF_MAX_BOXES);
+    A(ctx->emit_state, 8);
     A(ctx->status, 1);
 #undef A
     cudaMemset(ctx->d_len, 0, kLenSlots * sizeof(uint32_t));
@@ -238,9 +240,68 @@ apbf_status apbf_set_boxes(apbf_ctx *ctx, const float *bmin, const float *bmax, 
     if (n) {
         APBF_CUDA(cudaMemcpy(ctx->box_min, bmin, n * sizeof(float4), cudaMemcpyHostToDevice));
         APBF_CUDA(cudaMemcpy(ctx->box_max, bmax, n * sizeof(float4), cudaMemcpyHostToDevice));
+        std::vector<float4> zero(3 * (size_t)n, make_float4(0.f, 0.f, 0.f, 0.f));  // axis-aligned
+        APBF_CUDA(cudaMemcpy(ctx->box_rot, zero.data(), zero.size() * sizeof(float4), cudaMemcpyHostToDevice));
     }
     ctx->n_boxes = n;
+    ctx->n_aabb = n;
     ctx->graph_version++;
+    return APBF_OK;
+}
+
+apbf_status apbf_set_emitter(apbf_ctx *ctx, const apbf_emitter *e) {
+    if (!ctx || !e) return APBF_ERR_INVALID_ARG;
+    if (e->enabled && (!(e->radius > 0.0f) || !(e->speed > 0.0f) || e->nx == 0 || e->nz == 0 || !(e->jitter >= 0.0f) ||
+                       (uint64_t)e->nx * e->nz > 0xffffffu)) {
+        set_error("apbf_set_emitter: radius and speed > 0, 1 <= nx * nz <= 2^24, jitter >= 0");
+        return APBF_ERR_INVALID_ARG;
+    }
+    cudaSetDevice(ctx->device);
+    ctx->emitter = *e;
+    const double d = 2.0 * (double)e->radius;
+    ctx->emit_inv_mass = (float)(1.0 / (d * d * d));
+    APBF_CUDA(cudaMemset(ctx->emit_state, 0, 8 * sizeof(double)));
+    ctx->graph_version++;
+    return APBF_OK;
+}
+
+apbf_status apbf_set_oriented_boxes(apbf_ctx *ctx, const float *center, const float *half, const float *quat,
+                                    uint32_t n) {
+    if (!ctx || ctx->n_aabb + n > APBF_MAX_BOXES || (n && (!center || !half || !quat))) return APBF_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    std::vector<float4> c(n), h(n), rot(3 * (size_t)n);
+    for (uint32_t k = 0; k < n; ++k) {
+        const double qx = quat[4 * k], qy = quat[4 * k + 1], qz = quat[4 * k + 2], qw = quat[4 * k + 3];
+        const double nq = std::sqrt(qx * qx + qy * qy + qz * qz + qw * qw);
+        if (!(nq > 0.0) || !(half[4 * k] >= 0.0f) || !(half[4 * k + 1] >= 0.0f) || !(half[4 * k + 2] >= 0.0f)) {
+            set_error("apbf_set_oriented_boxes: zero quaternion or negative half extent");
+            return APBF_ERR_INVALID_ARG;
+        }
+        const double x = qx / nq, y = qy / nq, z = qz / nq, w = qw / nq;
+        // rows of R^T, i.e. the box's local axes in world coordinates (R rotates local -> world)
+        const double m[3][3] = {{1 - 2 * (y * y + z * z), 2 * (x * y + z * w), 2 * (x * z - y * w)},
+                                {2 * (x * y - z * w), 1 - 2 * (x * x + z * z), 2 * (y * z + x * w)},
+                                {2 * (x * z + y * w), 2 * (y * z - x * w), 1 - 2 * (x * x + y * y)}};
+        for (int r = 0; r < 3; ++r)
+            rot[3 * k + r] = make_float4((float)m[r][0], (float)m[r][1], (float)m[r][2], r == 0 ? 1.0f : 0.0f);
+        c[k] = make_float4(center[4 * k], center[4 * k + 1], center[4 * k + 2], 0.0f);
+        h[k] = make_float4(half[4 * k], half[4 * k + 1], half[4 * k + 2], 0.0f);
+    }
+    const uint32_t o = ctx->n_aabb;
+    if (n) {
+        APBF_CUDA(cudaMemcpy(ctx->box_min + o, c.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
+        APBF_CUDA(cudaMemcpy(ctx->box_max + o, h.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
+        APBF_CUDA(cudaMemcpy(ctx->box_rot + 3 * o, rot.data(), rot.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    }
+    ctx->n_boxes = o + n;
+    ctx->graph_version++;
+    return APBF_OK;
+}
+
+apbf_status apbf_get_box_rotations(apbf_ctx *ctx, float *rot_out, uint32_t n) {
+    if (!ctx || !rot_out || n > ctx->n_boxes) return APBF_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    APBF_CUDA(cudaMemcpy(rot_out, ctx->box_rot, 3 * (size_t)n * sizeof(float4), cudaMemcpyDeviceToHost));
     return APBF_OK;
 }
 
@@ -373,7 +434,9 @@ namespace apbf {
 // that graph instead of a launch of its own.
 apbf_status substep_body(apbf_ctx *ctx, float dt, cudaStream_t s, bool capture) {
     const apbf_settings &st = ctx->settings;
-    apbf_status r = velocity_handling(ctx, dt, ctx->scene.acceleration, s);
+    apbf_status r = emit(ctx, dt, s);  // new particles first (no reference counterpart)
+    if (r != APBF_OK) return r;
+    r = velocity_handling(ctx, dt, ctx->scene.acceleration, s);
     if (r != APBF_OK) return r;
     const bool adaptive = !st.basic_pbf;
     if (adaptive && (st.merge || st.split)) {

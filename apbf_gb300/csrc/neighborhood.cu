@@ -179,7 +179,7 @@ struct BuildArgs {
     int4 *pos_box;  // when non-null: receives box_collision(pos) (the first Jacobi iteration's box pass)
     const float *range;
     const float *radius;
-    const float4 *bmin, *bmax;
+    const float4 *bmin, *bmax, *rot;
     uint32_t nboxes;
     float scale;
     const uint32_t *d_len;
@@ -231,7 +231,7 @@ __global__ void __launch_bounds__(256, 3) k_build_rows(BuildArgs a) {
         }
         a.count[i] = c < a.maxn ? c : a.maxn;
         local += c < a.maxn ? c : a.maxn;
-        if (a.pos_box) a.pos_box[i] = box_push(p, a.radius[i], i, a.bmin, a.bmax, a.nboxes);
+        if (a.pos_box) a.pos_box[i] = box_push(p, a.radius[i], i, a.bmin, a.bmax, a.rot, a.nboxes);
     }
     // block reduction of the pair count and of the radius range
     for (int off = 16; off > 0; off >>= 1) {
@@ -350,6 +350,7 @@ apbf_status neighborhood_green(apbf_ctx *ctx, float range_scale, const float min
     ba.radius = f.radius;
     ba.bmin = ctx->box_min;
     ba.bmax = ctx->box_max;
+    ba.rot = ctx->box_rot;
     ba.nboxes = ctx->n_boxes;
     ba.scale = range_scale;
     ba.d_len = ctx->d_len;

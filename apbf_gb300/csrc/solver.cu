@@ -355,7 +355,7 @@ struct PassB {
     const float4 *rec;
     const int4 *shift;
     const float *radius;
-    const float4 *bmin, *bmax;
+    const float4 *bmin, *bmax, *rot;
     uint32_t nboxes;  // > 0: box collision of the next iteration applied to the output
     const uint32_t *count;
     const uint32_t *idx;
@@ -454,7 +454,7 @@ __global__ void __launch_bounds__(256, GAUSS && L == 1 ? 5 : 4) k_delta(PassB a)
         ay = wadd(ay, sh.y);
         az = wadd(az, sh.z);
         int4 out = make_int4(wadd(p.x, ax), wadd(p.y, ay), wadd(p.z, az), p.w);
-        if (nboxes) out = box_push(out, a.radius[j], j, a.bmin, a.bmax, nboxes);
+        if (nboxes) out = box_push(out, a.radius[j], j, a.bmin, a.bmax, a.rot, nboxes);
         a.pos_out[j] = out;
         if (a.prev_mode | a.acc_mode) {
             const float lj = reinterpret_cast<const float *>(a.rec + j)[0];  // applied (learned) lambda
@@ -584,6 +584,7 @@ apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s, const SolveOpts &o)
     b.radius = f.radius;
     b.bmin = ctx->box_min;
     b.bmax = ctx->box_max;
+    b.rot = ctx->box_rot;
     b.nboxes = box_after ? ctx->n_boxes : 0u;
     b.count = ctx->nb_count;
     b.idx = ctx->nb_idx;

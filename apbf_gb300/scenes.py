@@ -186,3 +186,41 @@ def block(n: int, seed: int = 0, iterations: int = 4, dt: float = 1.0 / 120.0) -
     gmin, gmax, L = _grid_for([0, 0, 0], box)
     return SceneSpec("block", st, bmin, bmax, gmin, gmax, L, (0.0, -392.4, 0.0), dt, iterations, 1, True,
                      {"side": side})
+
+
+def waterfall(initial: int = 384_000, seed: int = 0, substeps: int = 300, iterations: int = 6,
+              basic_pbf: bool = False, per_substep: int = 2000, scale: float = 1.0) -> SceneSpec:
+    """Waterfall: a seeded inflow of `per_substep` particles per substep (radius
+    0.0025 m) from a 0.2 x 0.2 m emitter falls 1.5 m onto a sloped box (30 degrees,
+    0.05 m thick) and runs into a 2 x 1 x 0.6 m tank pre-filled with `initial`
+    particles; dt = 1/240.  The emitter's stream speed follows from the rate:
+    per_substep particles per dt through 40 x 40 lattice cells of spacing 2r.
+    `scale` < 1 shrinks every length (tank, slope, drop, emitter) for tests."""
+    r_m = 0.0025
+    rng = np.random.default_rng(seed)
+    s = float(scale)
+    box = np.array([800.0, 960.0, 240.0]) * s          # x, y (up), z in radii
+    nx_fill, nz_fill = int(box[0] // 2), int(box[2] // 2)
+    layers = max(1, int(round(initial / (nx_fill * nz_fill)))) if initial > 0 else 0
+    pos = lattice([1.0, 1.0, 1.0], [nx_fill, layers, nz_fill], 2.0, 0.2, rng) if layers else np.zeros((0, 3))
+    st = make_state(pos)
+    bmin, bmax = wall_boxes([0, 0, 0], box, lid=True, thickness=32.0)
+    # the slope: descends towards +x; its upper end under the emitter
+    theta = -np.pi / 6.0
+    centre = np.array([300.0, 200.0, 120.0]) * s
+    half = np.array([200.0, 20.0, 100.0]) * s
+    quat = np.array([0.0, 0.0, np.sin(theta / 2.0), np.cos(theta / 2.0)])
+    upper = centre + np.array([np.cos(theta), np.sin(theta), 0.0]) * (-half[0])
+    cells = max(2, int(round(40 * s)))  # emitter lattice cells per side (0.2 m at full size)
+    dt = 1.0 / 240.0
+    speed = per_substep / float(cells * cells) * 2.0 / dt  # radii per second
+    emit_y = upper[1] + half[1] + 600.0 * s                # 1.5 m above the slope's top
+    emitter = dict(origin=(float(upper[0] - cells), float(emit_y), float(centre[2] - cells)), radius=1.0,
+                   nx=cells, nz=cells, speed=float(speed), jitter=0.2, seed=seed + 17)
+    gmin, gmax, L = _grid_for([0, 0, 0], box)
+    return SceneSpec("waterfall", st, bmin, bmax, gmin, gmax, L, (0.0, -9.81 / r_m, 0.0), dt, iterations, substeps,
+                     basic_pbf, {"r_m": r_m, "box": box.tolist(), "emitter": emitter,
+                                 "oriented_boxes": (np.array([[*centre, 0.0]], np.float32),
+                                                    np.array([[*half, 0.0]], np.float32),
+                                                    np.array([quat], np.float32)),
+                                 "capacity": int(initial + per_substep * substeps * 1.05) + 4096, "presteps": 0})

@@ -180,6 +180,42 @@ apbf_status apbf_create(const apbf_config *cfg, apbf_ctx **out);
 apbf_status apbf_destroy(apbf_ctx *ctx);
 apbf_status apbf_set_settings(apbf_ctx *ctx, const apbf_settings *s);   /* settings.cpp:66-90 */
 apbf_status apbf_set_scene(apbf_ctx *ctx, const apbf_scene *scene);
+/* Oriented boxes (no counterpart in the reference, whose boxes are axis-aligned):
+ * appended after the boxes of the last apbf_set_boxes call, each given by its
+ * centre, half extents (float4 each, w ignored) and rotation quaternion (x, y, z,
+ * w; local -> world).  Box collision pushes a particle out of an oriented box with
+ * the reference's rule (box_collision.comp:35-57) applied in the box's frame.
+ * apbf_set_boxes removes them. */
+apbf_status apbf_set_oriented_boxes(apbf_ctx *ctx, const float *center, const float *half, const float *quat,
+                                    uint32_t n);
+/* The rotation rows (3 float4 per box, the boxes' local axes; row 0 .w = 1 for an
+ * oriented box, all zero for an axis-aligned one) of the first n boxes, as used on
+ * the device. */
+apbf_status apbf_get_box_rotations(apbf_ctx *ctx, float *rot_out, uint32_t n);
+/* Particle emitter (no counterpart in the reference, whose scenes create all
+ * particles up front): a lattice stream of spacing 2 radius, nx x nz cells wide,
+ * moving at `speed` along -y through the emission plane y = origin[1].  Layer l
+ * crosses the plane at t_l = l * 2 radius / speed; each apbf_substep(dt) first
+ * appends the layers with T <= t_l < T + dt (T = stream time so far), at
+ * y = origin[1] + (t_l - T) * speed (above the plane, so the substep's velocity
+ * update carries them through it), x = origin[0] + (2i + 1) radius,
+ * z = origin[2] + (2j + 1) radius, each coordinate jittered uniformly by up to
+ * jitter * radius (hash of seed, layer, cell), velocity (0, -speed, 0) and the
+ * fluid defaults of a particle of that radius.  Stops after max_particles (0: no
+ * limit) or at the list capacity (APBF_FLAG_PARTICLE_OVERFLOW). */
+typedef struct apbf_emitter {
+    float origin[3];
+    float radius;
+    uint32_t nx, nz;
+    float speed;
+    float jitter;
+    uint32_t seed;
+    uint32_t max_particles;
+    uint32_t enabled;
+    uint32_t pad;
+} apbf_emitter;
+/* Sets the emitter and restarts its stream (T = 0, nothing emitted). */
+apbf_status apbf_set_emitter(apbf_ctx *ctx, const apbf_emitter *e);
 /* Axis-aligned collision boxes, vec4 min / vec4 max host arrays (user_controlled_boxes). */
 apbf_status apbf_set_boxes(apbf_ctx *ctx, const float *box_min4, const float *box_max4, uint32_t n);
 

@@ -631,35 +631,133 @@ static void smallest_component(const float v[3], float m[3]) {  /* box_collision
 }
 
 /* box_collision.comp:35-60 */
+/* box_collision.comp:35-57 for one box in its own frame (q relative to the frame,
+ * box [lo, hi]); returns whether the particle moved. */
+static int push_out(float q[3], const float lo[3], const float hi[3], float radius, const float h1[3],
+                    const float h2[3]) {
+    float tmin[3], tmax[3], m1[3], m2[3], neg[3];
+    for (int c = 0; c < 3; ++c) {
+        float bmin = (lo[c] - radius) - h1[c] * 0.05f;
+        float bmax = (hi[c] + radius) + h2[c] * 0.05f;
+        tmin[c] = bmin - q[c];
+        tmax[c] = bmax - q[c];
+        neg[c] = -tmin[c];
+    }
+    smallest_component(neg, m1);
+    smallest_component(tmax, m2);
+    for (int c = 0; c < 3; ++c) {
+        tmin[c] *= m1[c];
+        tmax[c] *= m2[c];
+    }
+    float dmin = -((tmin[0] + tmin[1]) + tmin[2]);
+    float dmax = (tmax[0] + tmax[1]) + tmax[2];
+    if (dmin <= 0.0f || dmax <= 0.0f) return 0;
+    for (int c = 0; c < 3; ++c) q[c] += dmin < dmax ? tmin[c] : tmax[c];
+    return 1;
+}
+
 void or_box_collision(or_fluid *f, const or_boxes *b) {
     for (uint32_t id = 0; id < f->n; ++id) {
         int32_t *ip = f->pos + 4 * (size_t)id;
         float pos[3] = {(float)ip[0] / 262144.0f, (float)ip[1] / 262144.0f, (float)ip[2] / 262144.0f};
         float radius = f->radius[id];
         for (uint32_t k = 0; k < b->n; ++k) {
-            float h1[3], h2[3], bmin[3], bmax[3], tmin[3], tmax[3], m1[3], m2[3], neg[3];
+            float h1[3], h2[3];
             hash31(((float)id * pos[0] - pos[1]) - pos[2], h1);
             hash31(((float)id * pos[1] + pos[0]) + pos[2], h2);
-            for (int c = 0; c < 3; ++c) {
-                bmin[c] = (b->bmin[4 * k + c] - radius) - h1[c] * 0.05f;
-                bmax[c] = (b->bmax[4 * k + c] + radius) + h2[c] * 0.05f;
-                tmin[c] = bmin[c] - pos[c];
-                tmax[c] = bmax[c] - pos[c];
-                neg[c] = -tmin[c];
+            const float *lo = b->bmin + 4 * k, *hi = b->bmax + 4 * k;
+            const float *R = b->rot ? b->rot + 12 * k : NULL;
+            if (!R || R[3] == 0.0f) {
+                push_out(pos, lo, hi, radius, h1, h2);
+                continue;
             }
-            smallest_component(neg, m1);
-            smallest_component(tmax, m2);
-            for (int c = 0; c < 3; ++c) {
-                tmin[c] *= m1[c];
-                tmax[c] *= m2[c];
-            }
-            float dmin = -((tmin[0] + tmin[1]) + tmin[2]);
-            float dmax = (tmax[0] + tmax[1]) + tmax[2];
-            if (dmin <= 0.0f || dmax <= 0.0f) continue;
-            for (int c = 0; c < 3; ++c) pos[c] += dmin < dmax ? tmin[c] : tmax[c];
+            /* oriented: q = R (p - centre), push in [-half, half], p = centre + R^T q */
+            float d[3] = {pos[0] - lo[0], pos[1] - lo[1], pos[2] - lo[2]};
+            float q[3], nlo[3] = {-hi[0], -hi[1], -hi[2]};
+            for (int r = 0; r < 3; ++r) q[r] = (R[4 * r] * d[0] + R[4 * r + 1] * d[1]) + R[4 * r + 2] * d[2];
+            if (!push_out(q, nlo, hi, radius, h1, h2)) continue;
+            for (int c = 0; c < 3; ++c) pos[c] = lo[c] + ((R[c] * q[0] + R[4 + c] * q[1]) + R[8 + c] * q[2]);
         }
         for (int c = 0; c < 3; ++c) ip[c] = f2i_f(pos[c] * 262144.0f);
     }
+}
+
+/* ---- emitter (restates the device's k_emit_plan / k_emit) ---- */
+static uint32_t emit_hash(uint32_t seed, uint64_t layer, uint32_t cell, uint32_t axis) {
+    uint64_t z = ((uint64_t)seed << 32) ^ (layer * 0x9E3779B97F4A7C15ull) ^ ((uint64_t)cell << 2) ^ axis;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (uint32_t)(z >> 32);
+}
+
+static int32_t f2i_trunc(float x) {
+    if (!(x == x)) return 0;
+    if (x >= 2147483647.0f) return 2147483647;
+    if (x <= -2147483648.0f) return (int32_t)(-2147483647 - 1);
+    return (int32_t)x;
+}
+
+uint32_t or_emit(or_fluid *f, const or_emitter *e, double state[2], float dt, float last_dt, int *overflow) {
+    if (overflow) *overflow = 0;
+    if (!e->enabled || dt <= 0.0f) return 0;
+    const double T = state[0];
+    const double layer_dt = (2.0 * (double)e->radius) / (double)e->speed;
+    const uint64_t l0 = (uint64_t)ceil(T / layer_dt), l1 = (uint64_t)ceil((T + (double)dt) / layer_dt);
+    const uint64_t per_layer = (uint64_t)e->nx * e->nz;
+    uint64_t want = (l1 - l0) * per_layer;
+    const uint64_t emitted = (uint64_t)state[1];
+    if (e->max_particles && emitted + want > e->max_particles) want = e->max_particles > emitted ? e->max_particles - emitted : 0;
+    const uint32_t n = f->n;
+    const uint64_t room = f->cap > n ? f->cap - n : 0;
+    if (want > room) {
+        if (overflow) *overflow = 1;
+        want = room;
+    }
+    state[0] = T + (double)dt;
+    state[1] = (double)(emitted + want);
+    const float jr = e->jitter * e->radius;
+    const double d = 2.0 * (double)e->radius;
+    const float inv_mass = (float)(1.0 / (d * d * d));
+    const int32_t backup_dy = f2i_trunc(e->speed * last_dt * 262144.0f);
+    for (uint64_t k = 0; k < want; ++k) {
+        const uint64_t layer = l0 + k / per_layer;
+        const uint32_t cell = (uint32_t)(k % per_layer), ci = cell / e->nz, cj = cell % e->nz;
+        float jit[3];
+        for (uint32_t a = 0; a < 3; ++a) {
+            const float u = (float)(emit_hash(e->seed, layer, cell, a) >> 8) * 5.9604644775390625e-8f;
+            jit[a] = ((2.0f * u) - 1.0f) * jr;
+        }
+        const double t_l = (double)layer * layer_dt;
+        const float dy = (float)((t_l - T) * (double)e->speed);
+        const float x = (e->origin[0] + (float)(2u * ci + 1u) * e->radius) + jit[0];
+        const float y = (e->origin[1] + dy) + jit[1];
+        const float z = (e->origin[2] + (float)(2u * cj + 1u) * e->radius) + jit[2];
+        const uint32_t id = n + (uint32_t)k;
+        int32_t *p = f->pos + 4 * (size_t)id, *b = f->pos_backup + 4 * (size_t)id;
+        p[0] = f2i_trunc(x * 262144.0f);
+        p[1] = f2i_trunc(y * 262144.0f);
+        p[2] = f2i_trunc(z * 262144.0f);
+        p[3] = 0;
+        b[0] = p[0];
+        b[1] = (int32_t)((uint32_t)p[1] + (uint32_t)backup_dy);
+        b[2] = p[2];
+        b[3] = 0;
+        float *v = f->vel + 4 * (size_t)id;
+        v[0] = 0.0f;
+        v[1] = -e->speed;
+        v[2] = 0.0f;
+        v[3] = 0.0f;
+        f->inv_mass[id] = inv_mass;
+        f->radius[id] = e->radius;
+        f->transferring[id] = 0u;
+        f->target_radius[id] = e->radius;
+        f->kernel_width[id] = e->radius * 4.0f;
+        f->boundariness[id] = 1.0f;
+        f->boundary_distance[id] = (uint32_t)(e->radius * 262144.0f);
+    }
+    f->n = n + (uint32_t)want;
+    return (uint32_t)want;
 }
 
 /* velocity_handling.cpp:15-31; infer_velocity.comp:30-31, apply_acceleration.comp:26-27,

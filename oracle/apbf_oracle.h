@@ -116,6 +116,10 @@ typedef struct or_boxes {
     uint32_t n;
     const float *bmin;
     const float *bmax;
+    /* NULL, or 12 floats per box: the rows of its rotation (its local axes); row 0
+     * element 3 != 0 marks an oriented box, whose bmin is its centre and bmax its
+     * half extents (no reference counterpart: the reference's boxes are axis-aligned). */
+    const float *rot;
 } or_boxes;
 
 /* ---- primitives (algorithms.cpp) ---- */
@@ -179,6 +183,23 @@ void or_incompressibility_apply(or_fluid *f, const or_neighbors *nb, const or_se
 
 /* ---- substep glue ---- */
 void or_box_collision(or_fluid *f, const or_boxes *b);
+
+/* Emitter (no reference counterpart; the device's apbf_set_emitter / the first
+ * stage of apbf_substep): appends the lattice layers that cross the emission plane
+ * during dt.  state: [0] stream time, [1] particles emitted so far. */
+typedef struct or_emitter {
+    float origin[3];
+    float radius;
+    uint32_t nx, nz;
+    float speed;
+    float jitter;
+    uint32_t seed;
+    uint32_t max_particles;
+    uint32_t enabled;
+    uint32_t pad;
+} or_emitter;
+/* returns the number appended; sets *overflow when the capacity cut the emission */
+uint32_t or_emit(or_fluid *f, const or_emitter *e, double state[2], float dt, float last_dt, int *overflow);
 void or_velocity_handling(or_fluid *f, float dt, float last_dt, const float accel[3]);
 
 /* ---- adaptive stages ---- */

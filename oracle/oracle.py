@@ -77,7 +77,16 @@ class OrNeighbors(C.Structure):
 
 
 class OrBoxes(C.Structure):
-    _fields_ = [("n", C.c_uint32), ("bmin", _f32p), ("bmax", _f32p)]
+    _fields_ = [("n", C.c_uint32), ("bmin", _f32p), ("bmax", _f32p), ("rot", _f32p)]
+
+
+def _boxes(boxes) -> tuple:
+    """(bmin, bmax) or (bmin, bmax, rot) -> OrBoxes and the arrays it points into."""
+    lo = np.ascontiguousarray(boxes[0], np.float32)
+    hi = np.ascontiguousarray(boxes[1], np.float32)
+    rot = np.ascontiguousarray(boxes[2], np.float32).reshape(-1) if len(boxes) > 2 and boxes[2] is not None else None
+    b = OrBoxes(lo.shape[0], _p(lo, _f32p), _p(hi, _f32p), _p(rot, _f32p) if rot is not None else None)
+    return b, (lo, hi, rot)
 
 
 class OrIncompOut(C.Structure):
@@ -122,6 +131,7 @@ def lib() -> C.CDLL:
         L.or_morton.restype = C.c_uint32
         L.or_delete_edit_list.restype = C.c_uint32
         L.or_kernel_height.restype = C.c_double
+        L.or_emit.restype = C.c_uint32
         L.or_kernel_height.argtypes = [C.c_int, C.POINTER(C.c_double), C.c_double]
         L.or_kernel_gradient.argtypes = [C.c_int, C.POINTER(C.c_double), C.c_double, C.POINTER(C.c_double)]
         _lib = L
@@ -310,12 +320,28 @@ def incompressibility(fs: FluidState, settings: OrSettings, lambda_in: np.ndarra
     return out
 
 
-def box_collision(fs: FluidState, bmin: np.ndarray, bmax: np.ndarray) -> None:
-    lo = np.ascontiguousarray(bmin, np.float32)
-    hi = np.ascontiguousarray(bmax, np.float32)
-    b = OrBoxes(lo.shape[0], _p(lo, _f32p), _p(hi, _f32p))
-    fs._boxes_keep = (lo, hi)
+def box_collision(fs: FluidState, bmin: np.ndarray, bmax: np.ndarray, rot: np.ndarray | None = None) -> None:
+    """rot: None (axis-aligned boxes) or 12 floats per box (rotation rows; see OrBoxes)."""
+    b, keep = _boxes((bmin, bmax, rot))
+    fs._boxes_keep = keep
     lib().or_box_collision(C.byref(fs.f), C.byref(b))
+
+
+class OrEmitter(C.Structure):
+    _fields_ = [("origin", C.c_float * 3), ("radius", C.c_float), ("nx", C.c_uint32), ("nz", C.c_uint32),
+                ("speed", C.c_float), ("jitter", C.c_float), ("seed", C.c_uint32), ("max_particles", C.c_uint32),
+                ("enabled", C.c_uint32), ("pad", C.c_uint32)]
+
+
+def emit(fs: FluidState, emitter, state: np.ndarray, dt: float, last_dt: float) -> tuple[int, bool]:
+    """Appends the emitter's particles for one substep (the device's first stage);
+    `emitter` has the fields of apbf_emitter, `state` is a float64[2] the caller keeps."""
+    e = OrEmitter((C.c_float * 3)(*emitter.origin), emitter.radius, emitter.nx, emitter.nz, emitter.speed,
+                  emitter.jitter, emitter.seed, emitter.max_particles, emitter.enabled, 0)
+    ov = C.c_int(0)
+    k = lib().or_emit(C.byref(fs.f), C.byref(e), state.ctypes.data_as(C.POINTER(C.c_double)), C.c_float(dt),
+                      C.c_float(last_dt), C.byref(ov))
+    return int(k), bool(ov.value)
 
 
 def velocity_handling(fs: FluidState, dt: float, last_dt: float, accel) -> None:
@@ -353,9 +379,7 @@ def reduce(fs: FluidState) -> np.ndarray:
 def substep(fs: FluidState, scene: OrScene, boxes: tuple, dt: float, cap_pairs: int) -> int:
     if fs.nb is None or fs.nb.cap < cap_pairs:
         fs.alloc_neighbors(cap_pairs)
-    lo = np.ascontiguousarray(boxes[0], np.float32)
-    hi = np.ascontiguousarray(boxes[1], np.float32)
-    b = OrBoxes(lo.shape[0], _p(lo, _f32p), _p(hi, _f32p))
+    b, keep = _boxes(boxes)
     tot = lib().or_substep(C.byref(fs.f), C.byref(fs.t), C.byref(fs.nb), C.byref(b), C.byref(scene), C.c_float(dt))
     if tot > fs.nb.cap:
         raise RuntimeError(f"oracle neighbour capacity {fs.nb.cap} < {tot}")
