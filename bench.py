@@ -25,6 +25,7 @@ import sys
 import threading
 import time
 from pathlib import Path
+from types import SimpleNamespace
 
 import numpy as np
 
@@ -39,6 +40,8 @@ WORKLOADS = {
     "water_drop_250k": ("water_drop", dict(total=250_000, basic_pbf=False)),
     "water_drop_250k_plain": ("water_drop", dict(total=250_000, basic_pbf=True)),
     "dam_break_32k": ("dam_break", dict(n_side=32)),
+    # 384k particles pre-filled + 2000/substep from the emitter: ~1M after 300 substeps
+    "waterfall_1m": ("waterfall", dict(initial=384_000, basic_pbf=False)),
     # 64 independent scenes, log-uniform 4k-200k particles, one graph launch per substep
     "batch64": ("batch", dict(scenes=64, lo=4_000, hi=200_000)),
 }
@@ -54,6 +57,11 @@ def make_spec(name: str, seed: int = 0, scale: float = 1.0):
         kw["total"] = int(kw["total"] * scale)
     if factory == "dam_break":
         return scenes.dam_break(seed=seed, **kw)
+    if factory == "waterfall":
+        spec = scenes.waterfall(initial=int(kw["initial"] * scale), seed=seed, basic_pbf=kw["basic_pbf"],
+                                scale=scale ** (1.0 / 3.0), per_substep=int(round(2000 * scale ** (2.0 / 3.0))))
+        spec.meta["presteps"] = 300  # the emitter has brought the count to ~1M
+        return spec
     basic = kw.pop("basic_pbf")
     return scenes.water_drop(seed=seed, basic_pbf=basic, **kw)
 
@@ -161,23 +169,48 @@ def traffic_from_profiles(kernel: str, n: int, pairs: int) -> float | None:
 
 
 # ----------------------------------------------------------------------------- CPU baseline
+def oracle_boxes(spec) -> tuple:
+    """The scene's boxes for the oracle: axis-aligned ones plus the oriented ones with
+    their rotation rows computed as apbf_set_oriented_boxes computes them."""
+    if spec.meta.get("oriented_boxes") is None:
+        return (spec.box_min, spec.box_max)
+    c, h, q = spec.meta["oriented_boxes"]
+    rot = np.zeros((len(spec.box_min) + len(c), 3, 4), np.float32)
+    for k, qq in enumerate(np.asarray(q, np.float64)):
+        x, y, z, w = qq / np.linalg.norm(qq)
+        m = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y + z * w), 2 * (x * z - y * w)],
+                      [2 * (x * y - z * w), 1 - 2 * (x * x + z * z), 2 * (y * z + x * w)],
+                      [2 * (x * z + y * w), 2 * (y * z - x * w), 1 - 2 * (x * x + y * y)]])
+        rot[len(spec.box_min) + k, :, :3] = m.astype(np.float32)
+        rot[len(spec.box_min) + k, 0, 3] = 1.0
+    return (np.concatenate([spec.box_min, c]), np.concatenate([spec.box_max, h]), rot)
+
+
 def cpu_baseline(workload: str, budget_s: float = 15.0) -> dict:
     """The single-threaded FP64 oracle on a bounded sample: the same scene at 1/8 of
     the particle count (every length halved), substeps until the budget is spent."""
     from oracle import oracle as orc
 
     spec = make_spec(workload, scale=1.0 / 8.0)
-    fs = orc.FluidState(spec.state)
+    cap = max(spec.n, int(spec.meta.get("capacity", 0) // 8)) + 4096
+    fs = orc.FluidState(spec.state, cap=cap)
     sc = orc.make_scene(orc.settings_from(settings_dict(spec)), spec.grid_min, spec.grid_max, spec.log2res,
                         spec.acceleration)
-    steps, t0 = 0, time.perf_counter()
+    boxes = oracle_boxes(spec)
+    est = np.zeros(2, np.float64)
+    em = spec.meta.get("emitter")
+    steps, processed, t0 = 0, 0, time.perf_counter()
     while True:
-        orc.substep(fs, sc, (spec.box_min, spec.box_max), np.float32(spec.dt), int(spec.n * 64))
+        if em:
+            orc.emit(fs, SimpleNamespace(**em, max_particles=0, enabled=1), est, np.float32(spec.dt),
+                     np.float32(sc.last_dt))
+        orc.substep(fs, sc, boxes, np.float32(spec.dt), int(cap * 64))
         steps += 1
+        processed += fs.n
         if time.perf_counter() - t0 > budget_s or steps >= 20:
             break
     el = time.perf_counter() - t0
-    return {"value": spec.n * steps / el, "unit": UNIT, "cores": 1, "kind": "port",
+    return {"value": processed / el, "unit": UNIT, "cores": 1, "kind": "port",
             "sample": f"{steps} substep(s) from the start of the {spec.n}-particle (1/8 scale) version of the "
                       f"scene, reference Jacobi rule until {settings_dict(spec)['density_error_target']} "
                       f"(max {settings_dict(spec)['solver_iterations']} passes), single-threaded FP64 oracle, "
@@ -239,15 +272,13 @@ def run_reference(args) -> None:
 def _make_ctx(spec, args, local, mode: int = 0, net=None):
     from apbf_gb300.api import Context
 
-    cap = int(spec.n * 1.25) + 1024
-    ctx = Context(particle_capacity=cap, max_neighbors=args.max_neighbors, max_log2res=max(spec.log2res, 3),
-                  device=local)
+    cap = max(int(spec.n * 1.25) + 1024, int(spec.meta.get("capacity", 0) * 1.15))
+    maxn = args.max_neighbors if spec.basic_pbf else max(args.max_neighbors, 256)
+    ctx = Context(particle_capacity=cap, max_neighbors=maxn, max_log2res=max(spec.log2res, 3), device=local)
     # iterate every substep until the mean density error is at most the target
     ctx.set_settings(basic_pbf=1 if spec.basic_pbf else 0, solver_iterations=args.max_iterations,
                      density_error_target=args.error_target)
-    ctx.set_scene(spec.grid_min, spec.grid_max, spec.log2res, spec.acceleration)
-    ctx.set_boxes(spec.box_min, spec.box_max)
-    ctx.upload(spec.state)
+    ctx.load_scene(spec)
     ctx.set_solve_graph(args.graph_mode)
     if net is not None:
         ctx.mlp_load(net.params)
@@ -268,11 +299,13 @@ def train_warm_start(args, local: int, rank: int) -> tuple[object, dict]:
     seeds = [1000 + 10 * rank + k for k in (1, 2)]
     specs = [make_spec(args.workload, seed=s) for s in seeds]
     per = [sp.meta.get("presteps", 0) + 60 for sp in specs]
-    cap = sum(int(sp.n * 1.3) * ((p + 2) // 3 + 1) for sp, p in zip(specs, per))
+    every = 3 if max(sp.n for sp in specs) < 500_000 else 12  # bounds the sample count of growing scenes
+    grown = [max(sp.n, int(sp.meta.get("capacity", 0))) for sp in specs]
+    cap = min(sum(int(g * 1.3) * ((p + every - 1) // every + 1) for g, p in zip(grown, per)), 120_000_000)
     buf = SampleBuffer.allocate(cap, device=local)
     for sp, p in zip(specs, per):
         ctx = _make_ctx(sp, args, local, N.WARM_PROJECTED)
-        record_rollout(ctx, sp.dt, p, buf, iterations=args.max_iterations, every=3)
+        record_rollout(ctx, sp.dt, p, buf, iterations=args.max_iterations, every=every)
         ctx.check_status()
         ctx.close()
     torch.cuda.synchronize()
@@ -321,6 +354,7 @@ def run_arm(spec, args, local, mode: int, net, dist, headline: bool) -> tuple[di
     torch.cuda.synchronize()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    n_start, _ = ctx.lengths()
     ctx.check_status()  # clears the pass and convergence counters
     launches0 = ctx.launch_count()
     clocks = ClockSampler(local) if headline else None
@@ -363,7 +397,9 @@ def run_arm(spec, args, local, mode: int, net, dist, headline: bool) -> tuple[di
         ctx.profile_enable(False, 0)
         ctx.set_settings(solver_iterations=args.max_iterations, density_error_target=args.error_target)
         ctx.check_status()
-    r = {"ms_per_step": total_ms / args.steps, "value": spec.n * args.steps / (total_ms / 1000.0),
+    n_mean = 0.5 * (n_start + n_end)  # particles per timed substep (an emitter adds some every substep)
+    r = {"ms_per_step": total_ms / args.steps, "value": n_mean * args.steps / (total_ms / 1000.0),
+         "particles_before": int(n_start), "particles_mean": n_mean,
          "density_passes_per_substep": info.density_passes / args.steps,
          "converged_substeps": f"{info.converged_substeps}/{args.steps}", "pairs": int(info.pairs),
          "particles_after": int(n_end), "presteps": presteps, "total_ms": total_ms, "gpu_launches": int(launches),
@@ -403,6 +439,7 @@ def run_ours(args) -> None:
             plain[name] = {k: v for k, v in r.items() if not k.startswith("_")}
     head, ctx = run_arm(spec, args, local, head_mode, net, dist, headline=True)
     total_ms = head["total_ms"]
+    n = head["particles_mean"]  # particles per timed substep
     particles_processed = n * args.steps
     if dist:
         t = torch.tensor([total_ms, particles_processed], dtype=torch.float64, device=f"cuda:{local}")
@@ -421,13 +458,14 @@ def run_ours(args) -> None:
     if dom:
         name, (cnt, ms) = dom
         per_launch_s = ms / cnt / 1000.0
-        alg = algorithmic_bytes(name, n, head["pairs"])
+        n_prof = head["particles_after"]  # the traced substeps follow the timed ones
+        alg = algorithmic_bytes(name, n_prof, head["pairs"])
         peak, peak_kind = measured_peak()
         if alg:
             ach = alg / per_launch_s / 1e9
             roof = {"kernel": name, "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
                     "frac": ach / peak, "peak_source": peak_kind,
-                    "traffic": traffic_from_profiles(name, n, head["pairs"]),
+                    "traffic": traffic_from_profiles(name, n_prof, head["pairs"]),
                     "algorithmic_bytes": alg, "launch_us": per_launch_s * 1e6}
     kernel_share = {k: round(v[1] / max(sum(x[1] for x in prof.values()), 1e-9), 4) for k, v in prof.items()}
 
@@ -446,7 +484,8 @@ def run_ours(args) -> None:
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 (int32 fixed-point positions and sums; bf16 MLP)",
             "data": "synthetic (seeded scene generator)",
-            "config": {"workload": args.workload, "particles": n, "particles_after": head["particles_after"],
+            "config": {"workload": args.workload, "particles": n, "particles_before": head["particles_before"],
+                       "particles_after": head["particles_after"],
                        "solver": solver,
                        "iterations": f"until mean density error <= {args.error_target} (max {args.max_iterations})",
                        "density_passes_per_substep": head["density_passes_per_substep"],
