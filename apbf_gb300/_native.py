@@ -142,7 +142,8 @@ class Emitter(C.Structure):
 
 
 class Tuning(C.Structure):
-    _fields_ = [("gather_lanes", C.c_uint32), ("reserved0", C.c_uint32), ("reserved", C.c_uint32 * 6)]
+    _fields_ = [("gather_lanes", C.c_uint32), ("pass_block", C.c_uint32), ("pass_blocks_per_sm", C.c_uint32),
+                ("reserved", C.c_uint32 * 5)]
 
 
 class KernelTime(C.Structure):

@@ -169,22 +169,31 @@ class Context:
     def tuning(self) -> dict:
         t = N.Tuning()
         N.check(self.lib.apbf_get_tuning(self.handle, C.byref(t)), "apbf_get_tuning")
-        return {"gather_lanes": t.gather_lanes}
+        return {"gather_lanes": t.gather_lanes, "pass_block": t.pass_block,
+                "pass_blocks_per_sm": t.pass_blocks_per_sm}
 
-    def set_tuning(self, gather_lanes: int) -> None:
+    def set_tuning(self, gather_lanes: int | None = None, pass_block: int | None = None,
+                   pass_blocks_per_sm: int | None = None) -> None:
         t = N.Tuning()
         N.check(self.lib.apbf_get_tuning(self.handle, C.byref(t)), "apbf_get_tuning")
-        t.gather_lanes = gather_lanes
+        if gather_lanes is not None:
+            t.gather_lanes = gather_lanes
+        if pass_block is not None:
+            t.pass_block = pass_block
+        if pass_blocks_per_sm is not None:
+            t.pass_blocks_per_sm = pass_blocks_per_sm
         N.check(self.lib.apbf_set_tuning(self.handle, C.byref(t)), "apbf_set_tuning")
 
     def autotune(self, stream=None) -> dict:
         """Times every launch-shape candidate on the current state (restored afterwards)
         and keeps the fastest; returns the choice and the per-pass times (ms)."""
         t = N.Tuning()
-        ms = (C.c_float * 4)()
+        ms = (C.c_float * 24)()
         N.check(self.lib.apbf_autotune(self.handle, _stream_handle(stream), C.byref(t), ms), "apbf_autotune")
-        return {"gather_lanes": t.gather_lanes,
-                "pass_ms": {str(l): round(float(v), 5) for l, v in zip((1, 2, 4, 8), ms)}}
+        keys = [f"L{l}/B{b}/S{p}" for l in (1, 2, 4, 8) for b in (128, 256) for p in (2, 4, 8)]
+        return {"gather_lanes": t.gather_lanes, "pass_block": t.pass_block,
+                "pass_blocks_per_sm": t.pass_blocks_per_sm,
+                "pass_ms": {k: round(float(v), 5) for k, v in zip(keys, ms)}}
 
     def set_solve_graph(self, mode: int | bool) -> None:
         """0: per-kernel launches; 1 (default): the Jacobi passes 1.. as one graph launch with a

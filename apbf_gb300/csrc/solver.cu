@@ -77,18 +77,19 @@ __device__ __forceinline__ void pair_terms(int hk, int gk, float3 d, float kw, K
 }
 
 // Fixed-order (deterministic) sum of per-block partial pairs with one block of
-// 256 threads: thread t sums partials t, t+256, ... in order, then a fixed tree.
+// blockDim.x (a power of two, at most 256) threads: thread t sums partials t,
+// t + blockDim.x, ... in order, then a fixed tree.
 __device__ __forceinline__ void block_sum2(const double *partials, int blocks, double &t1, double &t2) {
     __shared__ double s1[256], s2[256];
     double a = 0.0, b = 0.0;
-    for (int k = threadIdx.x; k < blocks; k += 256) {
+    for (int k = threadIdx.x; k < blocks; k += blockDim.x) {
         a += ((volatile const double *)partials)[2 * k];
         b += ((volatile const double *)partials)[2 * k + 1];
     }
     s1[threadIdx.x] = a;
     s2[threadIdx.x] = b;
     __syncthreads();
-    for (int off = 128; off > 0; off >>= 1) {
+    for (int off = blockDim.x / 2; off > 0; off >>= 1) {
         if ((int)threadIdx.x < off) {
             s1[threadIdx.x] += s1[threadIdx.x + off];
             s2[threadIdx.x] += s2[threadIdx.x + off];
@@ -562,13 +563,17 @@ apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s, const SolveOpts &o)
     a.b_up_factor = st.boundariness_underpressure_factor;
     const int g = ctx->red_blocks;
     const int lanes = ctx->tuning.gather_lanes;
+    const int pb = ctx->tuning.pass_block == 128 ? 128 : 256;
+    const int bps = (int)std::min(8u, std::max(1u, ctx->tuning.pass_blocks_per_sm));
+    // the error reduction has one partial per block: at most red_blocks blocks
+    const int ga = std::min(g, grid_for(ctx, (uint32_t)std::min<uint64_t>((uint64_t)cap * lanes, 0xffffffffu), pb, bps));
     APBF_BEFORE_LAUNCH(ctx, s, "k_density_lambda");
     launch_lanes(lanes, [&](auto lc) {
         constexpr int Lc = decltype(lc)::value;
         if (gauss)
-            k_density_lambda<true, Lc><<<g, kBlock, 0, s>>>(a);
+            k_density_lambda<true, Lc><<<ga, pb, 0, s>>>(a);
         else
-            k_density_lambda<false, Lc><<<g, kBlock, 0, s>>>(a);
+            k_density_lambda<false, Lc><<<ga, pb, 0, s>>>(a);
     });
     APBF_AFTER_LAUNCH(ctx, s, "k_density_lambda");
 
@@ -602,13 +607,13 @@ apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s, const SolveOpts &o)
     b.loop_offset = o.loop_offset;
     b.max_passes = o.max_passes;
     APBF_BEFORE_LAUNCH(ctx, s, "k_delta");
-    const int gd = grid_for(ctx, (uint32_t)std::min<uint64_t>((uint64_t)cap * lanes, 0xffffffffu));
+    const int gd = grid_for(ctx, (uint32_t)std::min<uint64_t>((uint64_t)cap * lanes, 0xffffffffu), pb, bps);
     launch_lanes(lanes, [&](auto lc) {
         constexpr int Lc = decltype(lc)::value;
         if (gauss)
-            k_delta<true, Lc><<<gd, kBlock, 0, s>>>(b);
+            k_delta<true, Lc><<<gd, pb, 0, s>>>(b);
         else
-            k_delta<false, Lc><<<gd, kBlock, 0, s>>>(b);
+            k_delta<false, Lc><<<gd, pb, 0, s>>>(b);
     });
     APBF_AFTER_LAUNCH(ctx, s, "k_delta");
     // the updated positions now live in the alternate buffer: swap position buffers

@@ -10,8 +10,8 @@
 
 namespace apbf {
 
-static apbf_status time_lanes(apbf_ctx *ctx, cudaStream_t s, int lanes, int reps, float *ms_out) {
-    ctx->tuning.gather_lanes = (uint32_t)lanes;
+static apbf_status time_shape(apbf_ctx *ctx, cudaStream_t s, const apbf_tuning &t, int reps, float *ms_out) {
+    ctx->tuning = t;
     SolveOpts o;  // plain pass: no early stop, no features, no lambda bookkeeping
     for (int k = 0; k < 2; ++k) {  // warm-up (one pair keeps the buffer roles)
         apbf_status r = incompressibility(ctx, s, o);
@@ -42,8 +42,9 @@ using namespace apbf;
 extern "C" apbf_status apbf_set_tuning(apbf_ctx *ctx, const apbf_tuning *t) {
     if (!ctx || !t) return APBF_ERR_INVALID_ARG;
     const uint32_t l = t->gather_lanes;
-    if (l != 1 && l != 2 && l != 4 && l != 8) {
-        set_error("apbf_set_tuning: gather_lanes must be 1, 2, 4 or 8");
+    if ((l != 1 && l != 2 && l != 4 && l != 8) || (t->pass_block != 128 && t->pass_block != 256) ||
+        t->pass_blocks_per_sm < 1 || t->pass_blocks_per_sm > 8) {
+        set_error("apbf_set_tuning: gather_lanes 1, 2, 4 or 8; pass_block 128 or 256; pass_blocks_per_sm 1..8");
         return APBF_ERR_INVALID_ARG;
     }
     ctx->tuning = *t;
@@ -83,11 +84,17 @@ extern "C" apbf_status apbf_autotune(apbf_ctx *ctx, void *stream, apbf_tuning *c
     const bool prof = ctx->prof_on;
     ctx->prof_on = false;
     const apbf_tuning before = ctx->tuning;
-    const int cands[4] = {1, 2, 4, 8};
-    float best_ms = 0.0f, times[4] = {0, 0, 0, 0};
+    const int lanes[4] = {1, 2, 4, 8}, blocks[2] = {128, 256}, per_sm[3] = {2, 4, 8};
+    constexpr int kCands = 24;
+    float best_ms = 0.0f, times[kCands] = {};
+    apbf_tuning best_t = before;
     int best = -1;
-    for (int c = 0; c < 4 && r == APBF_OK; ++c) {
-        r = time_lanes(ctx, s, cands[c], 4, &times[c]);
+    for (int c = 0; c < kCands && r == APBF_OK; ++c) {
+        apbf_tuning t = before;
+        t.gather_lanes = (uint32_t)lanes[c / 6];
+        t.pass_block = (uint32_t)blocks[(c / 3) % 2];
+        t.pass_blocks_per_sm = (uint32_t)per_sm[c % 3];
+        r = time_shape(ctx, s, t, 4, &times[c]);
         // restore the positions after every candidate (pairs of passes keep the roles)
         if (f.pos != pos_cur) r = r == APBF_OK ? APBF_ERR_CUDA : r;
         cudaMemcpyAsync(pos_cur, pos_save, cap * sizeof(int4), cudaMemcpyDeviceToDevice, s);
@@ -95,6 +102,7 @@ extern "C" apbf_status apbf_autotune(apbf_ctx *ctx, void *stream, apbf_tuning *c
         if (r == APBF_OK && (best < 0 || times[c] < best_ms)) {
             best = c;
             best_ms = times[c];
+            best_t = t;
         }
     }
     cudaMemcpyAsync(ctx->status, st_save, sizeof(Status), cudaMemcpyDeviceToDevice, s);
@@ -107,10 +115,10 @@ extern "C" apbf_status apbf_autotune(apbf_ctx *ctx, void *stream, apbf_tuning *c
         ctx->tuning = before;
         return r;
     }
-    ctx->tuning.gather_lanes = (uint32_t)cands[best];
+    ctx->tuning = best_t;
     ctx->graph_version++;
     if (chosen) *chosen = ctx->tuning;
     if (pass_ms)
-        for (int c = 0; c < 4; ++c) pass_ms[c] = times[c];
+        for (int c = 0; c < kCands; ++c) pass_ms[c] = times[c];
     return APBF_OK;
 }

@@ -165,9 +165,10 @@ typedef struct apbf_status_info {
  * reference's workgroup sizes are fixed in its shaders).  Results do not depend
  * on them. */
 typedef struct apbf_tuning {
-    uint32_t gather_lanes;   /* threads per particle in the density and position passes: 1, 2, 4 or 8 */
-    uint32_t reserved0;
-    uint32_t reserved[6];
+    uint32_t gather_lanes;        /* threads per particle in the density and position passes: 1, 2, 4 or 8 */
+    uint32_t pass_block;          /* threads per block of those passes: 128 or 256 */
+    uint32_t pass_blocks_per_sm;  /* their grid: up to this many blocks per SM (1..8) */
+    uint32_t reserved[5];
 } apbf_tuning;
 
 typedef struct apbf_ctx apbf_ctx;
@@ -288,10 +289,11 @@ apbf_status apbf_batch_substep(apbf_batch *batch, float dt, void *stream);
 apbf_status apbf_batch_destroy(apbf_batch *batch);
 
 /* Launch shapes (no counterpart in the reference).  apbf_autotune times every
- * gather_lanes candidate on the context's current particle state and neighbour
- * rows (call it after a substep or a neighbourhood search), keeps the fastest and
- * restores the state it ran on; pass_ms (may be NULL) receives the time of one
- * Jacobi pass for gather_lanes 1, 2, 4, 8. */
+ * candidate shape of the Jacobi passes on the context's current particle state and
+ * neighbour rows (call it after a substep or a neighbourhood search), keeps the
+ * fastest and restores the state it ran on; pass_ms (may be NULL) receives the
+ * time of one pass for each of the 24 candidates, in the order gather_lanes
+ * (1, 2, 4, 8) x pass_block (128, 256) x pass_blocks_per_sm (2, 4, 8). */
 apbf_status apbf_set_tuning(apbf_ctx *ctx, const apbf_tuning *t);
 apbf_status apbf_get_tuning(apbf_ctx *ctx, apbf_tuning *t);
 apbf_status apbf_autotune(apbf_ctx *ctx, void *stream, apbf_tuning *chosen, float *pass_ms);

@@ -27,10 +27,10 @@ def test_gather_lanes_bit_identical(name):
     else:
         spec, maxn = scenes.water_drop(total=20_000, seed=2, basic_pbf=False), 256
     results = []
-    for lanes in (1, 2, 4, 8):
+    for lanes, block, per_sm in ((1, 256, 8), (2, 256, 8), (4, 128, 2), (8, 256, 4), (1, 128, 4), (2, 128, 8)):
         ctx = _ctx(spec, 5, maxn=maxn)
-        ctx.set_tuning(gather_lanes=lanes)
-        assert ctx.tuning()["gather_lanes"] == lanes
+        ctx.set_tuning(gather_lanes=lanes, pass_block=block, pass_blocks_per_sm=per_sm)
+        assert ctx.tuning() == {"gather_lanes": lanes, "pass_block": block, "pass_blocks_per_sm": per_sm}
         for _ in range(8):
             ctx.substep(spec.dt)
         ctx.check_status()
@@ -49,9 +49,9 @@ def test_autotune_keeps_state():
     ctx.check_status()
     before, _ = ctx.download()
     res = ctx.autotune()
-    assert res["gather_lanes"] in (1, 2, 4, 8)
-    assert all(v > 0 for v in res["pass_ms"].values())
-    assert ctx.tuning()["gather_lanes"] == res["gather_lanes"]
+    assert res["gather_lanes"] in (1, 2, 4, 8) and res["pass_block"] in (128, 256)
+    assert len(res["pass_ms"]) == 24 and all(v > 0 for v in res["pass_ms"].values())
+    assert ctx.tuning() == {k: res[k] for k in ("gather_lanes", "pass_block", "pass_blocks_per_sm")}
     after, _ = ctx.download()
     for k in before:
         assert np.array_equal(before[k], after[k]), k
@@ -72,11 +72,12 @@ def test_autotune_keeps_state():
     ref.close()
 
 
-def test_set_tuning_rejects_bad_lanes():
+def test_set_tuning_rejects_bad_shapes():
     from apbf_gb300._native import ApbfError
 
     spec = scenes.dam_break(n_side=8)
     ctx = _ctx(spec, 2)
-    with pytest.raises(ApbfError):
-        ctx.set_tuning(gather_lanes=3)
+    for bad in (dict(gather_lanes=3), dict(pass_block=192), dict(pass_blocks_per_sm=0), dict(pass_blocks_per_sm=9)):
+        with pytest.raises(ApbfError):
+            ctx.set_tuning(**bad)
     ctx.close()
