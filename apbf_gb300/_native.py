@@ -143,7 +143,7 @@ class Emitter(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("gather_lanes", C.c_uint32), ("pass_block", C.c_uint32), ("pass_blocks_per_sm", C.c_uint32),
-                ("reserved", C.c_uint32 * 5)]
+                ("build_tiled", C.c_uint32), ("filter_in_density", C.c_uint32), ("reserved", C.c_uint32 * 3)]
 
 
 class KernelTime(C.Structure):

@@ -170,10 +170,12 @@ class Context:
         t = N.Tuning()
         N.check(self.lib.apbf_get_tuning(self.handle, C.byref(t)), "apbf_get_tuning")
         return {"gather_lanes": t.gather_lanes, "pass_block": t.pass_block,
-                "pass_blocks_per_sm": t.pass_blocks_per_sm}
+                "pass_blocks_per_sm": t.pass_blocks_per_sm, "build_tiled": t.build_tiled,
+                "filter_in_density": t.filter_in_density}
 
     def set_tuning(self, gather_lanes: int | None = None, pass_block: int | None = None,
-                   pass_blocks_per_sm: int | None = None) -> None:
+                   pass_blocks_per_sm: int | None = None, build_tiled: int | None = None,
+                   filter_in_density: int | None = None) -> None:
         t = N.Tuning()
         N.check(self.lib.apbf_get_tuning(self.handle, C.byref(t)), "apbf_get_tuning")
         if gather_lanes is not None:
@@ -182,6 +184,10 @@ class Context:
             t.pass_block = pass_block
         if pass_blocks_per_sm is not None:
             t.pass_blocks_per_sm = pass_blocks_per_sm
+        if build_tiled is not None:
+            t.build_tiled = build_tiled
+        if filter_in_density is not None:
+            t.filter_in_density = filter_in_density
         N.check(self.lib.apbf_set_tuning(self.handle, C.byref(t)), "apbf_set_tuning")
 
     def autotune(self, stream=None) -> dict:
@@ -192,7 +198,8 @@ class Context:
         N.check(self.lib.apbf_autotune(self.handle, _stream_handle(stream), C.byref(t), ms), "apbf_autotune")
         keys = [f"L{l}/B{b}/S{p}" for l in (1, 2, 4, 8) for b in (128, 256) for p in (2, 4, 8)]
         return {"gather_lanes": t.gather_lanes, "pass_block": t.pass_block,
-                "pass_blocks_per_sm": t.pass_blocks_per_sm,
+                "pass_blocks_per_sm": t.pass_blocks_per_sm, "build_tiled": t.build_tiled,
+                "filter_in_density": t.filter_in_density,
                 "pass_ms": {k: round(float(v), 5) for k, v in zip(keys, ms)}}
 
     def set_solve_graph(self, mode: int | bool) -> None:

@@ -65,6 +65,8 @@ struct Status {
     uint32_t converged_substeps;   // substeps in which a density pass met the target
     uint32_t pass_index;           // solve loop graph: index of the first pass of the current body run
     uint32_t loop_iters;           // solve loop graph: body runs since the context was created
+    uint32_t filter_tag;           // 1: this pass's density kernel left the boundariness filter to k_delta
+    uint32_t pad2[3];
 };
 
 // Device length block.
@@ -173,6 +175,7 @@ struct apbf_ctx {
     float *lambda = nullptr;
     int4 *shift = nullptr;
     float4 *solve_rec = nullptr;   // per particle: lambda, Gauss constants (ivd, norm), kernel width
+    int4 *filt = nullptr;          // per particle: gradient sum and boundariness > 0, for the deferred filter
     // learned warm start
     float *mlp_params = nullptr;   // FP32 parameter vector (mlp.cu)
     float *features = nullptr;     // per particle: 8 features of the first density pass
@@ -234,7 +237,7 @@ struct apbf_ctx {
     apbf::ProfSlot *prof_open = nullptr;
     bool capturing = false;        // launches go into a graph being built: not counted
 
-    apbf_tuning tuning = {1u, 256u, 8u, {0u, 0u, 0u, 0u, 0u}};  // launch shapes (apbf_set_tuning / apbf_autotune)
+    apbf_tuning tuning = {1u, 256u, 8u, 0u, 0u, {0u, 0u, 0u}};  // launch shapes (apbf_set_tuning / apbf_autotune)
 
     // solve loop graphs (graph.cu)
     int use_graphs = 1;

@@ -164,6 +164,7 @@ apbf_status apbf_create(const apbf_config *cfg, apbf_ctx **out) {
     A(ctx->lambda, cap);
     A(ctx->shift, cap);
     A(ctx->solve_rec, cap);
+    A(ctx->filt, cap);
     A(ctx->mlp_params, kMlpParams);
     A(ctx->features, (size_t)cap * 8);
     A(ctx->selfdir, cap);

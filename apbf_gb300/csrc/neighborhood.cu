@@ -250,6 +250,181 @@ __global__ void __launch_bounds__(256, 3) k_build_rows(BuildArgs a) {
     }
 }
 
+// The same rows as k_build_rows, built by blocks of kTileP consecutive (Morton-
+// sorted) particles that stage their candidates in shared memory: the block takes
+// the union of its particles' cell boxes (at most kTileCells cells), loads the
+// particles of those cells kTileBuf at a time with coalesced reads, and every
+// thread tests its particle against each staged candidate whose cell lies in the
+// particle's own box.  Candidates come in (z, y, x) cell order and index order
+// within a cell, the order of walk_cells, so the rows are identical.  A block whose
+// union is larger (a jump of the Morton curve inside the block) walks per thread.
+constexpr int kTileP = 64;
+constexpr int kTileCells = 216;
+constexpr int kTileBuf = 512;
+
+__global__ void __launch_bounds__(kTileP) k_build_rows_tiled(BuildArgs a) {
+    __shared__ int4 s_pos[kTileBuf];
+    __shared__ uint32_t s_idx[kTileBuf];
+    __shared__ uint16_t s_cell[kTileBuf];        // region-relative cell of the candidate: x | y << 5 | z << 10
+    __shared__ uint32_t s_start[kTileCells];
+    __shared__ uint32_t s_pre[kTileCells + 1];  // exclusive prefix of the cells' particle counts
+    __shared__ int s_box[6];
+    const uint32_t n = a.d_len[kLenParticles];
+    const uint32_t last = (1u << a.L) - 1u;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned long long local = 0;
+    long long rmin = 0x7fffffffffffffffll, rmax = -1;
+    for (uint32_t base = blockIdx.x * kTileP; base < n; base += gridDim.x * kTileP) {
+        const uint32_t i = base + threadIdx.x;
+        const bool valid = i < n;
+        int4 p = make_int4(0, 0, 0, 0);
+        long long R = -1;
+        uint32_t x0 = 1, x1 = 0, y0 = 1, y1 = 0, z0 = 1, z1 = 0;
+        if (valid) {
+            p = a.pos[i];
+            R = range_fixed(a.range[i], a.scale);
+            if (R < 0) {
+                set_flag(a.st, APBF_FLAG_NONFINITE);
+            } else {
+                rmin = R < rmin ? R : rmin;
+                rmax = R > rmax ? R : rmax;
+                const Bounds &b = a.b;
+                x0 = cell_coord((long long)p.x - R, b.lo[0], b.hi[0], a.L);
+                x1 = cell_coord((long long)p.x + R, b.lo[0], b.hi[0], a.L);
+                y0 = cell_coord((long long)p.y - R, b.lo[1], b.hi[1], a.L);
+                y1 = cell_coord((long long)p.y + R, b.lo[1], b.hi[1], a.L);
+                z0 = cell_coord((long long)p.z - R, b.lo[2], b.hi[2], a.L);
+                z1 = cell_coord((long long)p.z + R, b.lo[2], b.hi[2], a.L);
+            }
+        }
+        const bool has = valid && R >= 0;
+        if (threadIdx.x == 0) {
+            s_box[0] = s_box[2] = s_box[4] = 0x7fffffff;
+            s_box[1] = s_box[3] = s_box[5] = -1;
+        }
+        __syncthreads();
+        if (has) {
+            atomicMin(&s_box[0], (int)x0);
+            atomicMax(&s_box[1], (int)x1);
+            atomicMin(&s_box[2], (int)y0);
+            atomicMax(&s_box[3], (int)y1);
+            atomicMin(&s_box[4], (int)z0);
+            atomicMax(&s_box[5], (int)z1);
+        }
+        __syncthreads();
+        const int bx0 = s_box[0], by0 = s_box[2], bz0 = s_box[4];
+        const int nx = s_box[1] - bx0 + 1, ny = s_box[3] - by0 + 1, nz = s_box[5] - bz0 + 1;
+        const bool fast = has && a.fast_ok && x0 > 0 && y0 > 0 && z0 > 0 && x1 < last && y1 < last && z1 < last;
+        uint32_t c = 0;
+        if (s_box[1] < 0) {
+            // no particle of the block searches
+        } else if ((long long)nx * ny * nz > kTileCells || nx > 31 || ny > 31 || nz > 31) {
+            if (has) {
+                c = fast ? walk_cells<true>(i, p, R, x0, x1, y0, y1, z0, z1, a.pos, a.cstart, a.cend, a.stride,
+                                            a.maxn, a.idx)
+                         : walk_cells<false>(i, p, R, x0, x1, y0, y1, z0, z1, a.pos, a.cstart, a.cend, a.stride,
+                                             a.maxn, a.idx);
+            }
+        } else {
+            const int cells = nx * ny * nz;
+            // cell ranges of the region in (z, y, x) order
+            for (int k = threadIdx.x; k < cells; k += kTileP) {
+                const uint32_t cx = bx0 + k % nx, cy = by0 + (k / nx) % ny, cz = bz0 + k / (nx * ny);
+                const uint32_t key = spread3(cx) | (spread3(cy) << 1) | (spread3(cz) << 2);
+                const uint32_t cs = a.cstart[key], ce = a.cend[key];
+                s_start[k] = cs;
+                s_pre[k + 1] = ce - cs;
+            }
+            __syncthreads();
+            if (warp == 0) {  // exclusive prefix over the cells: 7 per lane, then a warp scan
+                uint32_t v[7], sum = 0;
+#pragma unroll
+                for (int t = 0; t < 7; ++t) {
+                    const int k = lane * 7 + t;
+                    v[t] = k < cells ? s_pre[k + 1] : 0u;
+                    sum += v[t];
+                }
+                uint32_t incl = sum;
+#pragma unroll
+                for (int off = 1; off < 32; off <<= 1) {
+                    const uint32_t o = __shfl_up_sync(0xffffffffu, incl, off);
+                    if (lane >= off) incl += o;
+                }
+                uint32_t run = incl - sum;
+#pragma unroll
+                for (int t = 0; t < 7; ++t) {
+                    const int k = lane * 7 + t;
+                    if (k < cells) s_pre[k] = run;
+                    run += v[t];
+                }
+                if (lane == 31) s_pre[cells] = incl;
+            }
+            __syncthreads();
+            const uint32_t total = s_pre[cells];
+            // this particle's own box relative to the region
+            const int ox0 = (int)x0 - bx0, ox1 = (int)x1 - bx0, oy0 = (int)y0 - by0, oy1 = (int)y1 - by0,
+                      oz0 = (int)z0 - bz0, oz1 = (int)z1 - bz0;
+            const uint32_t R32 = (uint32_t)R;
+            const unsigned long long R2 = (unsigned long long)R32 * R32;
+            for (uint32_t b0 = 0; b0 < total; b0 += kTileBuf) {
+                const uint32_t m = total - b0 < (uint32_t)kTileBuf ? total - b0 : (uint32_t)kTileBuf;
+                for (uint32_t k = threadIdx.x; k < m; k += kTileP) {
+                    const uint32_t g = b0 + k;
+                    int lo = 0, hi = cells;  // largest cell with s_pre[cell] <= g
+                    while (hi - lo > 1) {
+                        const int mid = (lo + hi) >> 1;
+                        if (s_pre[mid] <= g) lo = mid;
+                        else hi = mid;
+                    }
+                    const uint32_t j = s_start[lo] + (g - s_pre[lo]);
+                    s_pos[k] = a.pos[j];
+                    s_idx[k] = j;
+                    s_cell[k] = (uint16_t)((lo % nx) | (((lo / nx) % ny) << 5) | ((lo / (nx * ny)) << 10));
+                }
+                __syncthreads();
+                if (has) {
+                    for (uint32_t k = 0; k < m; ++k) {
+                        const uint32_t rc = s_cell[k];
+                        const int rx = rc & 31, ry = (rc >> 5) & 31, rz = rc >> 10;
+                        if (rx < ox0 || rx > ox1 || ry < oy0 || ry > oy1 || rz < oz0 || rz > oz1) continue;
+                        const uint32_t j = s_idx[k];
+                        if (j == i) continue;
+                        const int4 q = s_pos[k];
+                        if (fast ? !within32(p, q, R32, R2) : !within(p, q, R)) continue;
+                        if (c < a.maxn) a.idx[(size_t)c * a.stride + i] = j;
+                        ++c;
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        if (valid) {
+            if (c > a.maxn) {
+                set_flag(a.st, APBF_FLAG_NEIGHBOR_OVERFLOW);
+                atomicMax(&a.st->required_neighbors, c);
+            }
+            a.count[i] = c < a.maxn ? c : a.maxn;
+            local += c < a.maxn ? c : a.maxn;
+            if (a.pos_box) a.pos_box[i] = box_push(p, a.radius[i], i, a.bmin, a.bmax, a.rot, a.nboxes);
+        }
+        __syncthreads();  // s_box is reused by the next chunk
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        local += __shfl_down_sync(0xffffffffu, local, off);
+        long long a2 = __shfl_down_sync(0xffffffffu, rmin, off);
+        long long c2 = __shfl_down_sync(0xffffffffu, rmax, off);
+        rmin = a2 < rmin ? a2 : rmin;
+        rmax = c2 > rmax ? c2 : rmax;
+    }
+    if (lane == 0) {
+        if (local) atomicAdd(a.total, local);
+        if (rmax >= 0) {
+            atomicMin(&a.st->range_min, (unsigned long long)rmin);
+            atomicMax(&a.st->range_max, (unsigned long long)rmax);
+        }
+    }
+}
+
 __global__ void k_reverse_rows(const uint32_t *d_len, uint32_t stride, uint32_t maxn, const uint32_t *__restrict__ count,
                                const uint32_t *__restrict__ idx, uint32_t *__restrict__ rcount,
                                uint32_t *__restrict__ ridx, Status *st) {
@@ -367,7 +542,10 @@ apbf_status neighborhood_green(apbf_ctx *ctx, float range_scale, const float min
     ba.idx = ctx->nb_idx;
     ba.total = ctx->d_pairs;
     ba.st = ctx->status;
-    k_build_rows<<<grid_for(ctx, cap, kBlock, 8), kBlock, 0, s>>>(ba);
+    if (ctx->tuning.build_tiled)
+        k_build_rows_tiled<<<grid_for(ctx, cap, kTileP, 24), kTileP, 0, s>>>(ba);
+    else
+        k_build_rows<<<grid_for(ctx, cap, kBlock, 8), kBlock, 0, s>>>(ba);
     APBF_AFTER_LAUNCH(ctx, s, "k_build_rows");
     if (fuse_box) {  // the box-collided positions are the current ones now
         int4 *t = f.pos;

@@ -30,6 +30,24 @@ __device__ __forceinline__ float dot3x(float3 a, float3 b) {
     return __fadd_rn(__fadd_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)), __fmul_rn(a.z, b.z));
 }
 
+// The boundariness filter of incompressibility_3.comp:41-46,60 for the Gauss
+// kernel, whose gradient points along -d: the pair (i, j) at offset d = x_j - x_i
+// clears a non-zero boundariness of i when -normalize(gradW) . ed > 0.6 with
+// ed = -normalize(gradient sum of i).  Explicit rounding: the density pass and the
+// position pass (which takes the test over when rows are symmetric) must agree.
+__device__ __forceinline__ bool filter_dir(int32_t gx, int32_t gy, int32_t gz, float3 &ed) {
+    const float3 gi = make_float3((float)gx, (float)gy, (float)gz);
+    const float gl = __fsqrt_rn(dot3x(gi, gi));
+    if (!(gl > 0.0f)) return false;
+    ed = make_float3(-__fdiv_rn(gi.x, gl), -__fdiv_rn(gi.y, gl), -__fdiv_rn(gi.z, gl));
+    return true;
+}
+__device__ __forceinline__ bool gauss_filter_hit(float3 ed, float3 d) {
+    const float r2 = dot3x(d, d);
+    if (r2 < 1.0e-8f) return false;  // zero gradient: normalize() gives NaN, no filter
+    return -dot3x(ed, d) > __fmul_rn(0.6f, __fsqrt_rn(r2));
+}
+
 struct PassA {
     const int4 *pos;
     const float *inv_mass;
@@ -56,6 +74,7 @@ struct PassA {
     int projected;          // 1: pull-back allowed (passes after the first of a warm-started substep)
     int loop_offset;        // >= 0: solve loop pass number = st->pass_index + loop_offset
     uint32_t max_passes;    // loop passes from this number on are skipped
+    int4 *filt;             // non-null: Gauss filter deferred to the position pass when rows are symmetric
     float target;        // > 0: set st->converged when the error is at most this
     int early_exit;      // skip the pass when st->converged is set
     float rmin3;  // pow(2 * smallestTargetRadius, 3)
@@ -121,8 +140,13 @@ __device__ __forceinline__ int32_t group_wsum(int32_t v) {
 
 template <bool GAUSS, int L>
 __global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) {
-    if (a.early_exit && *(volatile uint32_t *)&a.st->converged) return;  // uniform over the grid
-    if (a.loop_offset >= 0 && a.st->pass_index + (uint32_t)a.loop_offset >= a.max_passes) return;
+    const bool skip = (a.early_exit && *(volatile uint32_t *)&a.st->converged) ||
+                      (a.loop_offset >= 0 && a.st->pass_index + (uint32_t)a.loop_offset >= a.max_passes);
+    // With symmetric rows the Gauss filter runs in this pass's position update, which
+    // gathers over the same neighbours anyway; filter_tag tells it whether to.
+    const bool defer = GAUSS && a.filt && a.method == 2 && a.st->range_min == a.st->range_max;
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.st->filter_tag = (!skip && defer) ? 1u : 0u;
+    if (skip) return;  // uniform over the grid
     const uint32_t n = a.d_len[kLenParticles];
     const uint32_t sub = threadIdx.x % L, gpb = blockDim.x / L;
     double e1 = 0.0, e2 = 0.0;
@@ -265,19 +289,16 @@ __global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) 
         }
         a.shift[i] = sh;
         // incompressibility_3.comp:41-46,60: filter (only changes a non-zero boundariness)
-        if (a.method == 2 && b > 0.0f) {
-            float3 gi = make_float3((float)gx, (float)gy, (float)gz);
-            float gl = sqrtf(dot3x(gi, gi));
-            if (gl > 0.0f) {
-                float3 ed = make_float3(-gi.x / gl, -gi.y / gl, -gi.z / gl);
+        if (defer) {
+            a.filt[i] = make_int4(gx, gy, gz, b > 0.0f ? 1 : 0);
+        } else if (a.method == 2 && b > 0.0f) {
+            float3 ed;
+            if (filter_dir(gx, gy, gz, ed)) {
                 for (uint32_t k = 0; k < cnt; ++k) {
                     const uint32_t j = a.idx[(size_t)k * a.stride + i];
                     const float3 d = fdiff(p, a.pos[j]);
                     if (GAUSS) {
-                        // the Gauss gradient points along -d: normalize(gradW) = -d / |d|
-                        const float r2 = dot3x(d, d);
-                        if (r2 < 1.0e-8f) continue;  // zero gradient: normalize() gives NaN, no filter
-                        if (-(ed.x * d.x + ed.y * d.y + ed.z * d.z) > 0.6f * sqrtf(r2)) {
+                        if (gauss_filter_hit(ed, d)) {
                             b = 0.0f;
                             break;
                         }
@@ -372,6 +393,8 @@ struct PassB {
     int prev_mode, acc_mode;
     int loop_offset;      // >= 0: solve loop pass number = st->pass_index + loop_offset
     uint32_t max_passes;  // loop passes from this number on copy through; box after all but the last
+    const int4 *filt;     // the density pass's deferred Gauss filter (gradient sum, boundariness > 0)
+    float *bness;
 };
 
 __device__ __forceinline__ void accumulate(float *dst, int mode, uint32_t j, float v) {
@@ -380,7 +403,7 @@ __device__ __forceinline__ void accumulate(float *dst, int mode, uint32_t j, flo
 }
 
 template <bool GAUSS, int L>
-__global__ void __launch_bounds__(256, GAUSS && L == 1 ? 5 : 4) k_delta(PassB a) {
+__global__ void __launch_bounds__(256, 4) k_delta(PassB a) {
     const uint32_t n = a.d_len[kLenParticles];
     bool skip = a.early_exit && *(volatile const uint32_t *)&a.st->converged;
     uint32_t nboxes = a.nboxes;
@@ -389,7 +412,22 @@ __global__ void __launch_bounds__(256, GAUSS && L == 1 ? 5 : 4) k_delta(PassB a)
         skip = skip || pass >= a.max_passes;
         if (pass + 1u >= a.max_passes) nboxes = 0u;  // no box collision after the last iteration
     }
+    // the density pass of this pass deferred the Gauss filter to here (symmetric rows)
+    const bool filter = GAUSS && *(volatile const uint32_t *)&a.st->filter_tag != 0u;
     if (skip) {
+        if (filter) {  // converged: no position update, but the filter still belongs to this pass
+            for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+                const int4 fj = a.filt[j];
+                float3 ed;
+                if (!fj.w || !filter_dir(fj.x, fj.y, fj.z, ed)) continue;
+                const int4 p = a.pos[j];
+                for (uint32_t k = 0; k < a.count[j]; ++k)
+                    if (gauss_filter_hit(ed, fdiff(p, a.pos[a.idx[(size_t)k * a.stride + j]]))) {
+                        a.bness[j] = 0.0f;
+                        break;
+                    }
+            }
+        }
         for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
             a.pos_out[j] = a.pos[j];
             accumulate(a.lam_prev, a.prev_mode, j, 0.0f);  // nothing applied in this pass
@@ -409,6 +447,12 @@ __global__ void __launch_bounds__(256, GAUSS && L == 1 ? 5 : 4) k_delta(PassB a)
         int32_t ax = 0, ay = 0, az = 0;
         const uint32_t cnt = valid ? cnt_arr[j] : 0u;
         const uint32_t *row = idx_arr + j;
+        float3 ed = make_float3(0.f, 0.f, 0.f);
+        bool fil = false, hit = false;  // this particle's deferred filter, and whether a neighbour cleared it
+        if (filter && valid) {
+            const int4 fj = a.filt[j];
+            fil = fj.w != 0 && filter_dir(fj.x, fj.y, fj.z, ed);
+        }
         for (uint32_t k0 = sub; k0 < cnt; k0 += L * kUnroll) {
             uint32_t ii[kUnroll];
             float4 rr[kUnroll];
@@ -425,6 +469,10 @@ __global__ void __launch_bounds__(256, GAUSS && L == 1 ? 5 : 4) k_delta(PassB a)
             }
 #pragma unroll
             for (int u = 0; u < kUnroll; ++u) {
+                if (fil && !hit && k0 + u * L < cnt) {
+                    const float3 dn = fdiff(qq[u], p);  // x_i - x_j ...
+                    hit = gauss_filter_hit(ed, make_float3(-dn.x, -dn.y, -dn.z));  // ... as the offset x_j - x_i
+                }
                 const float lam = k0 + u * L < cnt ? rr[u].x : 0.0f;
                 if (lam == 0.0f) continue;  // the applied lambda (incompressibility_3.comp:63); padding lanes
                 KConst c;
@@ -448,8 +496,15 @@ __global__ void __launch_bounds__(256, GAUSS && L == 1 ? 5 : 4) k_delta(PassB a)
             ax = group_wsum<L>(ax);
             ay = group_wsum<L>(ay);
             az = group_wsum<L>(az);
+            if (filter) {
+                int h = hit ? 1 : 0;
+#pragma unroll
+                for (int off = L / 2; off > 0; off >>= 1) h |= __shfl_xor_sync(0xffffffffu, h, off);
+                hit = h != 0;
+            }
         }
         if (!valid || sub != 0) continue;
+        if (hit) a.bness[j] = 0.0f;
         const int4 sh = a.shift[j];  // the self shift (incompressibility_2.comp:106-109)
         ax = wadd(ax, sh.x);
         ay = wadd(ay, sh.y);
@@ -552,6 +607,7 @@ apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s, const SolveOpts &o)
     a.projected = projected && prev_mode == 2 ? 1 : 0;
     a.loop_offset = o.loop_offset;
     a.max_passes = o.max_passes;
+    a.filt = ctx->tuning.filter_in_density ? nullptr : ctx->filt;
     const float rm2 = 2.0f * st.smallest_target_radius;
     a.rmin3 = rm2 * rm2 * rm2;
     a.hk = st.height_kernel_id;
@@ -606,6 +662,8 @@ apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s, const SolveOpts &o)
     b.acc_mode = acc_mode;
     b.loop_offset = o.loop_offset;
     b.max_passes = o.max_passes;
+    b.filt = ctx->filt;
+    b.bness = f.boundariness;
     APBF_BEFORE_LAUNCH(ctx, s, "k_delta");
     const int gd = grid_for(ctx, (uint32_t)std::min<uint64_t>((uint64_t)cap * lanes, 0xffffffffu), pb, bps);
     launch_lanes(lanes, [&](auto lc) {

@@ -30,7 +30,8 @@ def test_gather_lanes_bit_identical(name):
     for lanes, block, per_sm in ((1, 256, 8), (2, 256, 8), (4, 128, 2), (8, 256, 4), (1, 128, 4), (2, 128, 8)):
         ctx = _ctx(spec, 5, maxn=maxn)
         ctx.set_tuning(gather_lanes=lanes, pass_block=block, pass_blocks_per_sm=per_sm)
-        assert ctx.tuning() == {"gather_lanes": lanes, "pass_block": block, "pass_blocks_per_sm": per_sm}
+        assert ctx.tuning() == {"gather_lanes": lanes, "pass_block": block, "pass_blocks_per_sm": per_sm,
+                                "build_tiled": 0, "filter_in_density": 0}
         for _ in range(8):
             ctx.substep(spec.dt)
         ctx.check_status()
@@ -51,7 +52,8 @@ def test_autotune_keeps_state():
     res = ctx.autotune()
     assert res["gather_lanes"] in (1, 2, 4, 8) and res["pass_block"] in (128, 256)
     assert len(res["pass_ms"]) == 24 and all(v > 0 for v in res["pass_ms"].values())
-    assert ctx.tuning() == {k: res[k] for k in ("gather_lanes", "pass_block", "pass_blocks_per_sm")}
+    assert ctx.tuning() == {k: res[k] for k in ("gather_lanes", "pass_block", "pass_blocks_per_sm", "build_tiled",
+                                                "filter_in_density")}
     after, _ = ctx.download()
     for k in before:
         assert np.array_equal(before[k], after[k]), k
@@ -81,3 +83,66 @@ def test_set_tuning_rejects_bad_shapes():
         with pytest.raises(ApbfError):
             ctx.set_tuning(**bad)
     ctx.close()
+
+
+@pytest.mark.parametrize("name", ["dam_break", "water_drop_adaptive", "outside_grid"])
+def test_tiled_build_identical_rows(name):
+    """Neighbour rows built by shared-memory tiles equal the per-thread walk's, entry
+    for entry, and so do whole substeps."""
+    if name == "dam_break":
+        spec, maxn = scenes.dam_break(n_side=18), 128
+    elif name == "water_drop_adaptive":
+        spec, maxn = scenes.water_drop(total=20_000, seed=6, basic_pbf=False), 256
+    else:  # a block partly outside the search grid: clamped cells, the 64-bit predicate
+        from dataclasses import replace
+
+        spec = scenes.dam_break(n_side=14, seed=3)
+        st = {k: v.copy() for k, v in spec.state.items()}
+        st["position"][:, 0] -= np.int32(20 * 262144)
+        spec = replace(spec, state=st, box_min=np.zeros((0, 4), np.float32), box_max=np.zeros((0, 4), np.float32))
+        maxn = 160
+    out = []
+    for tiled in (0, 1):
+        ctx = _ctx(spec, 4, maxn=maxn)
+        ctx.set_tuning(build_tiled=tiled)
+        rows = []
+        for _ in range(5):
+            ctx.substep(spec.dt)
+            n, _ = ctx.lengths()
+            nb = ctx.neighbors_view()
+            cnt = nb["count"][:n].cpu().numpy().copy()
+            idx = nb["index"][:, :n].cpu().numpy().copy()
+            rows.append((cnt, idx))
+        ctx.check_status()
+        out.append((rows, ctx.download()[0]))
+        ctx.close()
+    (ra, sa), (rb, sb) = out
+    for (ca, ia), (cb, ib) in zip(ra, rb):
+        assert np.array_equal(ca, cb)
+        for k in range(int(ca.max())):
+            live = ca > k
+            assert np.array_equal(ia[k][live], ib[k][live]), k
+    for k in sa:
+        assert np.array_equal(sa[k], sb[k]), k
+
+
+@pytest.mark.parametrize("lanes", [1, 4])
+def test_deferred_filter_identical(lanes):
+    """The Gauss boundariness filter run in the position pass (symmetric rows) gives
+    the same substeps as running it in the density pass; a converged pass still
+    filters."""
+    spec = scenes.water_drop(total=30_000, seed=8, basic_pbf=True)
+    out = []
+    for inline in (1, 0):
+        ctx = _ctx(spec, 30, target=2e-3, maxn=192)
+        ctx.set_tuning(gather_lanes=lanes, filter_in_density=inline)
+        for _ in range(25):
+            ctx.substep(spec.dt)
+        info = ctx.check_status()
+        out.append((ctx.download()[0], info.density_passes, info.converged_substeps))
+        ctx.close()
+    (a, pa, ca), (b, pb, cb) = out
+    assert (pa, ca) == (pb, cb)
+    assert np.any(a["boundariness"] == 0) and np.any(a["boundariness"] > 0)
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
