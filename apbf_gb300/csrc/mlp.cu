@@ -1,9 +1,10 @@
 // mlp.cu -- the learned warm start of the Jacobi solve (no reference counterpart).
 //
-// A 6 -> 64 -> 64 -> 1 ReLU network maps per-particle features of the first
+// A 7 -> 64 -> 64 -> 1 ReLU network maps per-particle features of the first
 // density pass (neighbour count, density ratio, kernel width, the plain Jacobi
-// lambda, velocity divergence, the previous substep's applied lambda sum) to an
-// initial lambda that replaces the plain one in the first position update.  Weights are BF16 on the tensor cores with FP32
+// lambda, velocity divergence, the previous substep's applied lambda sum and its
+// neighbour mean) to an initial lambda that replaces the plain one in the first
+// position update.  Weights are BF16 on the tensor cores with FP32
 // accumulation (mma.sync m16n8k16); the master copy is FP32.
 //
 // Parameter vector (FP32), offsets in floats:
@@ -33,7 +34,7 @@ namespace apbf {
 constexpr int kP_MU = 0, kP_IS = 8, kP_W1 = 16, kP_B1 = 528, kP_W2 = 592, kP_B2 = 4688, kP_W3 = 4752, kP_B3 = 4816,
               kP_YS = 4817, kP_YM = 4818, kP_OM = 4819, kP_NMIN = 4820, kP_N = 4824;
 constexpr int kH = 64;          // hidden width
-constexpr int kF = 8;           // feature slots (6 used)
+constexpr int kF = 8;           // feature slots (7 used)
 constexpr int kRowsWarp = 32;   // rows per warp (two m16 tiles)
 constexpr int kWarps = 4;
 constexpr int kRowsCta = kRowsWarp * kWarps;

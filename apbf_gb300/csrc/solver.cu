@@ -167,6 +167,7 @@ __global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) 
         const bool feat = a.features != nullptr;
         const float4 vi = feat ? a.vel[i] : make_float4(0.f, 0.f, 0.f, 0.f);
         float div = 0.0f;  // sum_j m_j (v_j - v_i) . gradW_ij  (velocity divergence x density)
+        float nprev = 0.0f;  // sum_j lambda_prev_j (the neighbours' previous-substep lambda sums)
         // Batches of kUnroll pairs per lane: all row entries, then all neighbour
         // gathers, then the arithmetic, so each lane keeps kUnroll loads in flight.
         for (uint32_t k0 = sub; k0 < cnt; k0 += L * kUnroll) {
@@ -197,6 +198,7 @@ __global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) 
                 if (feat) {
                     const float4 vj = a.vel[jj[u]];
                     div += __int_as_float(q.w) * ((vj.x - vi.x) * g.x + (vj.y - vi.y) * g.y + (vj.z - vi.z) * g.z);
+                    nprev += a.lam_prev[jj[u]];
                 }
                 if (a.method == 1) {  // incompressibility_1.comp:62-68
                     const float den = kw * APBF_FIX / mjf;
@@ -213,7 +215,10 @@ __global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) 
             gx = group_wsum<L>(gx);
             gy = group_wsum<L>(gy);
             gz = group_wsum<L>(gz);
-            if (feat) div = group_sum<L>(div);
+            if (feat) {
+                div = group_sum<L>(div);
+                nprev = group_sum<L>(nprev);
+            }
             if (a.method == 1) {
                 cx = group_wsum<L>(cx);
                 cy = group_wsum<L>(cy);
@@ -274,7 +279,7 @@ __global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) 
             fo[3] = lam;
             fo[4] = density > 0.0f ? div / density : 0.0f;
             fo[5] = a.lam_prev[i];
-            fo[6] = 0.0f;
+            fo[6] = cnt ? nprev / (float)cnt : 0.0f;
             fo[7] = 0.0f;
             a.selfdir[i] = make_float4(-wgs.x * ird, -wgs.y * ird, -wgs.z * ird, im);
         }

@@ -9,9 +9,10 @@ lambda that the first position update uses:
     features  f0 neighbour count, f1 rho/rho0 - 1, f2 kernel width / radius,
               f3 the plain Jacobi lambda of that pass, f4 velocity divergence /
               density, f5 sum of the lambdas applied to the particle in the
-              previous substep (carried through the sort and split/merge)
+              previous substep (carried through the sort and split/merge),
+              f6 the mean of f5 over the particle's neighbours
     target    sum of min(0, lambda) over the first K plain passes of the substep
-    network   6 -> 64 -> 64 -> 1 ReLU, BF16 weights, FP32 accumulation (mma.sync)
+    network   7 -> 64 -> 64 -> 1 ReLU, BF16 weights, FP32 accumulation (mma.sync)
 
 Only the first update changes; the following passes are the plain solve, which
 keeps measuring the mean compression error and stops at density_error_target.
@@ -37,9 +38,9 @@ from . import _native as N
 PARAMS = N.MLP_PARAMS
 P_MU, P_IS, P_W1, P_B1, P_W2, P_B2, P_W3, P_B3, P_YS, P_YM, P_OMEGA, P_NMIN = (0, 8, 16, 528, 592, 4688, 4752, 4816,
                                                                              4817, 4818, 4819, 4820)
-HIDDEN, FEATURE_SLOTS, FEATURES_USED = 64, 8, 6
+HIDDEN, FEATURE_SLOTS, FEATURES_USED = 64, 8, 7
 FEATURE_NAMES = ("neighbour_count", "density_ratio_minus_1", "kernel_width_over_radius", "plain_lambda",
-                 "velocity_divergence", "previous_substep_lambda")
+                 "velocity_divergence", "previous_substep_lambda", "neighbours_previous_substep_lambda")
 
 
 def _ptr(t: torch.Tensor | None) -> C.c_void_p:

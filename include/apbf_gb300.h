@@ -326,12 +326,12 @@ apbf_status apbf_profile_read(apbf_ctx *ctx, apbf_kernel_time *out, uint32_t cap
 apbf_status apbf_launch_count(apbf_ctx *ctx, unsigned long long *out);
 
 /* ---- learned warm start of the Jacobi solve (no reference counterpart) ----
- * A 6 -> 64 -> 64 -> 1 ReLU network (BF16 weights, FP32 accumulation, tensor
+ * A 7 -> 64 -> 64 -> 1 ReLU network (BF16 weights, FP32 accumulation, tensor
  * cores) maps per-particle features of the first density pass of a substep --
  * neighbour count, rho/rho0 - 1, kernel width / radius, the plain Jacobi lambda,
  * velocity divergence / density, the sum of the lambdas applied to the particle
- * in the previous substep (8 slots, 6 used) -- to the lambda used by that
- * substep's first position update.  Later iterations are the plain solve, which stays the judge of the
+ * in the previous substep, and that sum's mean over the neighbours (8 slots, 7
+ * used) -- to the lambda used by that substep's first position update.  Later iterations are the plain solve, which stays the judge of the
  * density error (density_error_target).  Parameters are one FP32 vector of
  * apbf_mlp_param_count() floats: mu[8], 1/sigma[8], W1[64][8], b1[64],
  * W2[64][64], b2[64], w3[64], b3, y_scale, y_mean (lambda = y * y_scale + y_mean),

@@ -197,7 +197,7 @@ def test_recorded_samples_match_oracle(orc):
     div = outs[0]["divergence"].astype(np.float64) / dens
     dsc = np.abs(div).max()
     assert np.all(np.abs(X[:, 4] - div) <= 1e-4 * np.abs(div) + 1e-4 * dsc), np.abs(X[:, 4] - div).max()
-    assert np.all(X[:, 5:] == 0)  # no lambda history before the first substep
+    assert np.all(X[:, 5:] == 0)  # no lambda history before the first substep (f5, f6), f7 unused
     tgt = sum(np.minimum(o["lambda"].astype(np.float64), 0.0) for o in outs)
     tsc = np.abs(tgt).max()
     assert tsc > 0
@@ -227,6 +227,12 @@ def test_previous_substep_lambda_feature():
     assert np.all(X[:spec.n, 5] == 0)
     assert np.any(T[:spec.n] < 0)
     assert np.array_equal(np.sort(X[spec.n:, 5]), np.sort(T[:spec.n]))
+    # f6: the mean of f5 over the particle's neighbours (rows of the second substep)
+    rows = ctx.download_rows()
+    X2 = X[spec.n:]
+    want = np.array([X2[r, 5].astype(np.float64).mean() if len(r) else 0.0 for r in rows])
+    assert np.allclose(X2[:, 6], want, rtol=1e-5, atol=1e-6 * np.abs(want).max())
+    assert np.any(want != 0)
     ctx.close()
 
 
