@@ -12,6 +12,8 @@
 //     column-major so that consecutive particles' k-th entries are contiguous.
 //  6. k_reverse_rows (only when search radii differ): transpose the rows, so the
 //     position-update pass can gather instead of scattering with atomics.
+#include <algorithm>
+
 #include "apbf_internal.cuh"
 
 namespace apbf {
@@ -425,6 +427,113 @@ __global__ void __launch_bounds__(kTileP) k_build_rows_tiled(BuildArgs a) {
     }
 }
 
+// The same rows again, one warp per particle: lanes take 32 of the particle's
+// cells at a time, a warp scan turns their particle counts into offsets, and each
+// round the 32 lanes test 32 consecutive candidates (of whichever cells they fall
+// in) and append the hits with a ballot, so the row keeps the walk's order (cells
+// in (z, y, x) order, indices ascending within a cell) and the lanes stay busy
+// whatever the particles' cell counts.
+__global__ void __launch_bounds__(256) k_build_rows_warp(BuildArgs a) {
+    const uint32_t n = a.d_len[kLenParticles];
+    const uint32_t last = (1u << a.L) - 1u;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+    unsigned long long local = 0;
+    long long rmin = 0x7fffffffffffffffll, rmax = -1;
+    for (uint32_t i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps) {  // warp-uniform
+        const int4 p = a.pos[i];
+        const long long R = range_fixed(a.range[i], a.scale);
+        uint32_t c = 0;
+        if (R < 0) {
+            if (lane == 0) set_flag(a.st, APBF_FLAG_NONFINITE);
+        } else {
+            rmin = R < rmin ? R : rmin;
+            rmax = R > rmax ? R : rmax;
+            const Bounds &b = a.b;
+            const uint32_t x0 = cell_coord((long long)p.x - R, b.lo[0], b.hi[0], a.L);
+            const uint32_t x1 = cell_coord((long long)p.x + R, b.lo[0], b.hi[0], a.L);
+            const uint32_t y0 = cell_coord((long long)p.y - R, b.lo[1], b.hi[1], a.L);
+            const uint32_t y1 = cell_coord((long long)p.y + R, b.lo[1], b.hi[1], a.L);
+            const uint32_t z0 = cell_coord((long long)p.z - R, b.lo[2], b.hi[2], a.L);
+            const uint32_t z1 = cell_coord((long long)p.z + R, b.lo[2], b.hi[2], a.L);
+            const bool fast = a.fast_ok && x0 > 0 && y0 > 0 && z0 > 0 && x1 < last && y1 < last && z1 < last;
+            const uint32_t nx = x1 - x0 + 1, ny = y1 - y0 + 1, nz = z1 - z0 + 1;
+            const uint32_t ncells = nx * ny * nz;
+            const uint32_t R32 = (uint32_t)R;
+            const unsigned long long R2 = (unsigned long long)R32 * R32;
+            for (uint32_t cb = 0; cb < ncells; cb += 32) {
+                // this lane's cell and its particle range
+                const uint32_t k = cb + lane;
+                uint32_t cs = 0, cnt = 0;
+                if (k < ncells) {
+                    const uint32_t cx = x0 + k % nx, cy = y0 + (k / nx) % ny, cz = z0 + k / (nx * ny);
+                    const uint32_t key = spread3(cx) | (spread3(cy) << 1) | (spread3(cz) << 2);
+                    cs = a.cstart[key];
+                    cnt = a.cend[key] - cs;
+                }
+                uint32_t incl = cnt;  // inclusive scan of the counts over the lanes
+#pragma unroll
+                for (int off = 1; off < 32; off <<= 1) {
+                    const uint32_t o = __shfl_up_sync(0xffffffffu, incl, off);
+                    if (lane >= (uint32_t)off) incl += o;
+                }
+                const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+                const uint32_t excl = incl - cnt;
+                for (uint32_t t0 = 0; t0 < total; t0 += 32) {
+                    const uint32_t g = t0 + lane;
+                    // the lane whose cell holds candidate g: the last lane with excl <= g
+                    uint32_t lo = 0;
+#pragma unroll
+                    for (int step = 16; step > 0; step >>= 1) {
+                        const uint32_t e = __shfl_sync(0xffffffffu, excl, lo + step);
+                        if (e <= g) lo += step;
+                    }
+                    const uint32_t owner_cs = __shfl_sync(0xffffffffu, cs, lo);
+                    const uint32_t owner_ex = __shfl_sync(0xffffffffu, excl, lo);
+                    bool hit = false;
+                    uint32_t j = 0;
+                    if (g < total) {
+                        j = owner_cs + (g - owner_ex);
+                        if (j != i) {
+                            const int4 q = a.pos[j];
+                            hit = fast ? within32(p, q, R32, R2) : within(p, q, R);
+                        }
+                    }
+                    const uint32_t mask = __ballot_sync(0xffffffffu, hit);
+                    if (hit) {
+                        const uint32_t slot = c + __popc(mask & ((1u << lane) - 1u));
+                        if (slot < a.maxn) a.idx[(size_t)slot * a.stride + i] = j;
+                    }
+                    c += __popc(mask);
+                }
+            }
+        }
+        if (lane == 0) {
+            if (c > a.maxn) {
+                set_flag(a.st, APBF_FLAG_NEIGHBOR_OVERFLOW);
+                atomicMax(&a.st->required_neighbors, c);
+            }
+            a.count[i] = c < a.maxn ? c : a.maxn;
+            local += c < a.maxn ? c : a.maxn;
+            if (a.pos_box) a.pos_box[i] = box_push(p, a.radius[i], i, a.bmin, a.bmax, a.rot, a.nboxes);
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        local += __shfl_down_sync(0xffffffffu, local, off);
+        long long a2 = __shfl_down_sync(0xffffffffu, rmin, off);
+        long long c2 = __shfl_down_sync(0xffffffffu, rmax, off);
+        rmin = a2 < rmin ? a2 : rmin;
+        rmax = c2 > rmax ? c2 : rmax;
+    }
+    if (lane == 0) {
+        if (local) atomicAdd(a.total, local);
+        if (rmax >= 0) {
+            atomicMin(&a.st->range_min, (unsigned long long)rmin);
+            atomicMax(&a.st->range_max, (unsigned long long)rmax);
+        }
+    }
+}
+
 __global__ void k_reverse_rows(const uint32_t *d_len, uint32_t stride, uint32_t maxn, const uint32_t *__restrict__ count,
                                const uint32_t *__restrict__ idx, uint32_t *__restrict__ rcount,
                                uint32_t *__restrict__ ridx, Status *st) {
@@ -542,8 +651,11 @@ apbf_status neighborhood_green(apbf_ctx *ctx, float range_scale, const float min
     ba.idx = ctx->nb_idx;
     ba.total = ctx->d_pairs;
     ba.st = ctx->status;
-    if (ctx->tuning.build_tiled)
+    if (ctx->tuning.build_tiled == 1)
         k_build_rows_tiled<<<grid_for(ctx, cap, kTileP, 24), kTileP, 0, s>>>(ba);
+    else if (ctx->tuning.build_tiled == 2)
+        k_build_rows_warp<<<grid_for(ctx, (uint32_t)std::min<uint64_t>((uint64_t)cap * 32u, 0xffffffffu), kBlock, 8),
+                            kBlock, 0, s>>>(ba);
     else
         k_build_rows<<<grid_for(ctx, cap, kBlock, 8), kBlock, 0, s>>>(ba);
     APBF_AFTER_LAUNCH(ctx, s, "k_build_rows");

@@ -43,8 +43,9 @@ extern "C" apbf_status apbf_set_tuning(apbf_ctx *ctx, const apbf_tuning *t) {
     if (!ctx || !t) return APBF_ERR_INVALID_ARG;
     const uint32_t l = t->gather_lanes;
     if ((l != 1 && l != 2 && l != 4 && l != 8) || (t->pass_block != 128 && t->pass_block != 256) ||
-        t->pass_blocks_per_sm < 1 || t->pass_blocks_per_sm > 8) {
-        set_error("apbf_set_tuning: gather_lanes 1, 2, 4 or 8; pass_block 128 or 256; pass_blocks_per_sm 1..8");
+        t->pass_blocks_per_sm < 1 || t->pass_blocks_per_sm > 8 || t->build_tiled > 2) {
+        set_error("apbf_set_tuning: gather_lanes 1, 2, 4 or 8; pass_block 128 or 256; pass_blocks_per_sm 1..8; "
+                  "build_tiled 0, 1 or 2");
         return APBF_ERR_INVALID_ARG;
     }
     ctx->tuning = *t;

@@ -168,7 +168,8 @@ typedef struct apbf_tuning {
     uint32_t gather_lanes;        /* threads per particle in the density and position passes: 1, 2, 4 or 8 */
     uint32_t pass_block;          /* threads per block of those passes: 128 or 256 */
     uint32_t pass_blocks_per_sm;  /* their grid: up to this many blocks per SM (1..8) */
-    uint32_t build_tiled;         /* 1: neighbour rows built by blocks that stage candidates in shared memory */
+    uint32_t build_tiled;         /* neighbour-row build: 0 one thread per particle, 1 blocks that stage
+                                     candidates in shared memory, 2 one warp per particle (same rows) */
     uint32_t filter_in_density;   /* 1: the boundariness filter always runs in the density pass (else, with
                                      symmetric rows and the Gauss kernel, in the position pass) */
     uint32_t reserved[3];

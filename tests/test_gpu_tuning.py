@@ -79,7 +79,8 @@ def test_set_tuning_rejects_bad_shapes():
 
     spec = scenes.dam_break(n_side=8)
     ctx = _ctx(spec, 2)
-    for bad in (dict(gather_lanes=3), dict(pass_block=192), dict(pass_blocks_per_sm=0), dict(pass_blocks_per_sm=9)):
+    for bad in (dict(gather_lanes=3), dict(pass_block=192), dict(pass_blocks_per_sm=0), dict(pass_blocks_per_sm=9),
+                dict(build_tiled=3)):
         with pytest.raises(ApbfError):
             ctx.set_tuning(**bad)
     ctx.close()
@@ -87,8 +88,8 @@ def test_set_tuning_rejects_bad_shapes():
 
 @pytest.mark.parametrize("name", ["dam_break", "water_drop_adaptive", "outside_grid"])
 def test_tiled_build_identical_rows(name):
-    """Neighbour rows built by shared-memory tiles equal the per-thread walk's, entry
-    for entry, and so do whole substeps."""
+    """Neighbour rows built by shared-memory tiles and by a warp per particle equal
+    the per-thread walk's, entry for entry, and so do whole substeps."""
     if name == "dam_break":
         spec, maxn = scenes.dam_break(n_side=18), 128
     elif name == "water_drop_adaptive":
@@ -102,7 +103,7 @@ def test_tiled_build_identical_rows(name):
         spec = replace(spec, state=st, box_min=np.zeros((0, 4), np.float32), box_max=np.zeros((0, 4), np.float32))
         maxn = 160
     out = []
-    for tiled in (0, 1):
+    for tiled in (0, 1, 2):
         ctx = _ctx(spec, 4, maxn=maxn)
         ctx.set_tuning(build_tiled=tiled)
         rows = []
@@ -116,14 +117,15 @@ def test_tiled_build_identical_rows(name):
         ctx.check_status()
         out.append((rows, ctx.download()[0]))
         ctx.close()
-    (ra, sa), (rb, sb) = out
-    for (ca, ia), (cb, ib) in zip(ra, rb):
-        assert np.array_equal(ca, cb)
-        for k in range(int(ca.max())):
-            live = ca > k
-            assert np.array_equal(ia[k][live], ib[k][live]), k
-    for k in sa:
-        assert np.array_equal(sa[k], sb[k]), k
+    ra, sa = out[0]
+    for rb, sb in out[1:]:
+        for (ca, ia), (cb, ib) in zip(ra, rb):
+            assert np.array_equal(ca, cb)
+            for k in range(int(ca.max())):
+                live = ca > k
+                assert np.array_equal(ia[k][live], ib[k][live]), k
+        for k in sa:
+            assert np.array_equal(sa[k], sb[k]), k
 
 
 @pytest.mark.parametrize("lanes", [1, 4])
