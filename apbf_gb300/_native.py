@@ -206,6 +206,12 @@ SIGNATURES = {
     "apbf_mlp_forward": (_ST, [_P, _P, C.c_uint32, _P, _P]),
     "apbf_mlp_train_step": (_ST, [_P, _P, _P, _P, _P, _P, C.c_uint32, C.c_float, C.c_float, C.c_uint32, _P, _P,
                                   _P]),
+    "apbf_sphere_collision_apply": (_ST, [_P, _F3, C.c_float, C.c_int, _P]),
+    "apbf_inter_particle_collision_apply": (_ST, [_P, _P]),
+    "apbf_glue_generate": (_ST, [_P, C.c_uint32, _P]),
+    "apbf_glue_apply": (_ST, [_P, C.c_float, C.c_float, _P]),
+    "apbf_glue_get_view": (_ST, [_P, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
+                                 C.POINTER(C.c_void_p), C.POINTER(C.c_uint32)]),
     "apbf_sort_pairs": (_ST, [_P, _P, _P, _P, C.c_uint32, C.c_uint32, _P, _P, _P]),
     "apbf_sort_pairs_noalloc": (_ST, [_P, _P, _P, C.c_uint32, C.c_uint32, _P, _P, _P]),
     "apbf_prefix_sum": (_ST, [_P, _P, _P, C.c_uint32, _P]),

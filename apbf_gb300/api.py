@@ -514,6 +514,74 @@ class particle_transfer:
                 "particle_transfer.apply")
 
 
+class sphere_collision:
+    """pbd::sphere_collision (source/sphere_collision.h)."""
+
+    def set_data(self, ctx: Context) -> "sphere_collision":
+        self.ctx = ctx
+        return self
+
+    def set_sphere(self, center, radius: float, hollow: bool) -> "sphere_collision":
+        self.center, self.radius, self.hollow = tuple(center), float(radius), bool(hollow)
+        return self
+
+    def apply(self, stream=None) -> None:
+        N.check(self.ctx.lib.apbf_sphere_collision_apply(self.ctx.handle, (C.c_float * 3)(*self.center),
+                                                         C.c_float(self.radius), 1 if self.hollow else 0,
+                                                         _stream_handle(stream)), "sphere_collision.apply")
+
+
+class inter_particle_collision:
+    """pbd::inter_particle_collision (source/inter_particle_collision.h)."""
+
+    def set_data(self, ctx: Context) -> "inter_particle_collision":
+        self.ctx = ctx
+        return self
+
+    def apply(self, stream=None) -> None:
+        N.check(self.ctx.lib.apbf_inter_particle_collision_apply(self.ctx.handle, _stream_handle(stream)),
+                "inter_particle_collision.apply")
+
+
+class glue:
+    """pbd::glue (source/glue.h): applyNewGlue() builds the glue list, apply() enforces it."""
+
+    def __init__(self):
+        self.stability, self.elasticity, self.capacity = 1.0, 0.0, 1 << 20
+
+    def set_data(self, ctx: Context, capacity: int = 1 << 20) -> "glue":
+        self.ctx, self.capacity = ctx, capacity
+        return self
+
+    def set_stability(self, s: float) -> "glue":
+        self.stability = float(s)
+        return self
+
+    def set_elasticity(self, e: float) -> "glue":
+        self.elasticity = float(e)
+        return self
+
+    def applyNewGlue(self, stream=None) -> None:  # noqa: N802 (the reference's name)
+        N.check(self.ctx.lib.apbf_glue_generate(self.ctx.handle, self.capacity, _stream_handle(stream)),
+                "glue.applyNewGlue")
+
+    def apply(self, stream=None) -> None:
+        N.check(self.ctx.lib.apbf_glue_apply(self.ctx.handle, C.c_float(self.stability), C.c_float(self.elasticity),
+                                             _stream_handle(stream)), "glue.apply")
+
+    def view(self) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        p0, p1, d, ln = C.c_void_p(), C.c_void_p(), C.c_void_p(), C.c_void_p()
+        cap = C.c_uint32()
+        N.check(self.ctx.lib.apbf_glue_get_view(self.ctx.handle, C.byref(p0), C.byref(p1), C.byref(d), C.byref(ln),
+                                                C.byref(cap)), "apbf_glue_get_view")
+        m = int(device_tensor(ln.value, (1,), torch.int32, self.ctx.device).item())
+        out = []
+        for ptr in (p0, p1, d):
+            out.append(device_tensor(ptr.value, (cap.value,), torch.int32, self.ctx.device)[:m].cpu().numpy()
+                       .view(np.uint32).copy())
+        return tuple(out)
+
+
 class algorithms:
     """pbd::algorithms (source/algorithms.h:12-17) on device tensors."""
 

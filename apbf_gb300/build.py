@@ -23,7 +23,7 @@ OBJ_DIR = HERE / "_build"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off", "--expt-relaxed-constexpr"]
 # translation units whose FP32 arithmetic must not be contracted into FMAs
-NO_FMAD = {"glue.cu", "adaptive.cu"}
+NO_FMAD = {"glue.cu", "adaptive.cu", "constraints.cu"}
 
 
 def nvcc() -> str:

@@ -220,6 +220,8 @@ struct apbf_ctx {
     uint32_t n_boxes = 0;
     uint32_t n_aabb = 0;        // boxes set by apbf_set_boxes (the oriented ones follow)
     apbf_emitter emitter = {};  // emitter.enabled == 0: none
+    uint32_t *glue0 = nullptr, *glue1 = nullptr, *glue_d = nullptr, *glue_len = nullptr;  // glue list (constraints.cu)
+    uint32_t glue_cap = 0;
     float emit_inv_mass = 0.0f;
     double *emit_state = nullptr;  // device: [0] stream time T, [1] particles emitted, [2..3] this substep's plan
 
@@ -312,6 +314,7 @@ inline int32_t f2i_host(float x) {
 
 // ---- host-side stage launchers (defined in the .cu files) ----
 apbf_status emit(apbf_ctx *ctx, float dt, cudaStream_t s);  // glue.cu
+apbf_status glue_remap(apbf_ctx *ctx, cudaStream_t s);      // constraints.cu: glue ids follow a reorder
 apbf_status sort_pairs_device(apbf_ctx *ctx, const uint32_t *keys_in, const uint32_t *vals_in, const uint32_t *d_count,
                               uint32_t max_count, uint32_t key_bits, uint32_t *keys_out, uint32_t *vals_out,
                               cudaStream_t s);

@@ -78,6 +78,10 @@ apbf_status apbf_destroy(apbf_ctx *ctx) {
     }
     destroy_solve_graphs(ctx);
     destroy_substep_graphs(ctx);
+    cudaFree(ctx->glue0);
+    cudaFree(ctx->glue1);
+    cudaFree(ctx->glue_d);
+    cudaFree(ctx->glue_len);
     if (ctx->capture_stream) cudaStreamDestroy(ctx->capture_stream);
     if (ctx->capture_stream2) cudaStreamDestroy(ctx->capture_stream2);
     for (void *p : ctx->owned) cudaFree(p);

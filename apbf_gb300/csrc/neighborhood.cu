@@ -613,6 +613,8 @@ apbf_status neighborhood_green(apbf_ctx *ctx, float range_scale, const float min
     k_remap_transfers<<<grid_for(ctx, ctx->cfg.transfer_capacity), kBlock, 0, s>>>(ctx->tr[ctx->tcur], ctx->inv_perm,
                                                                                     ctx->d_len, ctx->status);
     APBF_AFTER_LAUNCH(ctx, s, "k_remap_transfers");
+    r = glue_remap(ctx, s);
+    if (r != APBF_OK) return r;
     swap_all(ctx);
     FluidBufs &f = ctx->fl[ctx->fcur];
 

@@ -375,6 +375,27 @@ apbf_status apbf_mlp_train_step(float *d_params, float *d_m, float *d_v, float *
                                 const float *d_targets, uint32_t n, float lr, float over_weight, uint32_t step,
                                 float *d_grad, float *d_loss, void *stream);
 
+/* ---- further constraint operators on the same lists ---- */
+/* sphere_collision::apply (source/sphere_collision.cpp:19-31, sphere_collision.comp):
+ * hollow != 0 keeps the particles inside the sphere, 0 outside. */
+apbf_status apbf_sphere_collision_apply(apbf_ctx *ctx, const float center[3], float radius, int hollow, void *stream);
+/* inter_particle_collision::apply (source/inter_particle_collision.cpp:10-18): one
+ * Jacobi step of the non-penetration constraint over the pairs of the neighbour
+ * rows of the last search. */
+apbf_status apbf_inter_particle_collision_apply(apbf_ctx *ctx, void *stream);
+/* glue::applyNewGlue (source/glue.cpp:48-60): replaces the glue list by the pairs of
+ * the neighbour rows that generate_glue.comp glues, in row order (the reference
+ * appends them unordered); grows the list to `capacity` entries on demand
+ * (APBF_FLAG_TRANSFER_OVERFLOW when more pairs qualify).  Glue ids follow later
+ * neighbour-search reorders. */
+apbf_status apbf_glue_generate(apbf_ctx *ctx, uint32_t capacity, void *stream);
+/* glue::apply (source/glue.cpp:38-46, glue.comp), every entry reading the positions
+ * before the pass (glue.comp reads the buffer it updates, a race). */
+apbf_status apbf_glue_apply(apbf_ctx *ctx, float stability, float elasticity, void *stream);
+/* The glue list: particle ids, rest distances (2^18 fixed point), device length. */
+apbf_status apbf_glue_get_view(apbf_ctx *ctx, uint32_t **p0, uint32_t **p1, uint32_t **dist, uint32_t **d_length,
+                               uint32_t *capacity);
+
 /* ---- parallel primitives (source/algorithms.h:12-17) ---- */
 /* algorithms::sort (source/algorithms.cpp:59-91): stable sort of (key, value) pairs
  * by key; only key bits below the highest set bit of value_upper_bound are used.

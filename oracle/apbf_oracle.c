@@ -682,6 +682,123 @@ void or_box_collision(or_fluid *f, const or_boxes *b) {
     }
 }
 
+/* ---- further constraints ---- */
+static float fract_p(float x) { return x - floorf(x); }
+/* shadertoy 4djSRW hash11 (MIT licence), sphere_collision.comp:24-30 */
+static float hash11(float p) {
+    p = fract_p(p * 0.1031f);
+    p *= p + 33.33f;
+    p *= p + p;
+    return fract_p(p);
+}
+
+/* sphere_collision.comp:42-58 */
+void or_sphere_collision(or_fluid *f, const float center[3], float radius, int hollow) {
+    for (uint32_t id = 0; id < f->n; ++id) {
+        int32_t *ip = f->pos + 4 * (size_t)id;
+        float px = (float)ip[0] / 262144.0f, py = (float)ip[1] / 262144.0f, pz = (float)ip[2] / 262144.0f;
+        const float r = f->radius[id];
+        const float dir = hollow ? -1.0f : 1.0f;
+        const float off = dir * (r + hash11((float)id * py + px + pz) * 0.05f);
+        const float rx = px - center[0], ry = py - center[1], rz = pz - center[2];
+        const float d = sqrtf(rx * rx + ry * ry + rz * rz);
+        const float target = radius + off;
+        if ((d < target) == (hollow != 0)) continue;
+        const float s = target / d;
+        ip[0] = f2i_f((center[0] + rx * s) * 262144.0f);
+        ip[1] = f2i_f((center[1] + ry * s) * 262144.0f);
+        ip[2] = f2i_f((center[2] + rz * s) * 262144.0f);
+    }
+}
+
+/* inter_particle_collision.comp:33-51 over the ordered pairs of the rows; a Jacobi
+ * step: reads the old positions, adds to a copy */
+void or_inter_particle_collision(or_fluid *f, const or_neighbors *nb) {
+    const uint32_t n = f->n;
+    int32_t *old = (int32_t *)malloc(16 * (size_t)(n ? n : 1));
+    memcpy(old, f->pos, 16 * (size_t)n);
+    for (uint32_t i = 0; i < n; ++i) {
+        const int32_t *p = old + 4 * (size_t)i;
+        const float r = f->radius[i], im = f->inv_mass[i];
+        for (uint32_t e = nb->offsets[i]; e < nb->offsets[i + 1]; ++e) {
+            const uint32_t j = nb->idx[e];
+            const float rN = f->radius[j];
+            if (rN > r || (rN == r && j >= i)) continue;
+            const int32_t *q = old + 4 * (size_t)j;
+            const float dx = (float)wrap_add(q[0], -p[0]), dy = (float)wrap_add(q[1], -p[1]),
+                        dz = (float)wrap_add(q[2], -p[2]);
+            const float dist = sqrtf(dx * dx + dy * dy + dz * dz);
+            const float ce = dist - (r + rN) * 262144.0f;
+            if (ce >= 0.0f) continue;
+            const float imN = f->inv_mass[j];
+            const float scalar = ce / (im + imN);
+            const float a = im * scalar / dist, b = -imN * scalar / dist;
+            int32_t *pi = f->pos + 4 * (size_t)i, *pj = f->pos + 4 * (size_t)j;
+            pi[0] = wrap_add(pi[0], f2i_f(a * dx));
+            pi[1] = wrap_add(pi[1], f2i_f(a * dy));
+            pi[2] = wrap_add(pi[2], f2i_f(a * dz));
+            pj[0] = wrap_add(pj[0], f2i_f(b * dx));
+            pj[1] = wrap_add(pj[1], f2i_f(b * dy));
+            pj[2] = wrap_add(pj[2], f2i_f(b * dz));
+        }
+    }
+    free(old);
+}
+
+/* generate_glue.comp:30-45, in row order */
+uint32_t or_glue_generate(const or_fluid *f, const or_neighbors *nb, uint32_t *g0, uint32_t *g1, uint32_t *gd,
+                          uint32_t cap) {
+    uint32_t m = 0;
+    for (uint32_t i = 0; i < f->n; ++i) {
+        const int32_t *p = f->pos + 4 * (size_t)i;
+        const float r = f->radius[i];
+        for (uint32_t e = nb->offsets[i]; e < nb->offsets[i + 1]; ++e) {
+            const uint32_t j = nb->idx[e];
+            const float rN = f->radius[j];
+            if (rN > r || (rN == r && i >= j)) continue;
+            const int32_t *q = f->pos + 4 * (size_t)j;
+            const float dx = (float)wrap_add(q[0], -p[0]) / 262144.0f, dy = (float)wrap_add(q[1], -p[1]) / 262144.0f,
+                        dz = (float)wrap_add(q[2], -p[2]) / 262144.0f;
+            const float dist = sqrtf(dx * dx + dy * dy + dz * dz);
+            const float gap = dist - r - rN;
+            if (gap > 2.0f * r) continue;
+            if (m < cap) {
+                g0[m] = i;
+                g1[m] = j;
+                gd[m] = f2u_f(dist * 262144.0f);
+            }
+            ++m;
+        }
+    }
+    return m;
+}
+
+/* glue.comp:39-54 (integer scatter: order-free) */
+void or_glue_apply(or_fluid *f, const uint32_t *g0, const uint32_t *g1, const uint32_t *gd, uint32_t m,
+                   float stability) {
+    const uint32_t n = f->n;
+    int32_t *old = (int32_t *)malloc(16 * (size_t)(n ? n : 1));
+    memcpy(old, f->pos, 16 * (size_t)n);  /* every entry reads the positions before any update */
+    for (uint32_t k = 0; k < m; ++k) {
+        const uint32_t a = g0[k], b = g1[k];
+        const int32_t *p0 = old + 4 * (size_t)a, *p1 = old + 4 * (size_t)b;
+        const float im0 = f->inv_mass[a], im1 = f->inv_mass[b];
+        const float dx = (float)wrap_add(p1[0], -p0[0]), dy = (float)wrap_add(p1[1], -p0[1]),
+                    dz = (float)wrap_add(p1[2], -p0[2]);
+        const float dist = sqrtf(dx * dx + dy * dy + dz * dz);
+        const float ce = dist - (float)gd[k];
+        const float scalar = stability * ce / ((im0 + im1) * dist);
+        int32_t *q0 = f->pos + 4 * (size_t)a, *q1 = f->pos + 4 * (size_t)b;
+        q0[0] = wrap_add(q0[0], f2i_f(im0 * scalar * dx));
+        q0[1] = wrap_add(q0[1], f2i_f(im0 * scalar * dy));
+        q0[2] = wrap_add(q0[2], f2i_f(im0 * scalar * dz));
+        q1[0] = wrap_add(q1[0], f2i_f(-im1 * scalar * dx));
+        q1[1] = wrap_add(q1[1], f2i_f(-im1 * scalar * dy));
+        q1[2] = wrap_add(q1[2], f2i_f(-im1 * scalar * dz));
+    }
+    free(old);
+}
+
 /* ---- emitter (restates the device's k_emit_plan / k_emit) ---- */
 static uint32_t emit_hash(uint32_t seed, uint64_t layer, uint32_t cell, uint32_t axis) {
     uint64_t z = ((uint64_t)seed << 32) ^ (layer * 0x9E3779B97F4A7C15ull) ^ ((uint64_t)cell << 2) ^ axis;

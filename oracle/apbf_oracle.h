@@ -184,6 +184,16 @@ void or_incompressibility_apply(or_fluid *f, const or_neighbors *nb, const or_se
 /* ---- substep glue ---- */
 void or_box_collision(or_fluid *f, const or_boxes *b);
 
+/* Further constraint operators (sphere_collision.comp, inter_particle_collision.comp,
+ * generate_glue.comp + glue.comp), plain FP32 arithmetic in the shaders' order. */
+void or_sphere_collision(or_fluid *f, const float center[3], float radius, int hollow);
+void or_inter_particle_collision(or_fluid *f, const or_neighbors *nb);
+/* glue pairs of the rows in row order; returns the count (at most cap written) */
+uint32_t or_glue_generate(const or_fluid *f, const or_neighbors *nb, uint32_t *g0, uint32_t *g1, uint32_t *gd,
+                          uint32_t cap);
+void or_glue_apply(or_fluid *f, const uint32_t *g0, const uint32_t *g1, const uint32_t *gd, uint32_t m,
+                   float stability);
+
 /* Emitter (no reference counterpart; the device's apbf_set_emitter / the first
  * stage of apbf_substep): appends the lattice layers that cross the emission plane
  * during dt.  state: [0] stream time, [1] particles emitted so far. */

@@ -131,6 +131,7 @@ def lib() -> C.CDLL:
         L.or_morton.restype = C.c_uint32
         L.or_delete_edit_list.restype = C.c_uint32
         L.or_kernel_height.restype = C.c_double
+        L.or_glue_generate.restype = C.c_uint32
         L.or_emit.restype = C.c_uint32
         L.or_kernel_height.argtypes = [C.c_int, C.POINTER(C.c_double), C.c_double]
         L.or_kernel_gradient.argtypes = [C.c_int, C.POINTER(C.c_double), C.c_double, C.POINTER(C.c_double)]
@@ -325,6 +326,29 @@ def box_collision(fs: FluidState, bmin: np.ndarray, bmax: np.ndarray, rot: np.nd
     b, keep = _boxes((bmin, bmax, rot))
     fs._boxes_keep = keep
     lib().or_box_collision(C.byref(fs.f), C.byref(b))
+
+
+def sphere_collision(fs: FluidState, center, radius: float, hollow: bool) -> None:
+    lib().or_sphere_collision(C.byref(fs.f), (C.c_float * 3)(*center), C.c_float(radius), C.c_int(1 if hollow else 0))
+
+
+def inter_particle_collision(fs: FluidState) -> None:
+    lib().or_inter_particle_collision(C.byref(fs.f), C.byref(fs.nb))
+
+
+def glue_generate(fs: FluidState, cap: int) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    g0 = np.zeros(cap, np.uint32)
+    g1 = np.zeros(cap, np.uint32)
+    gd = np.zeros(cap, np.uint32)
+    m = lib().or_glue_generate(C.byref(fs.f), C.byref(fs.nb), _p(g0, _u32p), _p(g1, _u32p), _p(gd, _u32p), cap)
+    m = min(int(m), cap)
+    return g0[:m].copy(), g1[:m].copy(), gd[:m].copy()
+
+
+def glue_apply(fs: FluidState, g0: np.ndarray, g1: np.ndarray, gd: np.ndarray, stability: float) -> None:
+    a, b, d = (np.ascontiguousarray(x, np.uint32) for x in (g0, g1, gd))
+    lib().or_glue_apply(C.byref(fs.f), _p(a, _u32p), _p(b, _u32p), _p(d, _u32p), C.c_uint32(a.size),
+                        C.c_float(stability))
 
 
 class OrEmitter(C.Structure):
