@@ -212,6 +212,11 @@ SIGNATURES = {
     "apbf_glue_apply": (_ST, [_P, C.c_float, C.c_float, _P]),
     "apbf_glue_get_view": (_ST, [_P, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
                                  C.POINTER(C.c_void_p), C.POINTER(C.c_uint32)]),
+    "apbf_list_apply_edit": (_ST, [_P, C.c_uint32, _P, _P, C.c_uint32, _P, _P]),
+    "apbf_list_delete_edit": (_ST, [_P, _P, _P, C.c_uint32, C.c_uint32, _P, _P, _P]),
+    "apbf_list_remap_index": (_ST, [_P, _P, _P, C.c_uint32, _P, _P, C.c_uint32, C.c_uint32, _P, _P, C.c_uint32, _P,
+                                    _P, _P]),
+    "apbf_list_append": (_ST, [_P, _P, C.c_uint32, _P, _P, C.c_uint32, C.c_uint32, _P, _P]),
     "apbf_sort_pairs": (_ST, [_P, _P, _P, _P, C.c_uint32, C.c_uint32, _P, _P, _P]),
     "apbf_sort_pairs_noalloc": (_ST, [_P, _P, _P, C.c_uint32, C.c_uint32, _P, _P, _P]),
     "apbf_prefix_sum": (_ST, [_P, _P, _P, C.c_uint32, _P]),

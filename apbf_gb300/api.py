@@ -514,6 +514,72 @@ class particle_transfer:
                 "particle_transfer.apply")
 
 
+class lists:
+    """The list-edit services (gpu_list / indexed_list, source/gpu_list.h, indexed_list.h) on
+    device tensors of 32-bit words with device lengths."""
+
+    @staticmethod
+    def _u32(n: int, device: int) -> torch.Tensor:
+        return torch.zeros(max(n, 1), dtype=torch.int32, device=f"cuda:{device}")
+
+    @staticmethod
+    def apply_edit(src: torch.Tensor, edit: torch.Tensor, edit_len: torch.Tensor | None = None,
+                   stride_words: int = 1, stream=None) -> torch.Tensor:
+        """gpu_list::apply_edit: dst[k] = src[edit[k]] (elements of stride_words words)."""
+        lib = N.load()
+        m = edit.numel()
+        dst = torch.zeros(max(m * stride_words, 1), dtype=src.dtype, device=src.device)
+        N.check(lib.apbf_list_apply_edit(C.c_void_p(src.data_ptr()), stride_words, C.c_void_p(edit.data_ptr()),
+                                         C.c_void_p(edit_len.data_ptr() if edit_len is not None else 0), m,
+                                         C.c_void_p(dst.data_ptr()), _stream_handle(stream)), "lists.apply_edit")
+        return dst[:m * stride_words]
+
+    @staticmethod
+    def delete_edit(ctx: "Context", deleted: torch.Tensor, n_hidden: int, stream=None) -> torch.Tensor:
+        """indexed_list::delete_these: the edit list of the surviving hidden ids."""
+        d_len = torch.tensor([deleted.numel()], dtype=torch.int32, device=deleted.device)
+        edit = lists._u32(n_hidden, ctx.device)
+        e_len = lists._u32(1, ctx.device)
+        N.check(ctx.lib.apbf_list_delete_edit(ctx.handle, C.c_void_p(deleted.data_ptr()), C.c_void_p(d_len.data_ptr()),
+                                              deleted.numel(), n_hidden, C.c_void_p(edit.data_ptr()),
+                                              C.c_void_p(e_len.data_ptr()), _stream_handle(stream)),
+                "lists.delete_edit")
+        return edit[:int(e_len.item())]
+
+    @staticmethod
+    def remap_index(ctx: "Context", index_list: torch.Tensor, edit: torch.Tensor, n_hidden_old: int,
+                    out_cap: int | None = None, stream=None) -> tuple[torch.Tensor, torch.Tensor, int]:
+        """indexed_list::apply_hidden_edit: (new index list, old position of each entry, full count)."""
+        dev = ctx.device
+        l_len = torch.tensor([index_list.numel()], dtype=torch.int32, device=f"cuda:{dev}")
+        e_len = torch.tensor([edit.numel()], dtype=torch.int32, device=f"cuda:{dev}")
+        cap = out_cap if out_cap is not None else max(1, 4 * index_list.numel() + edit.numel())
+        out, new_edit = lists._u32(cap, dev), lists._u32(cap, dev)
+        o_len, req = lists._u32(1, dev), lists._u32(1, dev)
+        lst = index_list if index_list.numel() else lists._u32(1, dev)
+        ed = edit if edit.numel() else lists._u32(1, dev)
+        N.check(ctx.lib.apbf_list_remap_index(ctx.handle, C.c_void_p(lst.data_ptr()), C.c_void_p(l_len.data_ptr()),
+                                              index_list.numel(), C.c_void_p(ed.data_ptr()),
+                                              C.c_void_p(e_len.data_ptr()), edit.numel(), n_hidden_old,
+                                              C.c_void_p(out.data_ptr()), C.c_void_p(new_edit.data_ptr()), cap,
+                                              C.c_void_p(o_len.data_ptr()), C.c_void_p(req.data_ptr()),
+                                              _stream_handle(stream)), "lists.remap_index")
+        m = int(o_len.item())
+        return out[:m], new_edit[:m], int(req.item())
+
+    @staticmethod
+    def append(dst: torch.Tensor, dst_len: torch.Tensor, src: torch.Tensor, src_len: torch.Tensor,
+               stride_words: int = 1, stream=None) -> None:
+        """gpu_list::operator+=: appends src after the dst_len elements of dst (capacity: dst's size)."""
+        lib = N.load()
+        scratch = torch.zeros(1, dtype=torch.int32, device=dst.device)
+        N.check(lib.apbf_list_append(C.c_void_p(dst.data_ptr()), C.c_void_p(dst_len.data_ptr()),
+                                     dst.numel() // stride_words, C.c_void_p(src.data_ptr()),
+                                     C.c_void_p(src_len.data_ptr()), src.numel() // stride_words, stride_words,
+                                     C.c_void_p(scratch.data_ptr()), _stream_handle(stream)), "lists.append")
+        torch.cuda.current_stream().synchronize()
+
+
 class sphere_collision:
     """pbd::sphere_collision (source/sphere_collision.h)."""
 

@@ -222,6 +222,7 @@ struct apbf_ctx {
     apbf_emitter emitter = {};  // emitter.enabled == 0: none
     uint32_t *glue0 = nullptr, *glue1 = nullptr, *glue_d = nullptr, *glue_len = nullptr;  // glue list (constraints.cu)
     uint32_t glue_cap = 0;
+    uint32_t *le_buf = nullptr;  // list services' scratch (listedit.cu), allocated on first use
     float emit_inv_mass = 0.0f;
     double *emit_state = nullptr;  // device: [0] stream time T, [1] particles emitted, [2..3] this substep's plan
 

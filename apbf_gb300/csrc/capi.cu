@@ -82,6 +82,7 @@ apbf_status apbf_destroy(apbf_ctx *ctx) {
     cudaFree(ctx->glue1);
     cudaFree(ctx->glue_d);
     cudaFree(ctx->glue_len);
+    cudaFree(ctx->le_buf);
     if (ctx->capture_stream) cudaStreamDestroy(ctx->capture_stream);
     if (ctx->capture_stream2) cudaStreamDestroy(ctx->capture_stream2);
     for (void *p : ctx->owned) cudaFree(p);

@@ -396,6 +396,35 @@ apbf_status apbf_glue_apply(apbf_ctx *ctx, float stability, float elasticity, vo
 apbf_status apbf_glue_get_view(apbf_ctx *ctx, uint32_t **p0, uint32_t **p1, uint32_t **dist, uint32_t **d_length,
                                uint32_t *capacity);
 
+/* ---- list-edit services (gpu_list / indexed_list, source/gpu_list.h, indexed_list.h) ----
+ * On plain device arrays with device lengths; the context provides scratch (its
+ * particle capacity bounds the lengths).  Results are deterministic. */
+/* gpu_list::apply_edit (gpu_list.h:125-135, copy_scattered_read.comp): dst[k] =
+ * src[edit[k]], stride_words 32-bit words per element, min(*d_edit_len, max_edit)
+ * elements (d_edit_len may be NULL: max_edit). */
+apbf_status apbf_list_apply_edit(const uint32_t *d_src, uint32_t stride_words, const uint32_t *d_edit,
+                                 const uint32_t *d_edit_len, uint32_t max_edit, uint32_t *d_dst, void *stream);
+/* indexed_list::delete_these (indexed_list.h:125-138): the edit list keeping every
+ * hidden id in [0, n_hidden) not named in d_deleted, in increasing order. */
+apbf_status apbf_list_delete_edit(apbf_ctx *ctx, const uint32_t *d_deleted, const uint32_t *d_deleted_len,
+                                  uint32_t max_deleted, uint32_t n_hidden, uint32_t *d_edit, uint32_t *d_edit_len,
+                                  void *stream);
+/* indexed_list::apply_hidden_edit (indexed_list.h:288-308): the index list after its
+ * hidden list was rebuilt by `edit` (new id e takes old id edit[e]): one entry e per
+ * old entry equal to edit[e], ordered by e, then by old position; d_new_edit (may be
+ * NULL) receives each entry's old position.  At most out_cap entries; d_required
+ * (may be NULL) receives the full count.  A duplication is the edit [0, n) followed
+ * by the duplicated ids (indexed_list::duplicate_these, indexed_list.h:140-152). */
+apbf_status apbf_list_remap_index(apbf_ctx *ctx, const uint32_t *d_list, const uint32_t *d_list_len,
+                                  uint32_t max_list, const uint32_t *d_edit, const uint32_t *d_edit_len,
+                                  uint32_t max_edit, uint32_t n_hidden_old, uint32_t *d_out, uint32_t *d_new_edit,
+                                  uint32_t out_cap, uint32_t *d_out_len, uint32_t *d_required, void *stream);
+/* gpu_list::operator+= (gpu_list.h:213-227, append_list.comp): appends src to dst up
+ * to dst_cap elements; d_scratch_word is one device word. */
+apbf_status apbf_list_append(uint32_t *d_dst, uint32_t *d_dst_len, uint32_t dst_cap, const uint32_t *d_src,
+                             const uint32_t *d_src_len, uint32_t max_src, uint32_t stride_words,
+                             uint32_t *d_scratch_word, void *stream);
+
 /* ---- parallel primitives (source/algorithms.h:12-17) ---- */
 /* algorithms::sort (source/algorithms.cpp:59-91): stable sort of (key, value) pairs
  * by key; only key bits below the highest set bit of value_upper_bound are used.

@@ -246,7 +246,11 @@ def delete_edit_list(n_hidden: int, deleted: np.ndarray) -> np.ndarray:
 def remap_index_list(lst: np.ndarray, edit: np.ndarray, n_hidden_old: int) -> tuple[np.ndarray, np.ndarray]:
     l_ = np.ascontiguousarray(lst, np.uint32)
     e = np.ascontiguousarray(edit, np.uint32)
-    cap = max(int(l_.size) * max(int(e.size), 1), 1)
+    # exact output size: one entry per (edit entry, equal index-list entry)
+    valid_l = l_[l_ < n_hidden_old]
+    cnt = np.bincount(valid_l, minlength=max(n_hidden_old, 1)) if valid_l.size else np.zeros(max(n_hidden_old, 1), int)
+    valid_e = e[e < n_hidden_old]
+    cap = max(int(cnt[valid_e].sum()) if valid_e.size else 0, 1)
     out = np.zeros(cap, np.uint32)
     ne = np.zeros(cap, np.uint32)
     lib().or_remap_index_list.restype = C.c_uint32
