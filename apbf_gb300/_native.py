@@ -212,6 +212,7 @@ SIGNATURES = {
     "apbf_glue_apply": (_ST, [_P, C.c_float, C.c_float, _P]),
     "apbf_glue_get_view": (_ST, [_P, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
                                  C.POINTER(C.c_void_p), C.POINTER(C.c_uint32)]),
+    "apbf_save_particle_info": (_ST, [_P, C.c_char_p, _F3, _P]),
     "apbf_list_apply_edit": (_ST, [_P, C.c_uint32, _P, _P, C.c_uint32, _P, _P]),
     "apbf_list_delete_edit": (_ST, [_P, _P, _P, C.c_uint32, C.c_uint32, _P, _P, _P]),
     "apbf_list_remap_index": (_ST, [_P, _P, _P, C.c_uint32, _P, _P, C.c_uint32, C.c_uint32, _P, _P, C.c_uint32, _P,

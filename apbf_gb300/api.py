@@ -163,6 +163,11 @@ class Context:
         self.emitter = e
         return self
 
+    def save_particle_info(self, folder: str, center=(0.0, 10.0, -60.0), stream=None) -> None:
+        """save_particle_info::apply: the reference's particle-info text files in `folder`."""
+        N.check(self.lib.apbf_save_particle_info(self.handle, str(folder).encode(), (C.c_float * 3)(*center),
+                                                 _stream_handle(stream)), "apbf_save_particle_info")
+
     def set_debug(self, enable: bool) -> None:
         N.check(self.lib.apbf_set_debug(self.handle, 1 if enable else 0), "apbf_set_debug")
 

@@ -396,6 +396,13 @@ apbf_status apbf_glue_apply(apbf_ctx *ctx, float stability, float elasticity, vo
 apbf_status apbf_glue_get_view(apbf_ctx *ctx, uint32_t **p0, uint32_t **p1, uint32_t **dist, uint32_t **d_length,
                                uint32_t *capacity);
 
+/* save_particle_info::apply (source/save_particle_info.cpp:22-125): writes
+ * centerDist.txt, radius.txt, neighborCount.txt, kernelWidth.txt, targetRadius.txt,
+ * boundaryDistance.txt (';'-separated) and data.csv (sorted by the distance to
+ * `center`, stably) into `folder`, with the reference's formatting; the
+ * reference's centre is (0, 10, -60).  Synchronises the stream. */
+apbf_status apbf_save_particle_info(apbf_ctx *ctx, const char *folder, const float center[3], void *stream);
+
 /* ---- list-edit services (gpu_list / indexed_list, source/gpu_list.h, indexed_list.h) ----
  * On plain device arrays with device lengths; the context provides scratch (its
  * particle capacity bounds the lengths).  Results are deterministic. */

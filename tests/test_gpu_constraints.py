@@ -112,3 +112,33 @@ def test_glue_bit_exact_and_follows_reorder(orc):
     after = {tuple(sorted((tuple(h["position"][a, :3]), tuple(h["position"][b, :3])))) for a, b in zip(a0, a1)}
     assert before == after
     ctx.close()
+
+
+def test_save_particle_info_files(tmp_path):
+    """save_particle_info: the reference's files, one value per particle in list order
+    (data.csv sorted by the distance to the centre), values as the state has them."""
+    from apbf_gb300.api import neighborhood_green
+
+    rng = np.random.default_rng(9)
+    pos = scenes.lattice([10, 10, 10], [10, 10, 10], 2.0, 0.2, rng)
+    st = scenes.make_state(pos)
+    ctx = _ctx(st)
+    neighborhood_green().set_data(ctx).set_range_scale(1.0).set_position_range((-8, -8, -8), (120, 120, 120),
+                                                                                5).apply()
+    g, _ = ctx.download()
+    n = g["position"].shape[0]
+    cnt = ctx.neighbors_view()["count"][:n].cpu().numpy()
+    ctx.save_particle_info(tmp_path, center=(0.0, 10.0, -60.0))
+    names = ["centerDist", "radius", "neighborCount", "kernelWidth", "targetRadius", "boundaryDistance"]
+    vals = {k: np.array([float(x) for x in (tmp_path / f"{k}.txt").read_text().split(";") if x]) for k in names}
+    p = g["position"][:, :3].astype(np.float32) / np.float32(262144.0)
+    cd = np.sqrt(np.sum((p - np.float32([0, 10, -60])) ** 2, axis=1))
+    assert all(v.size == n for v in vals.values())
+    assert np.allclose(vals["centerDist"], cd, rtol=1e-5)  # 6 significant digits
+    assert np.array_equal(vals["neighborCount"], cnt)
+    assert np.allclose(vals["radius"], g["radius"]) and np.allclose(vals["kernelWidth"], g["kernel_width"], rtol=1e-5)
+    lines = (tmp_path / "data.csv").read_text().strip().splitlines()
+    assert lines[0].startswith("center distance,boundary distance,kernel width,neighbor count")
+    d = np.array([[float(x) for x in ln.split(",")] for ln in lines[1:]])
+    assert d.shape == (n, 10) and np.all(np.diff(d[:, 0]) >= 0)
+    ctx.close()
