@@ -30,6 +30,8 @@ MAX_TRANSFERS = 10000
 MLP_PARAMS = 4824  # apbf_mlp_param_count()
 WARM_LEARNED = 1    # APBF_WARM_LEARNED
 WARM_PROJECTED = 2  # APBF_WARM_PROJECTED
+NEIGHBORHOOD_GREEN = 1  # APBF_NEIGHBORHOOD_GREEN
+NEIGHBORHOOD_BINARY_SEARCH = 3  # APBF_NEIGHBORHOOD_BINARY_SEARCH
 
 
 class ApbfError(RuntimeError):
@@ -174,6 +176,9 @@ SIGNATURES = {
     "apbf_get_lengths": (_ST, [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), _P]),
     "apbf_velocity_handling_apply": (_ST, [_P, C.c_float, _F3, _P]),
     "apbf_neighborhood_green_apply": (_ST, [_P, C.c_float, _F3, _F3, C.c_uint32, _P]),
+    "apbf_neighborhood_binary_search_apply": (_ST, [_P, C.c_float, _P]),
+    "apbf_calculate_position_code": (_ST, [_P, _P, C.c_uint32, _P, _P]),
+    "apbf_set_neighborhood_search": (_ST, [_P, C.c_int]),
     "apbf_box_collision_apply": (_ST, [_P, _P]),
     "apbf_incompressibility_apply": (_ST, [_P, _P]),
     "apbf_kernel_width_from_boundary_distance_apply": (_ST, [_P, _P]),

@@ -178,6 +178,29 @@ class Context:
                 "pass_blocks_per_sm": t.pass_blocks_per_sm, "build_tiled": t.build_tiled,
                 "filter_in_density": t.filter_in_density}
 
+    def set_neighborhood_search(self, method: int | str) -> None:
+        """The neighbour search of substep(): "green" (the default) or "binary_search",
+        or the NEIGHBORHOOD_TYPE number (shaders/cpu_gpu_shared_config.h:5)."""
+        m = {"green": N.NEIGHBORHOOD_GREEN, "binary_search": N.NEIGHBORHOOD_BINARY_SEARCH}.get(method, method)
+        N.check(self.lib.apbf_set_neighborhood_search(self.handle, int(m)), "apbf_set_neighborhood_search")
+
+    def position_codes(self, index_list: torch.Tensor | None = None, stream=None) -> torch.Tensor:
+        """calculate_position_code for the three code sections: (n, 3) uint32 words of
+        the 96-bit code of every particle (of index_list[k] when given), least
+        significant word first."""
+        n, _ = self.lengths()
+        dev = f"cuda:{self.device}"
+        out = torch.zeros((3, max(n, 1)), dtype=torch.int32, device=dev)
+        idx = None
+        if index_list is not None:
+            idx = index_list.to(device=dev, dtype=torch.int32).contiguous()
+        for w in range(3):
+            N.check(self.lib.apbf_calculate_position_code(self.handle, idx.data_ptr() if idx is not None else None, w,
+                                                          out[w].data_ptr(), _stream_handle(stream)),
+                    "apbf_calculate_position_code")
+        torch.cuda.synchronize(self.device)
+        return out[:, :n].t().contiguous()
+
     def set_tuning(self, gather_lanes: int | None = None, pass_block: int | None = None,
                    pass_blocks_per_sm: int | None = None, build_tiled: int | None = None,
                    filter_in_density: int | None = None) -> None:
@@ -444,6 +467,26 @@ class neighborhood_green:
         N.check(self.ctx.lib.apbf_neighborhood_green_apply(self.ctx.handle, C.c_float(self.range_scale), self.min_pos,
                                                            self.max_pos, self.log2res, _stream_handle(stream)),
                 "neighborhood_green.apply")
+
+
+class neighborhood_binary_search:
+    """pbd::neighborhood_binary_search (source/neighborhood_binary_search.h:8-21)."""
+
+    def __init__(self):
+        self.range_scale = 1.0
+
+    def set_data(self, ctx: Context) -> "neighborhood_binary_search":
+        self.ctx = ctx
+        return self
+
+    def set_range_scale(self, scale: float) -> "neighborhood_binary_search":
+        self.range_scale = float(scale)
+        return self
+
+    def apply(self, stream=None) -> None:
+        N.check(self.ctx.lib.apbf_neighborhood_binary_search_apply(self.ctx.handle, C.c_float(self.range_scale),
+                                                                   _stream_handle(stream)),
+                "neighborhood_binary_search.apply")
 
 
 class box_collision:

@@ -171,6 +171,8 @@ struct apbf_ctx {
     uint32_t *inv_perm = nullptr;
     uint32_t *cell_start = nullptr;
     uint32_t *cell_end = nullptr;
+    ulonglong2 *pos_code = nullptr;        // per particle: 96-bit position code {bits 0-63, bits 64-95}
+    int search_method = APBF_NEIGHBORHOOD_GREEN;  // the substep's neighbour search
 
     float *lambda = nullptr;
     int4 *shift = nullptr;
@@ -315,6 +317,7 @@ inline int32_t f2i_host(float x) {
 
 // ---- host-side stage launchers (defined in the .cu files) ----
 apbf_status emit(apbf_ctx *ctx, float dt, cudaStream_t s);  // glue.cu
+apbf_status reorder_particles(apbf_ctx *ctx, cudaStream_t s);  // neighborhood.cu: gather by ctx->perm
 apbf_status glue_remap(apbf_ctx *ctx, cudaStream_t s);      // constraints.cu: glue ids follow a reorder
 apbf_status sort_pairs_device(apbf_ctx *ctx, const uint32_t *keys_in, const uint32_t *vals_in, const uint32_t *d_count,
                               uint32_t max_count, uint32_t key_bits, uint32_t *keys_out, uint32_t *vals_out,
@@ -323,6 +326,8 @@ apbf_status prefix_sum_device(apbf_ctx *ctx, uint32_t *d_values, const uint32_t 
                               cudaStream_t s);
 apbf_status neighborhood_green(apbf_ctx *ctx, float range_scale, const float minp[3], const float maxp[3],
                                uint32_t log2res, cudaStream_t s, bool fuse_box = false);
+apbf_status neighborhood_binary_search(apbf_ctx *ctx, float range_scale, cudaStream_t s,
+                                       bool fuse_box = false);  // neighborhood_bs.cu
 apbf_status velocity_handling(apbf_ctx *ctx, float dt, const float accel[3], cudaStream_t s);
 apbf_status box_collision(apbf_ctx *ctx, cudaStream_t s);
 // feature_mode: 0 none, 1 write features + self-shift direction; acc_mode: 0 none,
@@ -519,6 +524,29 @@ __device__ __forceinline__ float3 hash31_rn(float p) {  // shadertoy 4djSRW hash
     return make_float3(fract_rn(__fmul_rn(__fadd_rn(q.x, q.y), q.z)), fract_rn(__fmul_rn(__fadd_rn(q.x, q.z), q.y)),
                        fract_rn(__fmul_rn(__fadd_rn(q.y, q.z), q.x)));
 }
+
+// Canonical search radius: floor(kw * scale * 2^18) from the FP32 inputs, clamped
+// below 2^31 (positions are int32, so no distance needs more).
+__device__ __forceinline__ long long range_fixed(float kw, float scale) {
+    double r = (double)kw * (double)scale * 262144.0;
+    if (!(r >= 0.0)) return -1;
+    if (r > 2147483647.0) r = 2147483647.0;
+    return (long long)floor(r);
+}
+
+// |b - a|^2 <= R^2 exactly.  Once every |d| <= R < 2^31 is known, each square is
+// one 32x32 -> 64-bit multiply and the sum cannot overflow 64 bits.
+__device__ __forceinline__ bool within(int4 a, int4 b, long long R) {
+    long long dx = (long long)b.x - a.x, dy = (long long)b.y - a.y, dz = (long long)b.z - a.z;
+    dx = dx < 0 ? -dx : dx;
+    dy = dy < 0 ? -dy : dy;
+    dz = dz < 0 ? -dz : dz;
+    if (dx > R || dy > R || dz > R) return false;
+    const uint32_t ux = (uint32_t)dx, uy = (uint32_t)dy, uz = (uint32_t)dz, ur = (uint32_t)R;
+    unsigned long long s = (unsigned long long)ux * ux + (unsigned long long)uy * uy + (unsigned long long)uz * uz;
+    return s <= (unsigned long long)ur * ur;
+}
+
 
 // box_collision.comp:35-57 on one box in the box's own frame: (qx, qy, qz) is the
 // particle position relative to the frame, [lo, hi] the box; the box is grown by the

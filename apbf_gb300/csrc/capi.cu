@@ -165,6 +165,7 @@ apbf_status apbf_create(const apbf_config *cfg, apbf_ctx **out) {
     const size_t ncells = (size_t)1 << (3 * cfg->max_log2res);
     A(ctx->cell_start, ncells);
     A(ctx->cell_end, ncells);
+    A(ctx->pos_code, cap);
     ctx->n_cells_log2_alloc = cfg->max_log2res;
     A(ctx->lambda, cap);
     A(ctx->shift, cap);
@@ -460,7 +461,10 @@ apbf_status substep_body(apbf_ctx *ctx, float dt, cudaStream_t s, bool capture) 
     // update of the previous iteration for the others.
     const bool spread = adaptive && !st.base_kernel_width_on_boundary_distance;
     const bool fuse_first = st.solver_iterations > 0 && !spread;
-    r = neighborhood_green(ctx, scale, ctx->scene.min_pos, ctx->scene.max_pos, ctx->scene.log2res, s, fuse_first);
+    if (ctx->search_method == APBF_NEIGHBORHOOD_BINARY_SEARCH)
+        r = neighborhood_binary_search(ctx, scale, s, fuse_first);
+    else
+        r = neighborhood_green(ctx, scale, ctx->scene.min_pos, ctx->scene.max_pos, ctx->scene.log2res, s, fuse_first);
     if (r != APBF_OK) return r;
     if (spread) {
         r = spread_kernel_width(ctx, s);

@@ -97,28 +97,6 @@ __global__ void k_cell_ranges(const uint32_t *__restrict__ skeys, const uint32_t
     }
 }
 
-// Canonical search radius: floor(kw * scale * 2^18) from the FP32 inputs, clamped
-// below 2^31 (positions are int32, so no distance needs more).
-__device__ __forceinline__ long long range_fixed(float kw, float scale) {
-    double r = (double)kw * (double)scale * 262144.0;
-    if (!(r >= 0.0)) return -1;
-    if (r > 2147483647.0) r = 2147483647.0;
-    return (long long)floor(r);
-}
-
-// |b - a|^2 <= R^2 exactly.  Once every |d| <= R < 2^31 is known, each square is
-// one 32x32 -> 64-bit multiply and the sum cannot overflow 64 bits.
-__device__ __forceinline__ bool within(int4 a, int4 b, long long R) {
-    long long dx = (long long)b.x - a.x, dy = (long long)b.y - a.y, dz = (long long)b.z - a.z;
-    dx = dx < 0 ? -dx : dx;
-    dy = dy < 0 ? -dy : dy;
-    dz = dz < 0 ? -dz : dz;
-    if (dx > R || dy > R || dz > R) return false;
-    const uint32_t ux = (uint32_t)dx, uy = (uint32_t)dy, uz = (uint32_t)dz, ur = (uint32_t)R;
-    unsigned long long s = (unsigned long long)ux * ux + (unsigned long long)uy * uy + (unsigned long long)uz * uz;
-    return s <= (unsigned long long)ur * ur;
-}
-
 // Exact 32-bit form of `within` for particles that both lie inside the grid
 // (coordinates differ by less than 2^31): the same predicate, half the
 // instructions.  R2 = R * R.
@@ -589,6 +567,25 @@ void swap_all(apbf_ctx *ctx) { ctx->fcur ^= 1; }
 
 }  // namespace
 
+// Gathers every particle attribute in the order ctx->perm gives (new id -> old id),
+// remaps the transfer and glue lists, and makes the gathered set current.
+apbf_status reorder_particles(apbf_ctx *ctx, cudaStream_t s) {
+    const uint32_t cap = ctx->cfg.particle_capacity;
+    FluidBufs &cur = ctx->fl[ctx->fcur];
+    FluidBufs &alt = ctx->fl[ctx->fcur ^ 1];
+    APBF_BEFORE_LAUNCH(ctx, s, "k_reorder");
+    k_reorder<<<grid_for(ctx, cap), kBlock, 0, s>>>(cur, alt, ctx->perm, ctx->inv_perm, ctx->d_len);
+    APBF_AFTER_LAUNCH(ctx, s, "k_reorder");
+    APBF_BEFORE_LAUNCH(ctx, s, "k_remap_transfers");
+    k_remap_transfers<<<grid_for(ctx, ctx->cfg.transfer_capacity), kBlock, 0, s>>>(ctx->tr[ctx->tcur], ctx->inv_perm,
+                                                                                    ctx->d_len, ctx->status);
+    APBF_AFTER_LAUNCH(ctx, s, "k_remap_transfers");
+    apbf_status r = glue_remap(ctx, s);
+    if (r != APBF_OK) return r;
+    swap_all(ctx);
+    return APBF_OK;
+}
+
 apbf_status neighborhood_green(apbf_ctx *ctx, float range_scale, const float minp[3], const float maxp[3],
                                uint32_t L, cudaStream_t s, bool fuse_box) {
     if (L < 1 || L > ctx->cfg.max_log2res || L > 10) {
@@ -607,15 +604,8 @@ apbf_status neighborhood_green(apbf_ctx *ctx, float range_scale, const float min
     apbf_status r = sort_pairs_device(ctx, ctx->keys[0], ctx->vals[0], ctx->d_len + kLenParticles, cap, 3u * L,
                                       ctx->sorted_keys, ctx->perm, s);
     if (r != APBF_OK) return r;
-    k_reorder<<<g, kBlock, 0, s>>>(cur, alt, ctx->perm, ctx->inv_perm, ctx->d_len);
-    APBF_AFTER_LAUNCH(ctx, s, "k_reorder");
-    APBF_BEFORE_LAUNCH(ctx, s, "k_remap_transfers");
-    k_remap_transfers<<<grid_for(ctx, ctx->cfg.transfer_capacity), kBlock, 0, s>>>(ctx->tr[ctx->tcur], ctx->inv_perm,
-                                                                                    ctx->d_len, ctx->status);
-    APBF_AFTER_LAUNCH(ctx, s, "k_remap_transfers");
-    r = glue_remap(ctx, s);
+    r = reorder_particles(ctx, s);
     if (r != APBF_OK) return r;
-    swap_all(ctx);
     FluidBufs &f = ctx->fl[ctx->fcur];
 
     const size_t ncells = (size_t)1 << (3 * L);

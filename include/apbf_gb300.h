@@ -240,6 +240,25 @@ apbf_status apbf_velocity_handling_apply(apbf_ctx *ctx, float dt, const float ac
  * (source/neighborhood_green.h:11-14, source/neighborhood_green.cpp:27-77). */
 apbf_status apbf_neighborhood_green_apply(apbf_ctx *ctx, float range_scale, const float min_pos[3],
                                           const float max_pos[3], uint32_t log2res, void *stream);
+/* neighborhood_binary_search::set_range_scale / apply
+ * (source/neighborhood_binary_search.h:11-12, source/neighborhood_binary_search.cpp:22-75):
+ * sorts the particles by the 96-bit interleave of their raw coordinates and builds
+ * each particle's row from the 27 cells of edge 2^k around its own cell, k the
+ * smallest level with 2^k >= its search radius.  The rows hold the same neighbours
+ * as apbf_neighborhood_green_apply's (the particle order differs); a row lists its
+ * cells in the reference's order, x fastest, each cell in ascending index. */
+apbf_status apbf_neighborhood_binary_search_apply(apbf_ctx *ctx, float range_scale, void *stream);
+/* shader_provider::calculate_position_code (source/shader_provider.h:47,
+ * calculate_position_code.comp:22-72): d_out[k] = 32-bit word code_section (0..2)
+ * of the 96-bit code of particle d_index_list[k] (of particle k when d_index_list
+ * is NULL), for every k below the particle count. */
+apbf_status apbf_calculate_position_code(apbf_ctx *ctx, const uint32_t *d_index_list, uint32_t code_section,
+                                         uint32_t *d_out, void *stream);
+/* The neighbour search of apbf_substep, numbered as NEIGHBORHOOD_TYPE
+ * (shaders/cpu_gpu_shared_config.h:5): Green (the default) or binary search. */
+#define APBF_NEIGHBORHOOD_GREEN 1
+#define APBF_NEIGHBORHOOD_BINARY_SEARCH 3
+apbf_status apbf_set_neighborhood_search(apbf_ctx *ctx, int method);
 /* box_collision::apply (source/box_collision.cpp:12-24). */
 apbf_status apbf_box_collision_apply(apbf_ctx *ctx, void *stream);
 /* incompressibility::apply, one Jacobi iteration (source/incompressibility.cpp:12-45). */

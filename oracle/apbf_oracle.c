@@ -385,6 +385,109 @@ uint64_t or_neighborhood_green(or_fluid *f, or_transfers *t, float range_scale, 
 }
 
 /* ------------------------------------------------------------------ */
+/* neighborhood_binary_search (neighborhood_binary_search.cpp:22-75)  */
+/* ------------------------------------------------------------------ */
+/* calculate_position_code.comp:22-62: code bit 3b + a is bit b of axis a, the
+ * coordinates taken as uint32; out[0] holds code bits 0-31, out[2] bits 64-95. */
+void or_position_code96(const int32_t *p, uint32_t out[3]) {
+    out[0] = out[1] = out[2] = 0;
+    for (uint32_t b = 0; b < 32; ++b)
+        for (uint32_t a = 0; a < 3; ++a) {
+            uint32_t bit = 3u * b + a;
+            if (((uint32_t)p[a] >> b) & 1u) out[bit / 32u] |= 1u << (bit % 32u);
+        }
+}
+
+static int cmp96(const uint32_t *a, const uint32_t *b) {
+    for (int w = 2; w >= 0; --w)
+        if (a[w] != b[w]) return a[w] < b[w] ? -1 : 1;
+    return 0;
+}
+
+/* neighborhood_binary_search.comp:186-275 with the canonical rules: level k the
+ * smallest with 2^k >= R; cells visited in the shader's order (x fastest, offsets
+ * -1, 0, +1; at k = 31 the offset +1 equals -1 and is skipped); each cell is the run
+ * of sorted codes in [corner code, corner code | low 3k bits]; exact predicate. */
+uint64_t or_neighbors_binary_search(const int32_t *pos4, const uint32_t *codes3, const float *range,
+                                    float range_scale, size_t n, or_neighbors *nb) {
+    uint64_t total = 0;
+    int write = 1;
+    nb->n = (uint32_t)n;
+    nb->offsets[0] = 0;
+    for (size_t i = 0; i < n; ++i) {
+        const int32_t *p = pos4 + 4 * i;
+        int64_t R = or_range_fixed(range[i], range_scale);
+        if (R >= 0) {
+            uint32_t k = 0;
+            while (((uint64_t)1 << k) < (uint64_t)R) ++k;
+            uint32_t nd = k == 31 ? 2u : 3u;
+            for (uint32_t dz = 0; dz < nd; ++dz)
+                for (uint32_t dy = 0; dy < nd; ++dy)
+                    for (uint32_t dx = 0; dx < nd; ++dx) {
+                        uint32_t d[3] = {dx, dy, dz};
+                        int32_t corner[3], top[3];
+                        for (int a = 0; a < 3; ++a) {
+                            uint64_t c = (((uint64_t)((uint32_t)p[a] >> k) + d[a] + 0xffffffffull) << k) & 0xffffffffull;
+                            uint64_t low = k ? (((uint64_t)1 << k) - 1) : 0;
+                            corner[a] = (int32_t)(uint32_t)c;
+                            top[a] = (int32_t)(uint32_t)(c | low);
+                        }
+                        uint32_t first[3], last[3];
+                        or_position_code96(corner, first);
+                        or_position_code96(top, last);
+                        /* lower bound: first j with code >= first */
+                        size_t lo = 0, hi = n;
+                        while (lo < hi) {
+                            size_t mid = (lo + hi) / 2;
+                            if (cmp96(codes3 + 3 * mid, first) < 0) lo = mid + 1; else hi = mid;
+                        }
+                        for (size_t j = lo; j < n && cmp96(codes3 + 3 * j, last) <= 0; ++j) {
+                            if (j == i || !within(p, pos4 + 4 * j, R)) continue;
+                            if (total >= nb->cap) write = 0;
+                            if (write) nb->idx[total] = (uint32_t)j;
+                            ++total;
+                        }
+                    }
+        }
+        if (write) nb->offsets[i + 1] = (uint32_t)total;
+    }
+    return total;
+}
+
+/* neighborhood_binary_search::apply: codes, stable sort by the 96-bit code (three
+ * stable passes, least significant word first), reorder, codes of the sorted list,
+ * rows.  perm_out / codes_out (may be NULL) receive the permutation and the sorted
+ * codes (3 words per particle). */
+uint64_t or_neighborhood_binary_search(or_fluid *f, or_transfers *t, float range_scale, or_neighbors *nb,
+                                       uint32_t *perm_out, uint32_t *codes_out) {
+    size_t n = f->n, m = n ? n : 1;
+    uint32_t *codes = (uint32_t *)malloc(m * 3 * sizeof(uint32_t));
+    uint32_t *keys = (uint32_t *)malloc(m * sizeof(uint32_t));
+    uint32_t *vals = (uint32_t *)malloc(m * sizeof(uint32_t));
+    uint32_t *skeys = (uint32_t *)malloc(m * sizeof(uint32_t));
+    uint32_t *perm = (uint32_t *)malloc(m * sizeof(uint32_t));
+    for (size_t i = 0; i < n; ++i) {
+        or_position_code96(f->pos + 4 * i, codes + 3 * i);
+        perm[i] = (uint32_t)i;
+    }
+    for (int w = 0; w < 3; ++w) {
+        for (size_t k = 0; k < n; ++k) {
+            keys[k] = codes[3 * (size_t)perm[k] + (size_t)w];
+            vals[k] = perm[k];
+        }
+        or_sort_pairs_stable(keys, vals, n, skeys, perm);
+    }
+    fluid_apply_edit(f, perm, (uint32_t)n);
+    transfers_remap(t, perm, (uint32_t)n, (uint32_t)n);
+    for (size_t i = 0; i < n; ++i) or_position_code96(f->pos + 4 * i, codes + 3 * i);
+    uint64_t total = or_neighbors_binary_search(f->pos, codes, f->kernel_width, range_scale, n, nb);
+    if (perm_out) memcpy(perm_out, perm, n * sizeof(uint32_t));
+    if (codes_out) memcpy(codes_out, codes, n * 3 * sizeof(uint32_t));
+    free(codes); free(keys); free(vals); free(skeys); free(perm);
+    return total;
+}
+
+/* ------------------------------------------------------------------ */
 /* smoothing kernels (kernels.glsl), FP64                              */
 /* ------------------------------------------------------------------ */
 static double dot3(const double a[3], const double b[3]) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
@@ -1228,7 +1331,9 @@ uint64_t or_substep(or_fluid *f, or_transfers *t, or_neighbors *nb, const or_box
     if (!s->basic_pbf && (s->merge || s->split)) or_particle_transfer(f, t, dt);
     if (!s->basic_pbf && s->base_kernel_width_on_boundary_distance) or_kernel_width_from_boundary_distance(f, s);
     float scale = (s->basic_pbf || s->base_kernel_width_on_boundary_distance) ? 1.0f : 1.5f;
-    uint64_t pairs = or_neighborhood_green(f, t, scale, sc->minp, sc->maxp, sc->log2res, nb, NULL, NULL);
+    uint64_t pairs = sc->search_method == 3 ? or_neighborhood_binary_search(f, t, scale, nb, NULL, NULL)
+                                            : or_neighborhood_green(f, t, scale, sc->minp, sc->maxp, sc->log2res, nb,
+                                                                    NULL, NULL);
     if (pairs > nb->cap) return pairs;
     if (!s->basic_pbf && !s->base_kernel_width_on_boundary_distance) or_spread_kernel_width(f, nb, s);
     for (int it = 0; it < s->solver_iterations; ++it) {

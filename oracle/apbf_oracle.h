@@ -154,6 +154,13 @@ uint64_t or_neighbors_brute(const int32_t *pos4, const float *range, float range
 uint64_t or_neighborhood_green(or_fluid *f, or_transfers *t, float range_scale, const float minp[3],
                                const float maxp[3], uint32_t log2res, or_neighbors *nb,
                                uint32_t *perm_out, uint32_t *keys_out);
+/* neighborhood_binary_search (calculate_position_code.comp, neighborhood_binary_search.comp):
+ * the 96-bit position code, the rows over a sorted code list, and the whole apply. */
+void or_position_code96(const int32_t *p, uint32_t out[3]);
+uint64_t or_neighbors_binary_search(const int32_t *pos4, const uint32_t *codes3, const float *range,
+                                    float range_scale, size_t n, or_neighbors *nb);
+uint64_t or_neighborhood_binary_search(or_fluid *f, or_transfers *t, float range_scale, or_neighbors *nb,
+                                       uint32_t *perm_out, uint32_t *codes_out);
 
 /* ---- smoothing kernels (kernels.glsl) ---- */
 double or_kernel_height(int id, const double r[3], double kw);
@@ -232,6 +239,7 @@ typedef struct or_scene {
     float accel[3];
     float last_dt;
     uint32_t max_transfers;
+    uint32_t search_method; /* NEIGHBORHOOD_TYPE numbering: 3 binary search, else Green */
 } or_scene;
 uint64_t or_substep(or_fluid *f, or_transfers *t, or_neighbors *nb, const or_boxes *b, or_scene *sc, float dt);
 

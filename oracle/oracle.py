@@ -103,6 +103,7 @@ class OrScene(C.Structure):
         ("accel", C.c_float * 3),
         ("last_dt", C.c_float),
         ("max_transfers", C.c_uint32),
+        ("search_method", C.c_uint32),
     ]
 
 
@@ -125,6 +126,8 @@ def lib() -> C.CDLL:
         L.or_neighbors_build.restype = C.c_uint64
         L.or_neighbors_brute.restype = C.c_uint64
         L.or_neighborhood_green.restype = C.c_uint64
+        L.or_neighborhood_binary_search.restype = C.c_uint64
+        L.or_neighbors_binary_search.restype = C.c_uint64
         L.or_substep.restype = C.c_uint64
         L.or_cell_coord.restype = C.c_uint32
         L.or_cell_coord.argtypes = [C.c_int64, C.c_int64, C.c_int64, C.c_uint32]
@@ -291,6 +294,28 @@ def neighborhood_green(fs: FluidState, range_scale: float, minp, maxp, log2res: 
     return perm[:fs.n], keys[:fs.n], int(tot)
 
 
+def position_codes(pos4: np.ndarray) -> np.ndarray:
+    """The 96-bit position code of every particle as 3 uint32 words (least significant first)."""
+    p = np.ascontiguousarray(pos4, np.int32)
+    out = np.zeros((p.shape[0], 3), np.uint32)
+    for i in range(p.shape[0]):
+        lib().or_position_code96(_p(p[i], _i32p), _p(out[i], _u32p))
+    return out
+
+
+def neighborhood_binary_search(fs: FluidState, range_scale: float, cap_pairs: int):
+    """neighborhood_binary_search::apply on the oracle state: (permutation, sorted
+    codes (n x 3 words), pair count); the rows land in the state."""
+    nb = fs.alloc_neighbors(cap_pairs)
+    perm = np.zeros(max(fs.n, 1), np.uint32)
+    codes = np.zeros((max(fs.n, 1), 3), np.uint32)
+    tot = lib().or_neighborhood_binary_search(C.byref(fs.f), C.byref(fs.t), C.c_float(range_scale), C.byref(nb),
+                                              _p(perm, _u32p), _p(codes, _u32p))
+    if tot > cap_pairs:
+        raise RuntimeError(f"oracle neighbour capacity {cap_pairs} < {tot}")
+    return perm[:fs.n], codes[:fs.n], int(tot)
+
+
 def set_rows(fs: FluidState, rows: list) -> None:
     """Installs neighbour rows (e.g. the device's, for lockstep stage checks)."""
     total = sum(len(r) for r in rows)
@@ -414,8 +439,10 @@ def substep(fs: FluidState, scene: OrScene, boxes: tuple, dt: float, cap_pairs: 
     return int(tot)
 
 
-def make_scene(settings: OrSettings, minp, maxp, log2res: int, accel, max_transfers: int = 10000) -> OrScene:
+def make_scene(settings: OrSettings, minp, maxp, log2res: int, accel, max_transfers: int = 10000,
+               search_method: int = 1) -> OrScene:
     sc = OrScene()
+    sc.search_method = search_method
     sc.settings = settings
     sc.minp = (C.c_float * 3)(*minp)
     sc.maxp = (C.c_float * 3)(*maxp)
