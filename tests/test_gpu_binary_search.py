@@ -47,7 +47,7 @@ def test_binary_search_parity(orc, seed, lo, hi, kw_lo, kw_hi, dups, scale):
     n = st["position"].shape[0]
     transfers = {"source": np.arange(0, 400, 2, dtype=np.uint32), "target": np.arange(1, 401, 2, dtype=np.uint32),
                  "time_left": np.linspace(0.1, 1.0, 200).astype(np.float32)}
-    ctx = _ctx(n, maxn=512)
+    ctx = _ctx(n, maxn=1024)  # radii up to 7.5 at 0.44 particles per unit volume: up to ~830 neighbours
     ctx.upload(st, transfers)
     neighborhood_binary_search().set_data(ctx).set_range_scale(scale).apply()
     info = ctx.check_status()
