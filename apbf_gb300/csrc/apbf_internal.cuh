@@ -66,7 +66,8 @@ struct Status {
     uint32_t pass_index;           // solve loop graph: index of the first pass of the current body run
     uint32_t loop_iters;           // solve loop graph: body runs since the context was created
     uint32_t filter_tag;           // 1: this pass's density kernel left the boundariness filter to k_delta
-    uint32_t pad2[3];
+    uint32_t kw_uniform;           // 1: every kernel width of this density pass had the same bits
+    uint32_t pad2[2];
 };
 
 // Device length block.
@@ -177,6 +178,7 @@ struct apbf_ctx {
     float *lambda = nullptr;
     int4 *shift = nullptr;
     float4 *solve_rec = nullptr;   // per particle: lambda, Gauss constants (ivd, norm), kernel width
+    int4 *solve_pk = nullptr;      // per particle: position (xyz) and applied lambda (w, float bits)
     int4 *filt = nullptr;          // per particle: gradient sum and boundariness > 0, for the deferred filter
     // learned warm start
     float *mlp_params = nullptr;   // FP32 parameter vector (mlp.cu)
@@ -593,10 +595,31 @@ __device__ __forceinline__ float dot3_rn(float4 a, float x, float y, float z) {
     return __fadd_rn(__fadd_rn(__fmul_rn(a.x, x), __fmul_rn(a.y, y)), __fmul_rn(a.z, z));
 }
 
+// True when push_out cannot move a particle at q whatever the jitter: some axis d
+// has q_d < fl(fl(lo_d - r) - c) or q_d >= fl(fl(hi_d + r) + c), c = 0.0500001 >=
+// every 0.05 * h with h in [0, 1).  Rounding is monotone, so then q_d <= the
+// jittered lower threshold (or >= the upper one), the selected component of
+// -toMin (toMax) is <= 0 and push_out returns false.  Only for finite thresholds
+// below 1e30, where every component push_out forms is finite.
+__device__ __forceinline__ bool box_clear(float qx, float qy, float qz, float3 lo, float3 hi, float r) {
+    const float c = 0.0500001f;
+    const float b0x = __fsub_rn(__fsub_rn(lo.x, r), c), b0y = __fsub_rn(__fsub_rn(lo.y, r), c),
+                b0z = __fsub_rn(__fsub_rn(lo.z, r), c);
+    const float b1x = __fadd_rn(__fadd_rn(hi.x, r), c), b1y = __fadd_rn(__fadd_rn(hi.y, r), c),
+                b1z = __fadd_rn(__fadd_rn(hi.z, r), c);
+    const float m = fmaxf(fmaxf(fmaxf(fabsf(b0x), fabsf(b0y)), fmaxf(fabsf(b0z), fabsf(b1x))),
+                          fmaxf(fabsf(b1y), fabsf(b1z)));
+    if (!(m < 1.0e30f)) return false;
+    return qx < b0x || qy < b0y || qz < b0z || qx >= b1x || qy >= b1y || qz >= b1z;
+}
+
 // Pushes one particle (sorted id `id`, radius r) out of every box.  Box k is
 // axis-aligned ([bmin, bmax], as in the reference) unless rot[3k].w != 0: then it
 // is oriented, bmin = its centre, bmax = its half extents and rot[3k..3k+2] the
 // rows of its rotation (local axis i = row i), and the same push runs in its frame.
+// The jitter hashes depend only on the id and the current position: they are
+// computed for the first box that may push and kept until a push moves the particle,
+// and boxes that box_clear rules out skip them (same results, box by box).
 __device__ __forceinline__ int4 box_push(int4 ip, float r, uint32_t id, const float4 *__restrict__ bmin,
                                          const float4 *__restrict__ bmax, const float4 *__restrict__ rot,
                                          uint32_t nb) {
@@ -604,20 +627,34 @@ __device__ __forceinline__ int4 box_push(int4 ip, float r, uint32_t id, const fl
     float px = __fdiv_rn((float)ip.x, 262144.0f), py = __fdiv_rn((float)ip.y, 262144.0f),
           pz = __fdiv_rn((float)ip.z, 262144.0f);
     const float fid = (float)id;
+    float3 h1 = make_float3(0.f, 0.f, 0.f), h2 = h1;
+    bool have = false;
     for (uint32_t k = 0; k < nb; ++k) {
-        const float3 h1 = hash31_rn(__fsub_rn(__fsub_rn(__fmul_rn(fid, px), py), pz));
-        const float3 h2 = hash31_rn(__fadd_rn(__fadd_rn(__fmul_rn(fid, py), px), pz));
         const float4 lo = bmin[k], hi = bmax[k];
         const float4 r0 = rot[3 * k];
         if (r0.w == 0.0f) {
-            push_out(px, py, pz, make_float3(lo.x, lo.y, lo.z), make_float3(hi.x, hi.y, hi.z), r, h1, h2);
+            const float3 l3 = make_float3(lo.x, lo.y, lo.z), u3 = make_float3(hi.x, hi.y, hi.z);
+            if (box_clear(px, py, pz, l3, u3, r)) continue;
+            if (!have) {
+                h1 = hash31_rn(__fsub_rn(__fsub_rn(__fmul_rn(fid, px), py), pz));
+                h2 = hash31_rn(__fadd_rn(__fadd_rn(__fmul_rn(fid, py), px), pz));
+                have = true;
+            }
+            if (push_out(px, py, pz, l3, u3, r, h1, h2)) have = false;
             continue;
         }
         const float4 r1 = rot[3 * k + 1], r2 = rot[3 * k + 2];
         const float dx = __fsub_rn(px, lo.x), dy = __fsub_rn(py, lo.y), dz = __fsub_rn(pz, lo.z);
         float qx = dot3_rn(r0, dx, dy, dz), qy = dot3_rn(r1, dx, dy, dz), qz = dot3_rn(r2, dx, dy, dz);
-        if (!push_out(qx, qy, qz, make_float3(-hi.x, -hi.y, -hi.z), make_float3(hi.x, hi.y, hi.z), r, h1, h2))
-            continue;
+        const float3 nh = make_float3(-hi.x, -hi.y, -hi.z), u3 = make_float3(hi.x, hi.y, hi.z);
+        if (box_clear(qx, qy, qz, nh, u3, r)) continue;
+        if (!have) {
+            h1 = hash31_rn(__fsub_rn(__fsub_rn(__fmul_rn(fid, px), py), pz));
+            h2 = hash31_rn(__fadd_rn(__fadd_rn(__fmul_rn(fid, py), px), pz));
+            have = true;
+        }
+        if (!push_out(qx, qy, qz, nh, u3, r, h1, h2)) continue;
+        have = false;
         // back to the world frame: p = centre + R^T q
         px = __fadd_rn(lo.x, __fadd_rn(__fadd_rn(__fmul_rn(r0.x, qx), __fmul_rn(r1.x, qy)), __fmul_rn(r2.x, qz)));
         py = __fadd_rn(lo.y, __fadd_rn(__fadd_rn(__fmul_rn(r0.y, qx), __fmul_rn(r1.y, qy)), __fmul_rn(r2.y, qz)));

@@ -170,6 +170,7 @@ apbf_status apbf_create(const apbf_config *cfg, apbf_ctx **out) {
     A(ctx->lambda, cap);
     A(ctx->shift, cap);
     A(ctx->solve_rec, cap);
+    A(ctx->solve_pk, cap);
     A(ctx->filt, cap);
     A(ctx->mlp_params, kMlpParams);
     A(ctx->features, (size_t)cap * 8);
@@ -190,7 +191,7 @@ apbf_status apbf_create(const apbf_config *cfg, apbf_ctx **out) {
     A(ctx->list_a, cap);
     A(ctx->list_b, cap);
     ctx->red_blocks = grid_for(ctx, cap, kBlock, 8);
-    A(ctx->red_partials, (size_t)4 * ctx->red_blocks);
+    A(ctx->red_partials, (size_t)6 * ctx->red_blocks);
     A(ctx->red_out, 4);
     A(ctx->box_min, APBF_MAX_BOXES);
     A(ctx->box_max, APBF_MAX_BOXES);
@@ -471,7 +472,9 @@ apbf_status substep_body(apbf_ctx *ctx, float dt, cudaStream_t s, bool capture) 
         if (r != APBF_OK) return r;
     }
     const bool converge = st.density_error_target > 0.0f;
-    if (converge) APBF_CUDA(cudaMemsetAsync(&ctx->status->converged, 0, sizeof(uint32_t), s));
+    // cleared even without a target: the solve loop graph's condition reads it, and a
+    // flag left by an earlier substep that had a target would end the loop early
+    APBF_CUDA(cudaMemsetAsync(&ctx->status->converged, 0, sizeof(uint32_t), s));
     const bool recording = ctx->rec_iterations > 0;
     const bool learned = (ctx->warm_start & APBF_WARM_LEARNED) && ctx->mlp_loaded;
     const bool projected = (ctx->warm_start & APBF_WARM_PROJECTED) != 0;

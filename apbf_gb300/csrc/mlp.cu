@@ -204,7 +204,8 @@ __global__ void __launch_bounds__(kRowsCta) k_mlp_forward(const float *__restric
 // density pass replaces the plain lambda in the solve record and in the self
 // shift (incompressibility_2.comp:106-109 with lambda_hat).
 __global__ void __launch_bounds__(kRowsCta) k_mlp_lambda(const float *__restrict__ P, const float *__restrict__ X,
-                                                          const float4 *__restrict__ selfdir, float4 *rec, int4 *shift,
+                                                          const float4 *__restrict__ selfdir, float4 *rec, int4 *pk,
+                                                          int4 *shift,
                                                           const uint32_t *d_len, const Status *st, int early_exit) {
     if (early_exit && *(volatile const uint32_t *)&st->converged) return;
     __shared__ SmemW w;
@@ -232,6 +233,7 @@ __global__ void __launch_bounds__(kRowsCta) k_mlp_lambda(const float *__restrict
                 float4 rc = rec[r];
                 rc.x = lam;
                 rec[r] = rc;
+                pk[r].w = __float_as_int(lam);
                 const float4 sd = selfdir[r];  // selfGrad (xyz), inverse mass (w)
                 int4 sh = make_int4(0, 0, 0, 0);
                 if (lam < 0.0f) {
@@ -521,7 +523,7 @@ apbf_status mlp_lambda(apbf_ctx *ctx, cudaStream_t s, bool early_exit) {
     const uint32_t ctas = (cap + kRowsCta - 1) / kRowsCta;
     APBF_BEFORE_LAUNCH(ctx, s, "k_mlp_lambda");
     k_mlp_lambda<<<ctas < 2048u ? ctas : 2048u, kRowsCta, 0, s>>>(ctx->mlp_params, ctx->features, ctx->selfdir,
-                                                                  ctx->solve_rec, ctx->shift, ctx->d_len,
+                                                                  ctx->solve_rec, ctx->solve_pk, ctx->shift, ctx->d_len,
                                                                   ctx->status, early_exit ? 1 : 0);
     APBF_AFTER_LAUNCH(ctx, s, "k_mlp_lambda");
     return APBF_OK;

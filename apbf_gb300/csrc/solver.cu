@@ -7,7 +7,8 @@
 //    squared-gradient sums, as 2^18 fixed-point integers) + incompressibility_2.comp
 //    (lambda, boundariness, self shift) + the boundariness filter of
 //    incompressibility_3.comp:41-46,60.  Writes lambda, the self shift, the
-//    per-particle Gauss constants and the FP64 density-error partials.
+//    per-particle Gauss constants and the density-error partials (64-bit
+//    fixed-point integers, turned into the FP64 mean by the last block).
 //  k_delta (particle j, over the particles whose rows contain j):
 //    incompressibility_3.comp:62-66 as a gather: x_j += sum_i int(gradW_ij * lambda_i * 2^18)
 //    plus the self shift, into the other position buffer.
@@ -60,10 +61,11 @@ struct PassA {
     float *lambda;
     int4 *shift;
     float4 *rec;  // per particle: lambda, Gauss ivd, Gauss norm, kernel width (read by k_delta)
+    int4 *pk;     // per particle: position xyz and the applied lambda (read by k_delta when widths are uniform)
     uint32_t *dbg_dens;
     int4 *dbg_grad;
     uint32_t *dbg_sq;
-    double *partials;
+    long long *partials;  // per block: the two error sums in 2^-24 fixed point, kernel-width bits min << 32 | max
     const uint32_t *d_len;
     Status *st;
     double *red_out;     // [2], [3]: mean compression / absolute error of this pass
@@ -119,6 +121,56 @@ __device__ __forceinline__ void block_sum2(const double *partials, int blocks, d
     t2 = s2[0];
 }
 
+// Mean density error terms: per particle in 2^-24 fixed point (the FP32 ratio
+// times 2^24 is exact; ratios of 128 and more saturate), summed as 64-bit
+// integers.  Integer sums are order-free, so the mean is deterministic without
+// FP64 arithmetic per particle (GB300's FP64 pipe is a small fraction of its FP32
+// rate).  NaN counts as saturated, so a NaN state never converges.
+constexpr float kErrScale = 16777216.0f;
+__device__ __forceinline__ long long err_fix(float x) {
+    return x != x ? 0x7fffffffll : (long long)__float2int_rn(__fmul_rn(x, kErrScale));
+}
+
+// Sums of the per-block integer error partials and the min / max of the
+// per-block kernel-width bits (partials of three words per block).
+__device__ __forceinline__ void block_reduce_partials(const long long *partials, int blocks, long long &t1,
+                                                      long long &t2, uint32_t &kmin, uint32_t &kmax) {
+    __shared__ long long s1[32], s2[32];
+    __shared__ uint32_t s3[32], s4[32];
+    long long a = 0, b = 0;
+    uint32_t lo = 0xffffffffu, hi = 0u;
+    for (int k = threadIdx.x; k < blocks; k += blockDim.x) {
+        a += ((volatile const long long *)partials)[3 * k];
+        b += ((volatile const long long *)partials)[3 * k + 1];
+        const unsigned long long w = (unsigned long long)((volatile const long long *)partials)[3 * k + 2];
+        lo = min(lo, (uint32_t)(w >> 32));
+        hi = max(hi, (uint32_t)w);
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, off);
+        b += __shfl_down_sync(0xffffffffu, b, off);
+    }
+    lo = __reduce_min_sync(0xffffffffu, lo);
+    hi = __reduce_max_sync(0xffffffffu, hi);
+    if ((threadIdx.x & 31) == 0) {
+        s1[threadIdx.x >> 5] = a;
+        s2[threadIdx.x >> 5] = b;
+        s3[threadIdx.x >> 5] = lo;
+        s4[threadIdx.x >> 5] = hi;
+    }
+    __syncthreads();
+    t1 = 0;
+    t2 = 0;
+    kmin = 0xffffffffu;
+    kmax = 0u;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+        t1 += s1[k];
+        t2 += s2[k];
+        kmin = min(kmin, s3[k]);
+        kmax = max(kmax, s4[k]);
+    }
+}
+
 constexpr int kUnroll = 4;
 
 // L threads per particle ("lanes"): lane s of a particle's group takes row
@@ -138,7 +190,9 @@ __device__ __forceinline__ int32_t group_wsum(int32_t v) {
     return v;
 }
 
-template <bool GAUSS, int L>
+// XTRA: the warm-start features or the centre-of-mass boundariness sums
+// (method 1) are gathered too; the common pass is compiled without them.
+template <bool GAUSS, int L, bool XTRA>
 __global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) {
     const bool skip = (a.early_exit && *(volatile uint32_t *)&a.st->converged) ||
                       (a.loop_offset >= 0 && a.st->pass_index + (uint32_t)a.loop_offset >= a.max_passes);
@@ -148,9 +202,11 @@ __global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) 
     if (blockIdx.x == 0 && threadIdx.x == 0) a.st->filter_tag = (!skip && defer) ? 1u : 0u;
     if (skip) return;  // uniform over the grid
     const uint32_t n = a.d_len[kLenParticles];
-    const uint32_t sub = threadIdx.x % L, gpb = blockDim.x / L;
-    double e1 = 0.0, e2 = 0.0;
+    const uint32_t sub = threadIdx.x % L;
+    long long e1 = 0, e2 = 0;
+    uint32_t kwlo = 0xffffffffu, kwhi = 0u;  // kernel-width bits seen by this thread
     // the block iterates as a whole (uniform trip count: the group shuffles need every lane)
+    const uint32_t gpb = blockDim.x / L;
     for (uint32_t base = blockIdx.x * gpb; base < n; base += gridDim.x * gpb) {
         const uint32_t i_raw = base + threadIdx.x / L;
         const bool valid = i_raw < n;
@@ -163,8 +219,12 @@ __global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) 
         uint32_t sq = 0;
         int32_t cx = 0, cy = 0, cz = 0, cw = 0;
         const uint32_t cnt = valid ? a.count[i] : 0u;
+        // loaded with the particle's other data, so that they are not one more round
+        // trip after the neighbour loop
+        const float im = a.inv_mass[i], radius = a.radius[i];
+        float b = a.bness[i];
         const uint32_t *row = a.idx + i;
-        const bool feat = a.features != nullptr;
+        const bool feat = XTRA && a.features != nullptr;
         const float4 vi = feat ? a.vel[i] : make_float4(0.f, 0.f, 0.f, 0.f);
         float div = 0.0f;  // sum_j m_j (v_j - v_i) . gradW_ij  (velocity divergence x density)
         float nprev = 0.0f;  // sum_j lambda_prev_j (the neighbours' previous-substep lambda sums)
@@ -200,7 +260,7 @@ __global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) 
                     div += __int_as_float(q.w) * ((vj.x - vi.x) * g.x + (vj.y - vi.y) * g.y + (vj.z - vi.z) * g.z);
                     nprev += a.lam_prev[jj[u]];
                 }
-                if (a.method == 1) {  // incompressibility_1.comp:62-68
+                if (XTRA && a.method == 1) {  // incompressibility_1.comp:62-68
                     const float den = kw * APBF_FIX / mjf;
                     cx = wadd(cx, f2i((float)wadd(q.x, -p.x) / den));
                     cy = wadd(cy, f2i((float)wadd(q.y, -p.y) / den));
@@ -219,7 +279,7 @@ __global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) 
                 div = group_sum<L>(div);
                 nprev = group_sum<L>(nprev);
             }
-            if (a.method == 1) {
+            if (XTRA && a.method == 1) {
                 cx = group_wsum<L>(cx);
                 cy = group_wsum<L>(cy);
                 cz = group_wsum<L>(cz);
@@ -227,7 +287,6 @@ __global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) 
             }
         }
         if (!valid || sub != 0) continue;
-        const float im = a.inv_mass[i], radius = a.radius[i];
         const float W0 = GAUSS ? c.norm : kernel_height(a.hk, 0.0f, kw, c);
         dens += f2u(W0 / im * APBF_FIX);  // incompressibility_0.comp:32-45 (the self term)
         // incompressibility_2.comp:77-109
@@ -240,10 +299,9 @@ __global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) 
         const float sgl = sqrtf(wgsq) * ird;
         sqs += wgsq * im;
         const float under = 1.0f - density * ird;
-        float b = a.bness[i];
         if (a.update_b) {
             float bn;
-            if (a.method == 1) {
+            if (XTRA && a.method == 1) {
                 float tm = (float)cw * APBF_INV_FIX + 1.0f / im;
                 float3 cv = make_float3((float)cx, (float)cy, (float)cz);
                 bn = sqrtf(dot3x(cv, cv)) / (APBF_FIX * tm) * a.b_sgl_factor;
@@ -271,6 +329,9 @@ __global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) 
             else applied = 0.0f;
         }
         a.rec[i] = make_float4(applied, c.ivd, c.norm, kw);
+        a.pk[i] = make_int4(p.x, p.y, p.z, __float_as_int(applied));
+        kwlo = min(kwlo, __float_as_uint(kw));
+        kwhi = max(kwhi, __float_as_uint(kw));
         if (feat) {
             float *fo = a.features + (size_t)i * 8;
             fo[0] = (float)cnt;
@@ -323,48 +384,60 @@ __global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) 
             }
         }
         a.bness[i] = b;
-        const double ratio = (double)density * (double)ird - 1.0;
-        e1 += ratio > 0.0 ? ratio : (double)pull;
-        e2 += fabs(ratio);
+        const float ratio = __fmaf_rn(density, ird, -1.0f);  // one rounding of the exact product - 1
+        e1 += err_fix(ratio > 0.0f ? ratio : pull);
+        e2 += err_fix(fabsf(ratio));
         if (a.dbg_dens) {
             a.dbg_dens[i] = dens;
             a.dbg_grad[i] = make_int4(gx, gy, gz, 0);
             a.dbg_sq[i] = sq;
         }
     }
-    // deterministic block reduction of the error sums
-    __shared__ double s1[8], s2[8];
+    // block reduction of the error sums and of the kernel-width bits
+    __shared__ long long s1[8], s2[8];
+    __shared__ uint32_t s3[8], s4[8];
     for (int off = 16; off > 0; off >>= 1) {
         e1 += __shfl_down_sync(0xffffffffu, e1, off);
         e2 += __shfl_down_sync(0xffffffffu, e2, off);
     }
+    kwlo = __reduce_min_sync(0xffffffffu, kwlo);
+    kwhi = __reduce_max_sync(0xffffffffu, kwhi);
     const int w = threadIdx.x >> 5;
     if ((threadIdx.x & 31) == 0) {
         s1[w] = e1;
         s2[w] = e2;
+        s3[w] = kwlo;
+        s4[w] = kwhi;
     }
     __syncthreads();
     __shared__ bool s_last;
     if (threadIdx.x == 0) {
-        double t1 = 0.0, t2 = 0.0;
+        long long t1 = 0, t2 = 0;
+        uint32_t lo = 0xffffffffu, hi = 0u;
         for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
             t1 += s1[k];
             t2 += s2[k];
+            lo = min(lo, s3[k]);
+            hi = max(hi, s4[k]);
         }
-        a.partials[2 * blockIdx.x] = t1;
-        a.partials[2 * blockIdx.x + 1] = t2;
+        a.partials[3 * blockIdx.x] = t1;
+        a.partials[3 * blockIdx.x + 1] = t2;
+        a.partials[3 * blockIdx.x + 2] = (long long)(((unsigned long long)lo << 32) | hi);
         __threadfence();
         s_last = atomicAdd(&a.st->done_blocks, 1u) == gridDim.x - 1;
     }
     __syncthreads();
     if (!s_last) return;
-    // the last block: fixed-order sum of all partials (deterministic), error and
-    // convergence flag for the passes that follow
+    // the last block: sum of all partials, error and convergence flag for the
+    // passes that follow
     __threadfence();
-    double t1, t2;
-    block_sum2(a.partials, gridDim.x, t1, t2);
+    long long t1, t2;
+    uint32_t kmin, kmax;
+    block_reduce_partials(a.partials, gridDim.x, t1, t2, kmin, kmax);
     if (threadIdx.x == 0) {
-        const double m1 = n ? t1 / n : 0.0, m2 = n ? t2 / n : 0.0;
+        a.st->kw_uniform = kmin == kmax ? 1u : 0u;  // the position update may gather the packed records
+        const double inv = 1.0 / (double)kErrScale;
+        const double m1 = n ? (double)t1 * inv / n : 0.0, m2 = n ? (double)t2 * inv / n : 0.0;
         a.red_out[2] = m1;
         a.red_out[3] = m2;
         a.st->density_passes += 1u;
@@ -380,6 +453,8 @@ struct PassB {
     const int4 *pos;
     int4 *pos_out;
     const float4 *rec;
+    const int4 *pk;   // the density pass's packed records (position, applied lambda)
+    const float *kw;
     const int4 *shift;
     const float *radius;
     const float4 *bmin, *bmax, *rot;
@@ -405,6 +480,64 @@ struct PassB {
 __device__ __forceinline__ void accumulate(float *dst, int mode, uint32_t j, float v) {
     if (mode == 1) dst[j] = v;
     else if (mode == 2) dst[j] += v;
+}
+
+// Sum over particle j's (reverse) row of int(gradW_ij * lambda_i * 2^18)
+// (incompressibility_3.comp:62-66 as a gather) and the deferred boundariness
+// filter.  PACKED: the neighbours' packed records (position, applied lambda) with
+// j's own Gauss constants cj; else the solve records and the positions.
+template <bool GAUSS, int L, bool PACKED>
+__device__ __forceinline__ int3 delta_row(const PassB &a, const uint32_t *row, uint32_t cnt, uint32_t j, uint32_t sub,
+                                          int4 p, KConst cj, bool fil, float3 ed, bool &hit, int4 start) {
+    int32_t ax = start.x, ay = start.y, az = start.z;
+    for (uint32_t k0 = sub; k0 < cnt; k0 += L * kUnroll) {
+        uint32_t ii[kUnroll];
+        float4 rr[kUnroll];
+        int4 qq[kUnroll];
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) {
+            const uint32_t k = k0 + u * L;
+            ii[u] = k < cnt ? row[(size_t)k * a.stride] : j;
+        }
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) {
+            if (PACKED) {
+                qq[u] = a.pk[ii[u]];
+            } else {
+                rr[u] = a.rec[ii[u]];
+                qq[u] = a.pos[ii[u]];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) {
+            if (fil && !hit && k0 + u * L < cnt) {
+                const float3 dn = fdiff(qq[u], p);  // x_i - x_j ...
+                hit = gauss_filter_hit(ed, make_float3(-dn.x, -dn.y, -dn.z));  // ... as the offset x_j - x_i
+            }
+            const float lam = k0 + u * L < cnt ? (PACKED ? __int_as_float(qq[u].w) : rr[u].x) : 0.0f;
+            if (lam == 0.0f) continue;  // the applied lambda (incompressibility_3.comp:63); padding lanes
+            KConst c;
+            if (PACKED) {
+                c = cj;
+            } else {
+                c.ivd = rr[u].y;
+                c.norm = rr[u].z;
+            }
+            const float3 d = fdiff(qq[u], p);
+            const float r2 = dot3x(d, d);
+            float3 g;
+            if (GAUSS) {
+                g = kernel_gradient(1, d, r2, 0.0f, c, gauss_height(r2, c));
+            } else {
+                g = kernel_gradient(a.gk, d, r2, rr[u].w, c, a.gk == 1 ? gauss_height(r2, c) : 0.0f);
+            }
+            const float sc = lam * APBF_FIX;
+            ax = wadd(ax, f2i(g.x * sc));
+            ay = wadd(ay, f2i(g.y * sc));
+            az = wadd(az, f2i(g.z * sc));
+        }
+    }
+    return make_int3(ax, ay, az);
 }
 
 template <bool GAUSS, int L>
@@ -441,15 +574,21 @@ __global__ void __launch_bounds__(256, 4) k_delta(PassB a) {
         return;
     }
     const bool sym = a.st->range_min == a.st->range_max;
+    // Equal kernel widths (same bits): every neighbour's Gauss constants are this
+    // particle's, so one 16-byte record (position, applied lambda) per neighbour is
+    // gathered instead of the solve record and the position.
+    const bool packed = GAUSS && a.st->kw_uniform != 0u;
     const uint32_t *cnt_arr = sym ? a.count : a.rcount;
     const uint32_t *idx_arr = sym ? a.idx : a.ridx;
-    const uint32_t sub = threadIdx.x % L, gpb = blockDim.x / L;
+    const uint32_t sub = threadIdx.x % L;
+    const uint32_t gpb = blockDim.x / L;
     for (uint32_t base = blockIdx.x * gpb; base < n; base += gridDim.x * gpb) {
         const uint32_t j_raw = base + threadIdx.x / L;
         const bool valid = j_raw < n;
         const uint32_t j = valid ? j_raw : 0u;
         const int4 p = a.pos[j];
-        int32_t ax = 0, ay = 0, az = 0;
+        const KConst cj = gauss_consts(packed ? a.kw[j] : 1.0f);
+        int32_t ax, ay, az;
         const uint32_t cnt = valid ? cnt_arr[j] : 0u;
         const uint32_t *row = idx_arr + j;
         float3 ed = make_float3(0.f, 0.f, 0.f);
@@ -458,45 +597,16 @@ __global__ void __launch_bounds__(256, 4) k_delta(PassB a) {
             const int4 fj = a.filt[j];
             fil = fj.w != 0 && filter_dir(fj.x, fj.y, fj.z, ed);
         }
-        for (uint32_t k0 = sub; k0 < cnt; k0 += L * kUnroll) {
-            uint32_t ii[kUnroll];
-            float4 rr[kUnroll];
-            int4 qq[kUnroll];
-#pragma unroll
-            for (int u = 0; u < kUnroll; ++u) {
-                const uint32_t k = k0 + u * L;
-                ii[u] = k < cnt ? row[(size_t)k * a.stride] : j;
-            }
-#pragma unroll
-            for (int u = 0; u < kUnroll; ++u) {
-                rr[u] = a.rec[ii[u]];
-                qq[u] = a.pos[ii[u]];
-            }
-#pragma unroll
-            for (int u = 0; u < kUnroll; ++u) {
-                if (fil && !hit && k0 + u * L < cnt) {
-                    const float3 dn = fdiff(qq[u], p);  // x_i - x_j ...
-                    hit = gauss_filter_hit(ed, make_float3(-dn.x, -dn.y, -dn.z));  // ... as the offset x_j - x_i
-                }
-                const float lam = k0 + u * L < cnt ? rr[u].x : 0.0f;
-                if (lam == 0.0f) continue;  // the applied lambda (incompressibility_3.comp:63); padding lanes
-                KConst c;
-                c.ivd = rr[u].y;
-                c.norm = rr[u].z;
-                const float3 d = fdiff(qq[u], p);
-                const float r2 = dot3x(d, d);
-                float3 g;
-                if (GAUSS) {
-                    g = kernel_gradient(1, d, r2, 0.0f, c, gauss_height(r2, c));
-                } else {
-                    g = kernel_gradient(a.gk, d, r2, rr[u].w, c, a.gk == 1 ? gauss_height(r2, c) : 0.0f);
-                }
-                const float sc = lam * APBF_FIX;
-                ax = wadd(ax, f2i(g.x * sc));
-                ay = wadd(ay, f2i(g.y * sc));
-                az = wadd(az, f2i(g.z * sc));
-            }
-        }
+        // the sums start from the self shift (incompressibility_2.comp:106-109) on the
+        // first lane: wrapping integer sums are order-free, and the load is in flight
+        // with the particle's other data
+        const int4 sh = (valid && sub == 0) ? a.shift[j] : make_int4(0, 0, 0, 0);
+        const float rj = a.radius[j];
+        int3 acc = packed ? delta_row<GAUSS, L, true>(a, row, cnt, j, sub, p, cj, fil, ed, hit, sh)
+                          : delta_row<GAUSS, L, false>(a, row, cnt, j, sub, p, cj, fil, ed, hit, sh);
+        ax = acc.x;
+        ay = acc.y;
+        az = acc.z;
         if (L > 1) {
             ax = group_wsum<L>(ax);
             ay = group_wsum<L>(ay);
@@ -510,12 +620,8 @@ __global__ void __launch_bounds__(256, 4) k_delta(PassB a) {
         }
         if (!valid || sub != 0) continue;
         if (hit) a.bness[j] = 0.0f;
-        const int4 sh = a.shift[j];  // the self shift (incompressibility_2.comp:106-109)
-        ax = wadd(ax, sh.x);
-        ay = wadd(ay, sh.y);
-        az = wadd(az, sh.z);
         int4 out = make_int4(wadd(p.x, ax), wadd(p.y, ay), wadd(p.z, az), p.w);
-        if (nboxes) out = box_push(out, a.radius[j], j, a.bmin, a.bmax, a.rot, nboxes);
+        if (nboxes) out = box_push(out, rj, j, a.bmin, a.bmax, a.rot, nboxes);
         a.pos_out[j] = out;
         if (a.prev_mode | a.acc_mode) {
             const float lj = reinterpret_cast<const float *>(a.rec + j)[0];  // applied (learned) lambda
@@ -596,10 +702,11 @@ apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s, const SolveOpts &o)
     a.lambda = ctx->lambda;
     a.shift = ctx->shift;
     a.rec = ctx->solve_rec;
+    a.pk = ctx->solve_pk;
     a.dbg_dens = ctx->debug ? ctx->dbg_density : nullptr;
     a.dbg_grad = ctx->dbg_grad;
     a.dbg_sq = ctx->dbg_sq;
-    a.partials = ctx->red_partials;
+    a.partials = reinterpret_cast<long long *>(ctx->red_partials);
     a.d_len = ctx->d_len;
     a.st = ctx->status;
     a.red_out = ctx->red_out;
@@ -628,13 +735,16 @@ apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s, const SolveOpts &o)
     const int bps = (int)std::min(8u, std::max(1u, ctx->tuning.pass_blocks_per_sm));
     // the error reduction has one partial per block: at most red_blocks blocks
     const int ga = std::min(g, grid_for(ctx, (uint32_t)std::min<uint64_t>((uint64_t)cap * lanes, 0xffffffffu), pb, bps));
+    const bool xtra = a.features != nullptr || a.method == 1;
     APBF_BEFORE_LAUNCH(ctx, s, "k_density_lambda");
     launch_lanes(lanes, [&](auto lc) {
         constexpr int Lc = decltype(lc)::value;
-        if (gauss)
-            k_density_lambda<true, Lc><<<ga, pb, 0, s>>>(a);
+        if (gauss && xtra)
+            k_density_lambda<true, Lc, true><<<ga, pb, 0, s>>>(a);
+        else if (gauss)
+            k_density_lambda<true, Lc, false><<<ga, pb, 0, s>>>(a);
         else
-            k_density_lambda<false, Lc><<<ga, pb, 0, s>>>(a);
+            k_density_lambda<false, Lc, true><<<ga, pb, 0, s>>>(a);
     });
     APBF_AFTER_LAUNCH(ctx, s, "k_density_lambda");
 
@@ -646,6 +756,8 @@ apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s, const SolveOpts &o)
     b.pos = f.pos;
     b.pos_out = alt.pos;
     b.rec = ctx->solve_rec;
+    b.pk = ctx->solve_pk;
+    b.kw = f.kernel_width;
     b.shift = ctx->shift;
     b.radius = f.radius;
     b.bmin = ctx->box_min;
@@ -691,10 +803,10 @@ apbf_status reduce_fp64(apbf_ctx *ctx, double out[4], cudaStream_t s) {
     const int g = ctx->red_blocks;
     // red_out[2..3] hold the error of the last density pass (its last block wrote them)
     APBF_BEFORE_LAUNCH(ctx, s, "k_mass_volume");
-    k_mass_volume<<<g, kBlock, 0, s>>>(f.inv_mass, f.radius, ctx->d_len, ctx->red_partials + 2 * g);
+    k_mass_volume<<<g, kBlock, 0, s>>>(f.inv_mass, f.radius, ctx->d_len, ctx->red_partials + 4 * g);
     APBF_AFTER_LAUNCH(ctx, s, "k_mass_volume");
     APBF_BEFORE_LAUNCH(ctx, s, "k_finalize_mass");
-    k_finalize_mass<<<1, 256, 0, s>>>(ctx->red_partials + 2 * g, g, ctx->red_out);
+    k_finalize_mass<<<1, 256, 0, s>>>(ctx->red_partials + 4 * g, g, ctx->red_out);
     APBF_AFTER_LAUNCH(ctx, s, "k_finalize_mass");
     APBF_CUDA(cudaMemcpyAsync(out, ctx->red_out, 4 * sizeof(double), cudaMemcpyDeviceToHost, s));
     APBF_CUDA(cudaStreamSynchronize(s));

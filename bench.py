@@ -468,6 +468,7 @@ def run_ours(args) -> None:
                     "traffic": traffic_from_profiles(name, n_prof, head["pairs"]),
                     "algorithmic_bytes": alg, "launch_us": per_launch_s * 1e6}
     kernel_share = {k: round(v[1] / max(sum(x[1] for x in prof.values()), 1e-9), 4) for k, v in prof.items()}
+    kernel_us = {k: round(v[1] / max(v[0], 1) * 1000.0, 2) for k, v in prof.items()}  # mean per launch
 
     # e2e: the same substep driven from pinned host buffers through the C ABI
     e2e = run_e2e(ctx, spec, args, local)
@@ -497,7 +498,8 @@ def run_ours(args) -> None:
             "state_after": head["state_after"],
             "plain": plain or None,
             "warm_start_training": train_info,
-            "roofline": roof, "kernel_share": kernel_share, "gpu_launches": head["gpu_launches"],
+            "roofline": roof, "kernel_share": kernel_share, "kernel_us": kernel_us,
+            "gpu_launches": head["gpu_launches"],
             "profiler_dropped": int(dropped), "clocks": clk, "e2e": e2e, "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)

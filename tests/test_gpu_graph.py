@@ -51,6 +51,31 @@ def test_graph_matches_launches_dam_break(iterations, target):
         assert a[3] < b[3], (a[3], b[3])
 
 
+@pytest.mark.parametrize("mode", [1, 2])
+def test_graph_runs_every_pass_without_target_after_converged_substeps(mode):
+    """Substeps with an error target converge (and set the device flag); a substep
+    without a target then runs all solver_iterations passes in the graph modes too."""
+    from apbf_gb300.api import Context
+
+    spec = scenes.dam_break(n_side=16)
+    ctx = Context(particle_capacity=spec.n, max_neighbors=128, max_log2res=max(spec.log2res, 3))
+    ctx.set_settings(basic_pbf=1, solver_iterations=40, density_error_target=5e-2)
+    ctx.set_scene(spec.grid_min, spec.grid_max, spec.log2res, spec.acceleration)
+    ctx.set_boxes(spec.box_min, spec.box_max)
+    ctx.upload(spec.state)
+    ctx.set_solve_graph(mode)
+    for _ in range(4):
+        ctx.substep(spec.dt)
+    info = ctx.check_status()
+    assert info.converged_substeps == 4
+    ctx.set_settings(solver_iterations=9, density_error_target=0.0)
+    for _ in range(2):
+        ctx.substep(spec.dt)
+    info = ctx.check_status()
+    assert info.density_passes == 18, info.density_passes
+    ctx.close()
+
+
 def test_graph_matches_launches_with_warm_start():
     from oracle import mlp_oracle as M
 
