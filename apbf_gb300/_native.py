@@ -201,6 +201,7 @@ SIGNATURES = {
     "apbf_mlp_load": (_ST, [_P, _P, _P]),
     "apbf_set_warm_start": (_ST, [_P, C.c_int]),
     "apbf_set_solve_graph": (_ST, [_P, C.c_int]),
+    "apbf_set_persistent_solve": (_ST, [_P, C.c_int]),
     "apbf_batch_create": (_ST, [_P, C.c_uint32, _P]),
     "apbf_batch_substep": (_ST, [_P, C.c_float, _P]),
     "apbf_batch_destroy": (_ST, [_P]),

@@ -235,6 +235,11 @@ class Context:
         device-side loop; 2: the whole substep as one graph launch."""
         N.check(self.lib.apbf_set_solve_graph(self.handle, int(mode)), "apbf_set_solve_graph")
 
+    def set_persistent_solve(self, enable: bool = True) -> None:
+        """Jacobi passes 1.. of a substep as one persistent cooperative kernel (same
+        results; used where it applies, see apbf_set_persistent_solve)."""
+        N.check(self.lib.apbf_set_persistent_solve(self.handle, 1 if enable else 0), "apbf_set_persistent_solve")
+
     # ---- lists ----
     def fluid_view(self) -> dict:
         v = N.FluidView()

@@ -67,7 +67,11 @@ struct Status {
     uint32_t loop_iters;           // solve loop graph: body runs since the context was created
     uint32_t filter_tag;           // 1: this pass's density kernel left the boundariness filter to k_delta
     uint32_t kw_uniform;           // 1: every kernel width of this density pass had the same bits
-    uint32_t pad2[2];
+    uint32_t bar_arrive;           // persistent solve: blocks arrived at the current grid barrier
+    uint32_t bar_gen;              // persistent solve: grid barriers released so far
+    uint32_t pad3;
+    unsigned long long loop_e1;    // persistent solve: error sums of the current pass (2^-24 fixed point)
+    unsigned long long loop_e2;
 };
 
 // Device length block.
@@ -248,6 +252,9 @@ struct apbf_ctx {
 
     // solve loop graphs (graph.cu)
     int use_graphs = 1;
+    int persistent_solve = 0;  // passes 1.. as one persistent cooperative kernel (apbf_set_persistent_solve)
+    int coop_blocks = 0;       // its resident grid (0: cooperative launches unavailable)
+    bool in_batch = false;     // being captured as one branch of a batch graph
     unsigned long long graph_version = 1;  // bumped by every change captured by value
     apbf::SolveGraph solve_graphs[apbf::kSolveGraphs];
     int solve_graph_next = 0;
@@ -348,6 +355,12 @@ struct SolveOpts {
     uint32_t max_passes = 0;  //   skipped from max_passes on, box after it unless it is the last
 };
 apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s, const SolveOpts &o = SolveOpts());
+// Passes 1.. of a substep as one persistent cooperative kernel with grid barriers
+// between the density and position phases; APBF_ERR_INVALID_ARG when the solve
+// does not qualify (then the caller uses the per-pass or graph forms).
+apbf_status solve_persistent(apbf_ctx *ctx, cudaStream_t s, const SolveOpts &o);
+bool solve_persistent_eligible(const apbf_ctx *ctx, const SolveOpts &o);
+int solve_persistent_blocks(int device, int num_sms);
 // Passes 1.. of a substep as one graph launch (a device-side while loop).
 apbf_status solve_loop(apbf_ctx *ctx, cudaStream_t s, const SolveOpts &o);
 // The same loop as a conditional node of the graph that stream s is capturing.

@@ -191,6 +191,7 @@ apbf_status apbf_create(const apbf_config *cfg, apbf_ctx **out) {
     A(ctx->list_a, cap);
     A(ctx->list_b, cap);
     ctx->red_blocks = grid_for(ctx, cap, kBlock, 8);
+    ctx->coop_blocks = solve_persistent_blocks(ctx->device, ctx->num_sms);
     A(ctx->red_partials, (size_t)6 * ctx->red_blocks);
     A(ctx->red_out, 4);
     A(ctx->box_min, APBF_MAX_BOXES);
@@ -323,6 +324,19 @@ apbf_status apbf_set_debug(apbf_ctx *ctx, int enable) {
 apbf_status apbf_set_solve_graph(apbf_ctx *ctx, int mode) {
     if (!ctx || mode < 0 || mode > 2) return APBF_ERR_INVALID_ARG;
     ctx->use_graphs = mode;
+    destroy_solve_graphs(ctx);
+    destroy_substep_graphs(ctx);
+    return APBF_OK;
+}
+
+apbf_status apbf_set_persistent_solve(apbf_ctx *ctx, int enable) {
+    if (!ctx) return APBF_ERR_INVALID_ARG;
+    if (enable && ctx->coop_blocks <= 0) {
+        set_error("apbf_set_persistent_solve: the device has no cooperative launches");
+        return APBF_ERR_INVALID_ARG;
+    }
+    ctx->persistent_solve = enable ? 1 : 0;
+    ctx->graph_version++;
     destroy_solve_graphs(ctx);
     destroy_substep_graphs(ctx);
     return APBF_OK;
@@ -497,6 +511,15 @@ apbf_status substep_body(apbf_ctx *ctx, float dt, cudaStream_t s, bool capture) 
         o.learned = learned && it == 0;
         o.prev_mode = track ? (it == 0 ? 1 : 2) : 0;
         o.projected = projected;
+        if (it == 1 && st.solver_iterations >= 2 && !recording) {
+            SolveOpts q = o;
+            q.max_passes = (uint32_t)st.solver_iterations;
+            if (solve_persistent_eligible(ctx, q)) {  // passes 1.. in one persistent launch
+                r = solve_persistent(ctx, s, q);
+                if (r != APBF_OK) return r;
+                break;
+            }
+        }
         if (it == 1 && loop_graph) {
             o.max_passes = (uint32_t)st.solver_iterations;
             r = capture ? solve_loop_captured(ctx, s, o) : solve_loop(ctx, s, o);

@@ -393,7 +393,9 @@ extern "C" apbf_status apbf_batch_substep(apbf_batch *b, float dt, void *stream)
             break;
         }
         c->capturing = true;
+        c->in_batch = true;  // parallel branches: no persistent solve (each would want the whole GPU)
         r = substep_body(c, dt, cs, true);
+        c->in_batch = false;
         c->capturing = false;
         if (r == APBF_OK && (cudaEventRecord(b->join[i], cs) != cudaSuccess ||
                              cudaStreamWaitEvent(b->stream, b->join[i], 0) != cudaSuccess))

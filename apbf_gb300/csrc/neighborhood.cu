@@ -177,7 +177,7 @@ struct BuildArgs {
 // particle.  A box that touches no edge cell of the grid only meets particles
 // inside the grid (edge cells also hold the clamped outsiders), so it uses the
 // 32-bit predicate.
-__global__ void __launch_bounds__(256, 3) k_build_rows(BuildArgs a) {
+__global__ void __launch_bounds__(256, 4) k_build_rows(BuildArgs a) {
     const uint32_t n = a.d_len[kLenParticles];
     const uint32_t last = (1u << a.L) - 1u;
     unsigned long long local = 0;

@@ -18,6 +18,7 @@
 // bit-identical to the atomic scatter.  Gradients are recomputed in k_delta
 // rather than stored (the reference writes 16 bytes per pair).
 #include <algorithm>
+#include <cstddef>
 #include <type_traits>
 
 #include "apbf_internal.cuh"
@@ -192,23 +193,20 @@ __device__ __forceinline__ int32_t group_wsum(int32_t v) {
 
 // XTRA: the warm-start features or the centre-of-mass boundariness sums
 // (method 1) are gathered too; the common pass is compiled without them.
-template <bool GAUSS, int L, bool XTRA>
-__global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) {
-    const bool skip = (a.early_exit && *(volatile uint32_t *)&a.st->converged) ||
-                      (a.loop_offset >= 0 && a.st->pass_index + (uint32_t)a.loop_offset >= a.max_passes);
-    // With symmetric rows the Gauss filter runs in this pass's position update, which
-    // gathers over the same neighbours anyway; filter_tag tells it whether to.
-    const bool defer = GAUSS && a.filt && a.method == 2 && a.st->range_min == a.st->range_max;
-    if (blockIdx.x == 0 && threadIdx.x == 0) a.st->filter_tag = (!skip && defer) ? 1u : 0u;
-    if (skip) return;  // uniform over the grid
-    const uint32_t n = a.d_len[kLenParticles];
-    const uint32_t sub = threadIdx.x % L;
+// Per-thread partial results of a density pass: the two error sums (2^-24 fixed
+// point) and the range of the kernel-width bits.
+struct PassSums {
     long long e1 = 0, e2 = 0;
-    uint32_t kwlo = 0xffffffffu, kwhi = 0u;  // kernel-width bits seen by this thread
-    // the block iterates as a whole (uniform trip count: the group shuffles need every lane)
-    const uint32_t gpb = blockDim.x / L;
-    for (uint32_t base = blockIdx.x * gpb; base < n; base += gridDim.x * gpb) {
-        const uint32_t i_raw = base + threadIdx.x / L;
+    uint32_t kwlo = 0xffffffffu, kwhi = 0u;
+};
+
+// One particle (row i_raw, lane sub of its group of L) of a density pass:
+// incompressibility_0..2 and the boundariness filter of incompressibility_3.
+// Every lane of the group must call it (group shuffles).
+template <bool GAUSS, int L, bool XTRA>
+__device__ __forceinline__ void density_one(const PassA &a, uint32_t i_raw, uint32_t n, uint32_t sub, bool defer,
+                                            PassSums &ps) {
+    {
         const bool valid = i_raw < n;
         const uint32_t i = valid ? i_raw : 0u;
         const int4 p = a.pos[i];
@@ -286,7 +284,7 @@ __global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) 
                 cw = group_wsum<L>(cw);
             }
         }
-        if (!valid || sub != 0) continue;
+        if (!valid || sub != 0) return;
         const float W0 = GAUSS ? c.norm : kernel_height(a.hk, 0.0f, kw, c);
         dens += f2u(W0 / im * APBF_FIX);  // incompressibility_0.comp:32-45 (the self term)
         // incompressibility_2.comp:77-109
@@ -330,8 +328,8 @@ __global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) 
         }
         a.rec[i] = make_float4(applied, c.ivd, c.norm, kw);
         a.pk[i] = make_int4(p.x, p.y, p.z, __float_as_int(applied));
-        kwlo = min(kwlo, __float_as_uint(kw));
-        kwhi = max(kwhi, __float_as_uint(kw));
+        ps.kwlo = min(ps.kwlo, __float_as_uint(kw));
+        ps.kwhi = max(ps.kwhi, __float_as_uint(kw));
         if (feat) {
             float *fo = a.features + (size_t)i * 8;
             fo[0] = (float)cnt;
@@ -385,41 +383,82 @@ __global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) 
         }
         a.bness[i] = b;
         const float ratio = __fmaf_rn(density, ird, -1.0f);  // one rounding of the exact product - 1
-        e1 += err_fix(ratio > 0.0f ? ratio : pull);
-        e2 += err_fix(fabsf(ratio));
+        ps.e1 += err_fix(ratio > 0.0f ? ratio : pull);
+        ps.e2 += err_fix(fabsf(ratio));
         if (a.dbg_dens) {
             a.dbg_dens[i] = dens;
             a.dbg_grad[i] = make_int4(gx, gy, gz, 0);
             a.dbg_sq[i] = sq;
         }
     }
-    // block reduction of the error sums and of the kernel-width bits
+}
+
+// Block sums of the per-thread PassSums, valid in thread 0.
+__device__ __forceinline__ PassSums block_pass_sums(PassSums ps) {
     __shared__ long long s1[8], s2[8];
     __shared__ uint32_t s3[8], s4[8];
     for (int off = 16; off > 0; off >>= 1) {
-        e1 += __shfl_down_sync(0xffffffffu, e1, off);
-        e2 += __shfl_down_sync(0xffffffffu, e2, off);
+        ps.e1 += __shfl_down_sync(0xffffffffu, ps.e1, off);
+        ps.e2 += __shfl_down_sync(0xffffffffu, ps.e2, off);
     }
-    kwlo = __reduce_min_sync(0xffffffffu, kwlo);
-    kwhi = __reduce_max_sync(0xffffffffu, kwhi);
+    ps.kwlo = __reduce_min_sync(0xffffffffu, ps.kwlo);
+    ps.kwhi = __reduce_max_sync(0xffffffffu, ps.kwhi);
     const int w = threadIdx.x >> 5;
     if ((threadIdx.x & 31) == 0) {
-        s1[w] = e1;
-        s2[w] = e2;
-        s3[w] = kwlo;
-        s4[w] = kwhi;
+        s1[w] = ps.e1;
+        s2[w] = ps.e2;
+        s3[w] = ps.kwlo;
+        s4[w] = ps.kwhi;
     }
     __syncthreads();
+    PassSums t;
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+            t.e1 += s1[k];
+            t.e2 += s2[k];
+            t.kwlo = min(t.kwlo, s3[k]);
+            t.kwhi = max(t.kwhi, s4[k]);
+        }
+    }
+    __syncthreads();  // the shared arrays may be reused by the next call
+    return t;
+}
+
+// The end of a density pass, once all its sums are in (one thread): mean errors,
+// width uniformity, pass counter and the convergence flag for the passes that follow.
+__device__ __forceinline__ void finish_pass(const PassA &a, uint32_t n, long long t1, long long t2) {
+    const double inv = 1.0 / (double)kErrScale;
+    const double m1 = n ? (double)t1 * inv / n : 0.0, m2 = n ? (double)t2 * inv / n : 0.0;
+    a.red_out[2] = m1;
+    a.red_out[3] = m2;
+    a.st->density_passes += 1u;
+    if (a.target > 0.0f && m1 <= (double)a.target) {
+        a.st->converged = 1u;  // the remaining passes of the substep are skipped
+        a.st->converged_substeps += 1u;
+    }
+}
+
+template <bool GAUSS, int L, bool XTRA>
+__global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) {
+    const bool skip = (a.early_exit && *(volatile uint32_t *)&a.st->converged) ||
+                      (a.loop_offset >= 0 && a.st->pass_index + (uint32_t)a.loop_offset >= a.max_passes);
+    // With symmetric rows the Gauss filter runs in this pass's position update, which
+    // gathers over the same neighbours anyway; filter_tag tells it whether to.
+    const bool defer = GAUSS && a.filt && a.method == 2 && a.st->range_min == a.st->range_max;
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.st->filter_tag = (!skip && defer) ? 1u : 0u;
+    if (skip) return;  // uniform over the grid
+    const uint32_t n = a.d_len[kLenParticles];
+    const uint32_t sub = threadIdx.x % L;
+    PassSums ps;
+    // the block iterates as a whole (uniform trip count: the group shuffles need every lane)
+    const uint32_t gpb = blockDim.x / L;
+    for (uint32_t base = blockIdx.x * gpb; base < n; base += gridDim.x * gpb)
+        density_one<GAUSS, L, XTRA>(a, base + threadIdx.x / L, n, sub, defer, ps);
+    const PassSums bs = block_pass_sums(ps);
     __shared__ bool s_last;
     if (threadIdx.x == 0) {
-        long long t1 = 0, t2 = 0;
-        uint32_t lo = 0xffffffffu, hi = 0u;
-        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
-            t1 += s1[k];
-            t2 += s2[k];
-            lo = min(lo, s3[k]);
-            hi = max(hi, s4[k]);
-        }
+        const long long t1 = bs.e1, t2 = bs.e2;
+        const uint32_t lo = bs.kwlo, hi = bs.kwhi;
         a.partials[3 * blockIdx.x] = t1;
         a.partials[3 * blockIdx.x + 1] = t2;
         a.partials[3 * blockIdx.x + 2] = (long long)(((unsigned long long)lo << 32) | hi);
@@ -435,17 +474,9 @@ __global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) 
     uint32_t kmin, kmax;
     block_reduce_partials(a.partials, gridDim.x, t1, t2, kmin, kmax);
     if (threadIdx.x == 0) {
-        a.st->kw_uniform = kmin == kmax ? 1u : 0u;  // the position update may gather the packed records
-        const double inv = 1.0 / (double)kErrScale;
-        const double m1 = n ? (double)t1 * inv / n : 0.0, m2 = n ? (double)t2 * inv / n : 0.0;
-        a.red_out[2] = m1;
-        a.red_out[3] = m2;
-        a.st->density_passes += 1u;
         a.st->done_blocks = 0u;
-        if (a.target > 0.0f && m1 <= (double)a.target) {
-            a.st->converged = 1u;  // the remaining passes of the substep are skipped
-            a.st->converged_substeps += 1u;
-        }
+        a.st->kw_uniform = kmin == kmax ? 1u : 0u;  // the position update may gather the packed records
+        finish_pass(a, n, t1, t2);
     }
 }
 
@@ -540,50 +571,15 @@ __device__ __forceinline__ int3 delta_row(const PassB &a, const uint32_t *row, u
     return make_int3(ax, ay, az);
 }
 
+// One particle (row j_raw, lane sub of its group of L) of a position update:
+// incompressibility_3 as a gather, the deferred filter, the next iteration's box
+// collision (nboxes > 0) and the lambda bookkeeping.  Every lane of the group
+// must call it (group shuffles).
 template <bool GAUSS, int L>
-__global__ void __launch_bounds__(256, 4) k_delta(PassB a) {
-    const uint32_t n = a.d_len[kLenParticles];
-    bool skip = a.early_exit && *(volatile const uint32_t *)&a.st->converged;
-    uint32_t nboxes = a.nboxes;
-    if (a.loop_offset >= 0) {
-        const uint32_t pass = a.st->pass_index + (uint32_t)a.loop_offset;
-        skip = skip || pass >= a.max_passes;
-        if (pass + 1u >= a.max_passes) nboxes = 0u;  // no box collision after the last iteration
-    }
-    // the density pass of this pass deferred the Gauss filter to here (symmetric rows)
-    const bool filter = GAUSS && *(volatile const uint32_t *)&a.st->filter_tag != 0u;
-    if (skip) {
-        if (filter) {  // converged: no position update, but the filter still belongs to this pass
-            for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
-                const int4 fj = a.filt[j];
-                float3 ed;
-                if (!fj.w || !filter_dir(fj.x, fj.y, fj.z, ed)) continue;
-                const int4 p = a.pos[j];
-                for (uint32_t k = 0; k < a.count[j]; ++k)
-                    if (gauss_filter_hit(ed, fdiff(p, a.pos[a.idx[(size_t)k * a.stride + j]]))) {
-                        a.bness[j] = 0.0f;
-                        break;
-                    }
-            }
-        }
-        for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
-            a.pos_out[j] = a.pos[j];
-            accumulate(a.lam_prev, a.prev_mode, j, 0.0f);  // nothing applied in this pass
-            accumulate(a.lam_acc, a.acc_mode, j, 0.0f);
-        }
-        return;
-    }
-    const bool sym = a.st->range_min == a.st->range_max;
-    // Equal kernel widths (same bits): every neighbour's Gauss constants are this
-    // particle's, so one 16-byte record (position, applied lambda) per neighbour is
-    // gathered instead of the solve record and the position.
-    const bool packed = GAUSS && a.st->kw_uniform != 0u;
-    const uint32_t *cnt_arr = sym ? a.count : a.rcount;
-    const uint32_t *idx_arr = sym ? a.idx : a.ridx;
-    const uint32_t sub = threadIdx.x % L;
-    const uint32_t gpb = blockDim.x / L;
-    for (uint32_t base = blockIdx.x * gpb; base < n; base += gridDim.x * gpb) {
-        const uint32_t j_raw = base + threadIdx.x / L;
+__device__ __forceinline__ void delta_one(const PassB &a, uint32_t j_raw, uint32_t n, uint32_t sub, bool packed,
+                                          bool filter, const uint32_t *cnt_arr, const uint32_t *idx_arr,
+                                          uint32_t nboxes) {
+    {
         const bool valid = j_raw < n;
         const uint32_t j = valid ? j_raw : 0u;
         const int4 p = a.pos[j];
@@ -618,7 +614,7 @@ __global__ void __launch_bounds__(256, 4) k_delta(PassB a) {
                 hit = h != 0;
             }
         }
-        if (!valid || sub != 0) continue;
+        if (!valid || sub != 0) return;
         if (hit) a.bness[j] = 0.0f;
         int4 out = make_int4(wadd(p.x, ax), wadd(p.y, ay), wadd(p.z, az), p.w);
         if (nboxes) out = box_push(out, rj, j, a.bmin, a.bmax, a.rot, nboxes);
@@ -629,6 +625,168 @@ __global__ void __launch_bounds__(256, 4) k_delta(PassB a) {
             accumulate(a.lam_acc, a.acc_mode, j, lj);
         }
     }
+}
+
+// A converged pass (no position update) of particle j: the deferred filter still
+// belongs to it, the positions are copied through and nothing is applied.
+__device__ __forceinline__ void delta_skip_filter(const PassB &a, uint32_t j) {
+    const int4 fj = a.filt[j];
+    float3 ed;
+    if (!fj.w || !filter_dir(fj.x, fj.y, fj.z, ed)) return;
+    const int4 p = a.pos[j];
+    for (uint32_t k = 0; k < a.count[j]; ++k)
+        if (gauss_filter_hit(ed, fdiff(p, a.pos[a.idx[(size_t)k * a.stride + j]]))) {
+            a.bness[j] = 0.0f;
+            break;
+        }
+}
+__device__ __forceinline__ void delta_skip_copy(const PassB &a, uint32_t j) {
+    a.pos_out[j] = a.pos[j];
+    accumulate(a.lam_prev, a.prev_mode, j, 0.0f);  // nothing applied in this pass
+    accumulate(a.lam_acc, a.acc_mode, j, 0.0f);
+}
+
+template <bool GAUSS, int L>
+__global__ void __launch_bounds__(256, 4) k_delta(PassB a) {
+    const uint32_t n = a.d_len[kLenParticles];
+    bool skip = a.early_exit && *(volatile const uint32_t *)&a.st->converged;
+    uint32_t nboxes = a.nboxes;
+    if (a.loop_offset >= 0) {
+        const uint32_t pass = a.st->pass_index + (uint32_t)a.loop_offset;
+        skip = skip || pass >= a.max_passes;
+        if (pass + 1u >= a.max_passes) nboxes = 0u;  // no box collision after the last iteration
+    }
+    // the density pass of this pass deferred the Gauss filter to here (symmetric rows)
+    const bool filter = GAUSS && *(volatile const uint32_t *)&a.st->filter_tag != 0u;
+    if (skip) {
+        if (filter)  // converged: no position update, but the filter still belongs to this pass
+            for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+                delta_skip_filter(a, j);
+        for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+            delta_skip_copy(a, j);
+        return;
+    }
+    const bool sym = a.st->range_min == a.st->range_max;
+    // Equal kernel widths (same bits): every neighbour's Gauss constants are this
+    // particle's, so one 16-byte record (position, applied lambda) per neighbour is
+    // gathered instead of the solve record and the position.
+    const bool packed = GAUSS && a.st->kw_uniform != 0u;
+    const uint32_t *cnt_arr = sym ? a.count : a.rcount;
+    const uint32_t *idx_arr = sym ? a.idx : a.ridx;
+    const uint32_t sub = threadIdx.x % L;
+    const uint32_t gpb = blockDim.x / L;
+    for (uint32_t base = blockIdx.x * gpb; base < n; base += gridDim.x * gpb)
+        delta_one<GAUSS, L>(a, base + threadIdx.x / L, n, sub, packed, filter, cnt_arr, idx_arr, nboxes);
+}
+
+// ---- the solve loop as one persistent cooperative kernel ----
+
+struct LoopArgs {
+    int4 *pos_a;          // positions before the first loop pass; the final positions end here
+    int4 *pos_b;          // the other position buffer
+    uint32_t first;       // number of the first loop pass
+    uint32_t max_passes;  // passes from this number on do not run
+    uint32_t nboxes;      // boxes of the next iteration's collision (none after the last pass)
+    int defer;            // the density pass may leave the Gauss filter to the position phase (rows symmetric)
+};
+
+constexpr uint32_t kBarrierSpins = 1u << 22;  // x __nanosleep(64): a few hundred ms at most
+
+// Grid barrier of a cooperative launch (every block resident).  The last block to
+// arrive finishes the density pass when fin is set (one thread, all partial sums
+// in) and releases the others; a wait that exceeds kBarrierSpins sets
+// APBF_FLAG_SPIN_LIMIT and returns false, after which the block leaves the kernel
+// (the blocks still waiting give up in turn, so every wait ends).
+__device__ __forceinline__ bool grid_barrier(Status *st, uint32_t &gen, const PassA *fin, uint32_t n) {
+    __syncthreads();
+    __shared__ uint32_t s_ok;
+    if (threadIdx.x == 0) {
+        uint32_t ok = 1u;
+        __threadfence();
+        const uint32_t arrived = atomicAdd(&st->bar_arrive, 1u) + 1u;
+        if (arrived == gridDim.x) {
+            if (fin) {
+                const unsigned long long t1 = *(volatile unsigned long long *)&st->loop_e1;
+                const unsigned long long t2 = *(volatile unsigned long long *)&st->loop_e2;
+                st->loop_e1 = 0ull;
+                st->loop_e2 = 0ull;
+                finish_pass(*fin, n, (long long)t1, (long long)t2);
+            }
+            st->bar_arrive = 0u;
+            __threadfence();
+            atomicAdd(&st->bar_gen, 1u);  // release
+        } else {
+            uint32_t spins = 0;
+            while (*(volatile uint32_t *)&st->bar_gen == gen) {
+                if (++spins > kBarrierSpins) {
+                    set_flag(st, APBF_FLAG_SPIN_LIMIT);
+                    st->spin_where = 3u;
+                    ok = 0u;
+                    break;
+                }
+                __nanosleep(64);
+            }
+            __threadfence();
+        }
+        s_ok = ok;
+    }
+    __syncthreads();
+    ++gen;
+    return s_ok != 0u;
+}
+
+// Jacobi passes first .. max_passes-1 of a substep (or until a density pass meets
+// the error target) in one launch: per pass, the density phase (density_one for
+// every particle, error sums by integer atomics), a grid barrier whose last block
+// finishes the pass, the position phase (delta_one) and a second barrier.  The
+// per-particle arithmetic is the two-kernel form's own, so the results are
+// identical; what goes away is two launches per pass and their ramp-up and drain.
+// The widths' uniformity is the one pass 0 found (widths do not change within a
+// substep).
+template <bool GAUSS>
+__global__ void __launch_bounds__(256, 4) k_solve_loop(PassA a, PassB b, LoopArgs l) {
+    Status *st = a.st;
+    if (a.early_exit && *(volatile uint32_t *)&st->converged) return;  // pass 0 met the target: no loop pass
+    uint32_t gen = *(volatile uint32_t *)&st->bar_gen;  // read before this block's first arrival
+    const uint32_t n = a.d_len[kLenParticles];
+    const bool sym = st->range_min == st->range_max;
+    // with symmetric rows the Gauss filter runs in the position phase (as k_density_lambda decides)
+    const bool defer = l.defer != 0 && sym;
+    const bool packed = GAUSS && st->kw_uniform != 0u;
+    const uint32_t *cnt_arr = sym ? b.count : b.rcount;
+    const uint32_t *idx_arr = sym ? b.idx : b.ridx;
+    const uint32_t T = gridDim.x * blockDim.x, t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    int4 *cur = l.pos_a, *nxt = l.pos_b;
+    for (uint32_t pass = l.first; pass < l.max_passes; ++pass) {
+        a.pos = cur;
+        PassSums ps;
+        for (uint32_t i = t0; i < n; i += T) density_one<GAUSS, 1, false>(a, i, n, 0u, defer, ps);
+        const PassSums bs = block_pass_sums(ps);
+        if (threadIdx.x == 0) {
+            atomicAdd(&st->loop_e1, (unsigned long long)bs.e1);
+            atomicAdd(&st->loop_e2, (unsigned long long)bs.e2);
+        }
+        if (!grid_barrier(st, gen, &a, n)) return;
+        b.pos = cur;
+        b.pos_out = nxt;
+        if (*(volatile uint32_t *)&st->converged != 0u) {
+            // converged: no position update (the positions stay in cur), the deferred
+            // filter still belongs to this pass
+            for (uint32_t j = t0; j < n; j += T) {
+                if (defer) delta_skip_filter(b, j);
+                accumulate(b.lam_prev, b.prev_mode, j, 0.0f);
+            }
+            break;
+        }
+        const uint32_t nb = pass + 1u < l.max_passes ? l.nboxes : 0u;
+        for (uint32_t j = t0; j < n; j += T) delta_one<GAUSS, 1>(b, j, n, 0u, packed, defer, cnt_arr, idx_arr, nb);
+        if (!grid_barrier(st, gen, nullptr, n)) return;
+        int4 *t = cur;
+        cur = nxt;
+        nxt = t;
+    }
+    if (cur != l.pos_a)  // an odd number of updates: bring the positions back to the caller's buffer
+        for (uint32_t j = t0; j < n; j += T) l.pos_a[j] = cur[j];
 }
 
 __global__ void k_mass_volume(const float *inv_mass, const float *radius, const uint32_t *d_len, double *partials) {
@@ -682,14 +840,13 @@ void launch_lanes(int lanes, F &&f) {
     }
 }
 
-apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s, const SolveOpts &o) {
-    const bool box_after = o.box_after, converge = o.converge, learned = o.learned, projected = o.projected;
-    const int feature_mode = o.feature_mode, acc_mode = o.acc_mode, prev_mode = o.prev_mode;
-    const uint32_t cap = ctx->cfg.particle_capacity;
+// Kernel arguments of the density pass (PassA) and the position update (PassB)
+// for the context's current buffers and the solve options.
+static PassA make_pass_a(apbf_ctx *ctx, const SolveOpts &o) {
+    const bool converge = o.converge, projected = o.projected;
+    const int feature_mode = o.feature_mode, prev_mode = o.prev_mode;
     FluidBufs &f = ctx->fl[ctx->fcur];
-    FluidBufs &alt = ctx->fl[ctx->fcur ^ 1];
     const apbf_settings &st = ctx->settings;
-    const bool gauss = st.height_kernel_id == 1 && st.gradient_kernel_id == 1;
     PassA a;
     a.pos = f.pos;
     a.inv_mass = f.inv_mass;
@@ -729,6 +886,53 @@ apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s, const SolveOpts &o)
     a.b_speed = st.boundariness_adaption_speed;
     a.b_sgl_factor = st.boundariness_self_grad_length_factor;
     a.b_up_factor = st.boundariness_underpressure_factor;
+    return a;
+}
+
+static PassB make_pass_b(apbf_ctx *ctx, const SolveOpts &o) {
+    FluidBufs &f = ctx->fl[ctx->fcur];
+    FluidBufs &alt = ctx->fl[ctx->fcur ^ 1];
+    const apbf_settings &st = ctx->settings;
+    PassB b;
+    b.pos = f.pos;
+    b.pos_out = alt.pos;
+    b.rec = ctx->solve_rec;
+    b.pk = ctx->solve_pk;
+    b.kw = f.kernel_width;
+    b.shift = ctx->shift;
+    b.radius = f.radius;
+    b.bmin = ctx->box_min;
+    b.bmax = ctx->box_max;
+    b.rot = ctx->box_rot;
+    b.nboxes = o.box_after ? ctx->n_boxes : 0u;
+    b.count = ctx->nb_count;
+    b.idx = ctx->nb_idx;
+    b.rcount = ctx->rev_count;
+    b.ridx = ctx->rev_idx;
+    b.stride = ctx->row_stride;
+    b.d_len = ctx->d_len;
+    b.st = ctx->status;
+    b.gk = st.gradient_kernel_id;
+    b.early_exit = o.converge ? 1 : 0;
+    b.lam_prev = f.lambda_prev;
+    b.lam_acc = ctx->lam_acc;
+    b.prev_mode = o.prev_mode;
+    b.acc_mode = o.acc_mode;
+    b.loop_offset = o.loop_offset;
+    b.max_passes = o.max_passes;
+    b.filt = ctx->filt;
+    b.bness = f.boundariness;
+    return b;
+}
+
+apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s, const SolveOpts &o) {
+    const bool converge = o.converge, learned = o.learned;
+    const uint32_t cap = ctx->cfg.particle_capacity;
+    FluidBufs &f = ctx->fl[ctx->fcur];
+    FluidBufs &alt = ctx->fl[ctx->fcur ^ 1];
+    const apbf_settings &st = ctx->settings;
+    const bool gauss = st.height_kernel_id == 1 && st.gradient_kernel_id == 1;
+    const PassA a = make_pass_a(ctx, o);
     const int g = ctx->red_blocks;
     const int lanes = ctx->tuning.gather_lanes;
     const int pb = ctx->tuning.pass_block == 128 ? 128 : 256;
@@ -752,35 +956,7 @@ apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s, const SolveOpts &o)
         apbf_status r = mlp_lambda(ctx, s, converge);
         if (r != APBF_OK) return r;
     }
-    PassB b;
-    b.pos = f.pos;
-    b.pos_out = alt.pos;
-    b.rec = ctx->solve_rec;
-    b.pk = ctx->solve_pk;
-    b.kw = f.kernel_width;
-    b.shift = ctx->shift;
-    b.radius = f.radius;
-    b.bmin = ctx->box_min;
-    b.bmax = ctx->box_max;
-    b.rot = ctx->box_rot;
-    b.nboxes = box_after ? ctx->n_boxes : 0u;
-    b.count = ctx->nb_count;
-    b.idx = ctx->nb_idx;
-    b.rcount = ctx->rev_count;
-    b.ridx = ctx->rev_idx;
-    b.stride = ctx->row_stride;
-    b.d_len = ctx->d_len;
-    b.st = ctx->status;
-    b.gk = st.gradient_kernel_id;
-    b.early_exit = converge ? 1 : 0;
-    b.lam_prev = f.lambda_prev;
-    b.lam_acc = ctx->lam_acc;
-    b.prev_mode = prev_mode;
-    b.acc_mode = acc_mode;
-    b.loop_offset = o.loop_offset;
-    b.max_passes = o.max_passes;
-    b.filt = ctx->filt;
-    b.bness = f.boundariness;
+    const PassB b = make_pass_b(ctx, o);
     APBF_BEFORE_LAUNCH(ctx, s, "k_delta");
     const int gd = grid_for(ctx, (uint32_t)std::min<uint64_t>((uint64_t)cap * lanes, 0xffffffffu), pb, bps);
     launch_lanes(lanes, [&](auto lc) {
@@ -796,6 +972,60 @@ apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s, const SolveOpts &o)
     f.pos = alt.pos;
     alt.pos = tmp;
     return APBF_OK;
+}
+
+bool solve_persistent_eligible(const apbf_ctx *ctx, const SolveOpts &o) {
+    const apbf_settings &st = ctx->settings;
+    return ctx->persistent_solve && ctx->coop_blocks > 0 && !ctx->in_batch && st.height_kernel_id == 1 &&
+           st.gradient_kernel_id == 1 &&
+           st.boundariness_calculation_method != 1 && !o.feature_mode && !o.learned && !o.acc_mode &&
+           !ctx->debug && !ctx->prof_on && o.max_passes >= 2;
+}
+
+apbf_status solve_persistent(apbf_ctx *ctx, cudaStream_t s, const SolveOpts &o) {
+    if (!solve_persistent_eligible(ctx, o)) return APBF_ERR_INVALID_ARG;
+    SolveOpts q = o;
+    q.loop_offset = -1;
+    q.box_after = true;  // decided per pass in the kernel
+    PassA a = make_pass_a(ctx, q);
+    PassB b = make_pass_b(ctx, q);
+    a.features = nullptr;
+    LoopArgs l;
+    l.pos_a = ctx->fl[ctx->fcur].pos;
+    l.pos_b = ctx->fl[ctx->fcur ^ 1].pos;
+    l.first = 1u;
+    l.max_passes = o.max_passes;
+    l.nboxes = ctx->n_boxes;
+    l.defer = (a.filt && a.method == 2) ? 1 : 0;
+    // barrier counters and pass sums start from zero on every launch
+    APBF_CUDA(cudaMemsetAsync(&ctx->status->bar_arrive, 0,
+                              offsetof(Status, loop_e2) + sizeof(unsigned long long) - offsetof(Status, bar_arrive), s));
+    const uint32_t want = (ctx->cfg.particle_capacity + 255u) / 256u;
+    const uint32_t grid = std::max(1u, std::min((uint32_t)ctx->coop_blocks, want));
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    APBF_BEFORE_LAUNCH(ctx, s, "k_solve_loop");
+    APBF_CUDA(cudaLaunchKernelEx(&cfg, k_solve_loop<true>, a, b, l));
+    APBF_AFTER_LAUNCH(ctx, s, "k_solve_loop");
+    return APBF_OK;
+}
+
+// Resident blocks of the persistent solve kernel (0: cooperative launches are
+// not available), computed once per context.
+int solve_persistent_blocks(int device, int num_sms) {
+    int coop = 0;
+    if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device) != cudaSuccess || !coop) return 0;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve_loop<true>, 256, 0) != cudaSuccess) return 0;
+    return per_sm * num_sms;
 }
 
 apbf_status reduce_fp64(apbf_ctx *ctx, double out[4], cudaStream_t s) {

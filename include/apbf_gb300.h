@@ -300,6 +300,15 @@ apbf_status apbf_set_debug(apbf_ctx *ctx, int enable);
  * All modes give the same results.  Tracing, debugging and sample recording run
  * a substep with per-kernel launches. */
 apbf_status apbf_set_solve_graph(apbf_ctx *ctx, int mode);
+/* Jacobi passes 1.. of apbf_substep as one persistent cooperative kernel (no
+ * counterpart in the reference): a resident grid runs every remaining pass, with
+ * grid barriers between the density and position phases instead of two kernel
+ * launches per pass.  Same results as the other forms.  Used for the Gauss kernels
+ * without the centre-of-mass boundariness (method 1), outside tracing, debugging
+ * and sample recording; otherwise apbf_set_solve_graph's form runs.  A barrier
+ * wait that gives up sets the spin-limit status (APBF_ERR_SPIN_LIMIT).  Fails with
+ * APBF_ERR_INVALID_ARG on a device without cooperative launches. */
+apbf_status apbf_set_persistent_solve(apbf_ctx *ctx, int enable);
 
 /* A batch of contexts (independent scenes on one device) whose substeps run as the
  * parallel branches of one CUDA graph: apbf_batch_substep advances every context
