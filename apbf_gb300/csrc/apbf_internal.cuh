@@ -351,6 +351,7 @@ struct SolveOpts {
     bool learned = false;     // the network's lambda replaces the computed one in this update
     int prev_mode = 0;        // lambda_prev: 0 off, 1 reset, 2 add the applied lambda
     bool projected = false;   // with prev_mode 2: pull-back up to the substep's accumulated push
+    bool later_pass = false;  // not the first pass of a substep (the widths' uniformity is known)
     int loop_offset = -1;     // >= 0: a pass of the solve loop graph, number = pass_index + offset;
     uint32_t max_passes = 0;  //   skipped from max_passes on, box after it unless it is the last
 };

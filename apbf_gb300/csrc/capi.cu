@@ -505,6 +505,7 @@ apbf_status substep_body(apbf_ctx *ctx, float dt, cudaStream_t s, bool capture) 
         }
         SolveOpts o;
         o.box_after = it + 1 < st.solver_iterations;
+        o.later_pass = it > 0;
         o.converge = converge;
         o.feature_mode = it == 0 && (learned || recording) ? 1 : 0;
         o.acc_mode = recording && (uint32_t)it < ctx->rec_iterations ? (it == 0 ? 1 : 2) : 0;

@@ -242,6 +242,7 @@ __global__ void __launch_bounds__(kRowsCta) k_mlp_lambda(const float *__restrict
                     sh.y = f2i(sd.y * sc);
                     sh.z = f2i(sd.z * sc);
                 }
+                sh.w = shift[r].w;  // the density pass's deferred-filter flag
                 shift[r] = sh;
             }
     }

@@ -59,10 +59,11 @@ struct PassA {
     const uint32_t *count;
     const uint32_t *idx;
     uint32_t stride;
-    float *lambda;
+    float *lambda;  // non-null (debug): the pass's lambda
     int4 *shift;
     float4 *rec;  // per particle: lambda, Gauss ivd, Gauss norm, kernel width (read by k_delta)
     int4 *pk;     // per particle: position xyz and the applied lambda (read by k_delta when widths are uniform)
+    int rec_if_mixed;  // 1 (passes after the first): rec only when the widths are not all equal
     uint32_t *dbg_dens;
     int4 *dbg_grad;
     uint32_t *dbg_sq;
@@ -205,7 +206,7 @@ struct PassSums {
 // Every lane of the group must call it (group shuffles).
 template <bool GAUSS, int L, bool XTRA>
 __device__ __forceinline__ void density_one(const PassA &a, uint32_t i_raw, uint32_t n, uint32_t sub, bool defer,
-                                            PassSums &ps) {
+                                            bool write_rec, PassSums &ps) {
     {
         const bool valid = i_raw < n;
         const uint32_t i = valid ? i_raw : 0u;
@@ -313,7 +314,7 @@ __device__ __forceinline__ void density_one(const PassA &a, uint32_t i_raw, uint
         }
         float lam = under / (ird * ird * (sqs + 0.01f));
         lam /= a.rmin3 / ird * im;
-        a.lambda[i] = lam;
+        if (a.lambda) a.lambda[i] = lam;
         // The lambda this pass applies: the reference applies only pushes (lambda < 0,
         // incompressibility_2.comp:106, incompressibility_3.comp:63).  Projected mode
         // (warm-started solve) also applies a pull-back lambda > 0 where earlier passes
@@ -326,7 +327,7 @@ __device__ __forceinline__ void density_one(const PassA &a, uint32_t i_raw, uint
             if (applied > 0.0f) pull = under * (applied / lam);
             else applied = 0.0f;
         }
-        a.rec[i] = make_float4(applied, c.ivd, c.norm, kw);
+        if (write_rec) a.rec[i] = make_float4(applied, c.ivd, c.norm, kw);
         a.pk[i] = make_int4(p.x, p.y, p.z, __float_as_int(applied));
         ps.kwlo = min(ps.kwlo, __float_as_uint(kw));
         ps.kwhi = max(ps.kwhi, __float_as_uint(kw));
@@ -351,10 +352,13 @@ __device__ __forceinline__ void density_one(const PassA &a, uint32_t i_raw, uint
         } else if (!(lam >= 0.0f)) {
             set_flag(a.st, APBF_FLAG_NONFINITE);  // NaN lambda: no shift (int(NaN) = 0)
         }
-        a.shift[i] = sh;
-        // incompressibility_3.comp:41-46,60: filter (only changes a non-zero boundariness)
+        // incompressibility_3.comp:41-46,60: filter (only changes a non-zero boundariness);
+        // deferred, it is recorded for particles with boundariness, flagged in shift.w
         if (defer) {
-            a.filt[i] = make_int4(gx, gy, gz, b > 0.0f ? 1 : 0);
+            if (b > 0.0f) {
+                a.filt[i] = make_int4(gx, gy, gz, 1);
+                sh.w = 1;
+            }
         } else if (a.method == 2 && b > 0.0f) {
             float3 ed;
             if (filter_dir(gx, gy, gz, ed)) {
@@ -381,6 +385,7 @@ __device__ __forceinline__ void density_one(const PassA &a, uint32_t i_raw, uint
                 }
             }
         }
+        a.shift[i] = sh;
         a.bness[i] = b;
         const float ratio = __fmaf_rn(density, ird, -1.0f);  // one rounding of the exact product - 1
         ps.e1 += err_fix(ratio > 0.0f ? ratio : pull);
@@ -449,11 +454,13 @@ __global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) 
     if (skip) return;  // uniform over the grid
     const uint32_t n = a.d_len[kLenParticles];
     const uint32_t sub = threadIdx.x % L;
+    // passes after the first: the widths' uniformity of the first pass still holds
+    const bool write_rec = !(a.rec_if_mixed && a.st->kw_uniform != 0u);
     PassSums ps;
     // the block iterates as a whole (uniform trip count: the group shuffles need every lane)
     const uint32_t gpb = blockDim.x / L;
     for (uint32_t base = blockIdx.x * gpb; base < n; base += gridDim.x * gpb)
-        density_one<GAUSS, L, XTRA>(a, base + threadIdx.x / L, n, sub, defer, ps);
+        density_one<GAUSS, L, XTRA>(a, base + threadIdx.x / L, n, sub, defer, write_rec, ps);
     const PassSums bs = block_pass_sums(ps);
     __shared__ bool s_last;
     if (threadIdx.x == 0) {
@@ -587,16 +594,17 @@ __device__ __forceinline__ void delta_one(const PassB &a, uint32_t j_raw, uint32
         int32_t ax, ay, az;
         const uint32_t cnt = valid ? cnt_arr[j] : 0u;
         const uint32_t *row = idx_arr + j;
+        // the self shift (incompressibility_2.comp:106-109); w flags a deferred filter
+        const int4 shj = valid ? a.shift[j] : make_int4(0, 0, 0, 0);
         float3 ed = make_float3(0.f, 0.f, 0.f);
         bool fil = false, hit = false;  // this particle's deferred filter, and whether a neighbour cleared it
-        if (filter && valid) {
+        if (filter && shj.w != 0) {
             const int4 fj = a.filt[j];
-            fil = fj.w != 0 && filter_dir(fj.x, fj.y, fj.z, ed);
+            fil = filter_dir(fj.x, fj.y, fj.z, ed);
         }
-        // the sums start from the self shift (incompressibility_2.comp:106-109) on the
-        // first lane: wrapping integer sums are order-free, and the load is in flight
-        // with the particle's other data
-        const int4 sh = (valid && sub == 0) ? a.shift[j] : make_int4(0, 0, 0, 0);
+        // the sums start from the self shift on the first lane: wrapping integer sums
+        // are order-free, and the load is in flight with the particle's other data
+        const int4 sh = sub == 0 ? shj : make_int4(0, 0, 0, 0);
         const float rj = a.radius[j];
         int3 acc = packed ? delta_row<GAUSS, L, true>(a, row, cnt, j, sub, p, cj, fil, ed, hit, sh)
                           : delta_row<GAUSS, L, false>(a, row, cnt, j, sub, p, cj, fil, ed, hit, sh);
@@ -620,7 +628,7 @@ __device__ __forceinline__ void delta_one(const PassB &a, uint32_t j_raw, uint32
         if (nboxes) out = box_push(out, rj, j, a.bmin, a.bmax, a.rot, nboxes);
         a.pos_out[j] = out;
         if (a.prev_mode | a.acc_mode) {
-            const float lj = reinterpret_cast<const float *>(a.rec + j)[0];  // applied (learned) lambda
+            const float lj = __int_as_float(a.pk[j].w);  // applied (learned) lambda
             accumulate(a.lam_prev, a.prev_mode, j, lj);
             accumulate(a.lam_acc, a.acc_mode, j, lj);
         }
@@ -630,9 +638,10 @@ __device__ __forceinline__ void delta_one(const PassB &a, uint32_t j_raw, uint32
 // A converged pass (no position update) of particle j: the deferred filter still
 // belongs to it, the positions are copied through and nothing is applied.
 __device__ __forceinline__ void delta_skip_filter(const PassB &a, uint32_t j) {
+    if (!a.shift[j].w) return;
     const int4 fj = a.filt[j];
     float3 ed;
-    if (!fj.w || !filter_dir(fj.x, fj.y, fj.z, ed)) return;
+    if (!filter_dir(fj.x, fj.y, fj.z, ed)) return;
     const int4 p = a.pos[j];
     for (uint32_t k = 0; k < a.count[j]; ++k)
         if (gauss_filter_hit(ed, fdiff(p, a.pos[a.idx[(size_t)k * a.stride + j]]))) {
@@ -760,7 +769,7 @@ __global__ void __launch_bounds__(256, 4) k_solve_loop(PassA a, PassB b, LoopArg
     for (uint32_t pass = l.first; pass < l.max_passes; ++pass) {
         a.pos = cur;
         PassSums ps;
-        for (uint32_t i = t0; i < n; i += T) density_one<GAUSS, 1, false>(a, i, n, 0u, defer, ps);
+        for (uint32_t i = t0; i < n; i += T) density_one<GAUSS, 1, false>(a, i, n, 0u, defer, !packed, ps);
         const PassSums bs = block_pass_sums(ps);
         if (threadIdx.x == 0) {
             atomicAdd(&st->loop_e1, (unsigned long long)bs.e1);
@@ -856,10 +865,11 @@ static PassA make_pass_a(apbf_ctx *ctx, const SolveOpts &o) {
     a.count = ctx->nb_count;
     a.idx = ctx->nb_idx;
     a.stride = ctx->row_stride;
-    a.lambda = ctx->lambda;
+    a.lambda = ctx->debug ? ctx->lambda : nullptr;
     a.shift = ctx->shift;
     a.rec = ctx->solve_rec;
     a.pk = ctx->solve_pk;
+    a.rec_if_mixed = o.later_pass ? 1 : 0;
     a.dbg_dens = ctx->debug ? ctx->dbg_density : nullptr;
     a.dbg_grad = ctx->dbg_grad;
     a.dbg_sq = ctx->dbg_sq;
