@@ -280,6 +280,8 @@ def _make_ctx(spec, args, local, mode: int = 0, net=None):
                      density_error_target=args.error_target)
     ctx.load_scene(spec)
     ctx.set_solve_graph(args.graph_mode)
+    if getattr(args, "persistent", False):
+        ctx.set_persistent_solve(True)
     if net is not None:
         ctx.mlp_load(net.params)
     if mode:
@@ -498,7 +500,7 @@ def run_ours(args) -> None:
                        "converged_substeps": head["converged_substeps"], "presteps": head["presteps"],
                        "dt": spec.dt, "adaptive": not spec.basic_pbf, "pairs": head["pairs"],
                        "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas x{world}",
-                       "graph_mode": args.graph_mode,
+                       "graph_mode": args.graph_mode, "persistent_solve": bool(args.persistent),
                        "tuning": head["tuning"]},
             "state_after": head["state_after"],
             "plain": plain or None,
@@ -772,6 +774,8 @@ def main() -> None:
     ap.add_argument("--graph-mode", type=int, default=2, choices=(0, 1, 2),
                     help="0 per-kernel launches, 1 solve loop as a graph, 2 whole substep as a graph")
     ap.add_argument("--prof-steps", type=int, default=8, help="traced substeps after the timed ones (kernel shares)")
+    ap.add_argument("--persistent", action="store_true",
+                    help="Jacobi passes 1.. as one persistent cooperative kernel (apbf_set_persistent_solve)")
     ap.add_argument("--ws-min-neighbors", type=float, default=16.0)
     ap.add_argument("--ws-omega", type=float, default=2.0)
     args = ap.parse_args()
