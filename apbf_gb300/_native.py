@@ -125,6 +125,13 @@ class NeighborsView(C.Structure):
     ]
 
 
+class HostFluid(C.Structure):
+    """apbf_host_fluid: host pointers of the particle lists (null fields are skipped)."""
+    _fields_ = [(name, C.c_void_p) for name in (
+        "position", "velocity", "inverse_mass", "radius", "pos_backup", "transferring", "target_radius",
+        "kernel_width", "boundariness", "boundary_distance", "lambda_prev")]
+
+
 class StatusInfo(C.Structure):
     _fields_ = [
         ("flags", C.c_uint32),
@@ -202,6 +209,8 @@ SIGNATURES = {
     "apbf_set_warm_start": (_ST, [_P, C.c_int]),
     "apbf_set_solve_graph": (_ST, [_P, C.c_int]),
     "apbf_set_persistent_solve": (_ST, [_P, C.c_int]),
+    "apbf_fluid_write": (_ST, [_P, _P, C.c_uint32, _P]),
+    "apbf_fluid_read": (_ST, [_P, _P, C.c_uint32, _P, _P]),
     "apbf_batch_create": (_ST, [_P, C.c_uint32, _P]),
     "apbf_batch_substep": (_ST, [_P, C.c_float, _P]),
     "apbf_batch_destroy": (_ST, [_P]),

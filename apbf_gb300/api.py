@@ -302,6 +302,40 @@ class Context:
         torch.cuda.synchronize(self.device)
         self.set_lengths(n, nt, stream)
 
+    @staticmethod
+    def _host_fluid(host: dict) -> N.HostFluid:
+        hf = N.HostFluid()
+        for name, _ in N.HostFluid._fields_:
+            a = host.get(name)
+            if a is None:
+                continue
+            if isinstance(a, torch.Tensor):
+                if a.is_cuda or not a.is_contiguous():
+                    raise ValueError(f"{name}: a contiguous host tensor is needed")
+                setattr(hf, name, a.data_ptr())
+            else:
+                if not a.flags["C_CONTIGUOUS"]:
+                    raise ValueError(f"{name}: a C-contiguous array is needed")
+                setattr(hf, name, a.ctypes.data)
+        return hf
+
+    def fluid_write(self, host: dict, count: int, stream=None) -> None:
+        """apbf_fluid_write: `count` particles from host arrays (the FLUID_FIELDS layout,
+        plus an optional 'lambda_prev'; numpy arrays or host tensors, pinned for
+        asynchronous copies) into the lists, and the particle length; absent fields keep
+        their device values.  Stream-ordered: keep the arrays alive until it has run."""
+        hf = self._host_fluid(host)
+        N.check(self.lib.apbf_fluid_write(self.handle, C.byref(hf), int(count), _stream_handle(stream)),
+                "apbf_fluid_write")
+
+    def fluid_read(self, host: dict, max_count: int, count_out, stream=None) -> None:
+        """apbf_fluid_read: enqueues the copy of the particle length into count_out (a
+        one-element int32 host tensor) and of up to max_count particles into the given
+        host arrays.  Valid after the stream is synchronised."""
+        hf = self._host_fluid(host)
+        N.check(self.lib.apbf_fluid_read(self.handle, C.byref(hf), int(max_count), C.c_void_p(count_out.data_ptr()),
+                                         _stream_handle(stream)), "apbf_fluid_read")
+
     def download(self, stream=None) -> tuple[dict, dict]:
         """Host copy of the current lists (numpy), lengths applied."""
         n, nt = self.lengths(stream)

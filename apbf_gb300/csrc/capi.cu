@@ -33,6 +33,9 @@ apbf_status dalloc(T **p, size_t count, std::vector<void *> &owned) {
 }
 
 }  // namespace
+
+// gpu_list::set_length from a host value, stream-ordered (no synchronisation).
+__global__ void k_set_length(uint32_t *d_len, uint32_t slot, uint32_t v) { d_len[slot] = v; }
 }  // namespace apbf
 
 using namespace apbf;
@@ -392,6 +395,54 @@ apbf_status apbf_set_lengths(apbf_ctx *ctx, uint32_t np, uint32_t nt, void *stre
     // a new state has no lambda history (the warm start's previous-substep feature)
     APBF_CUDA(cudaMemsetAsync(ctx->fl[ctx->fcur].lambda_prev, 0, (size_t)ctx->cfg.particle_capacity * sizeof(float), s));
     APBF_CUDA(cudaStreamSynchronize(s));
+    return APBF_OK;
+}
+
+apbf_status apbf_fluid_write(apbf_ctx *ctx, const apbf_host_fluid *in, uint32_t count, void *stream) {
+    if (!ctx || !in) return APBF_ERR_INVALID_ARG;
+    if (count > ctx->cfg.particle_capacity) {
+        set_error("apbf_fluid_write: count above the particle capacity");
+        return APBF_ERR_INVALID_ARG;
+    }
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    const FluidBufs &f = ctx->fl[ctx->fcur];
+    const size_t n = count;
+    const struct {
+        void *dst;
+        const void *src;
+        size_t bytes;
+    } fields[] = {{f.pos, in->position, 16}, {f.vel, in->velocity, 16}, {f.inv_mass, in->inverse_mass, 4},
+                  {f.radius, in->radius, 4}, {f.pos_backup, in->pos_backup, 16}, {f.transferring, in->transferring, 4},
+                  {f.target_radius, in->target_radius, 4}, {f.kernel_width, in->kernel_width, 4},
+                  {f.boundariness, in->boundariness, 4}, {f.boundary_distance, in->boundary_distance, 4},
+                  {f.lambda_prev, in->lambda_prev, 4}};
+    for (const auto &fd : fields)
+        if (fd.src && n) APBF_CUDA(cudaMemcpyAsync(fd.dst, fd.src, n * fd.bytes, cudaMemcpyHostToDevice, s));
+    APBF_BEFORE_LAUNCH(ctx, s, "k_set_length");
+    apbf::k_set_length<<<1, 1, 0, s>>>(ctx->d_len, kLenParticles, count);
+    APBF_AFTER_LAUNCH(ctx, s, "k_set_length");
+    return APBF_OK;
+}
+
+apbf_status apbf_fluid_read(apbf_ctx *ctx, apbf_host_fluid *out, uint32_t max_count, uint32_t *h_count, void *stream) {
+    if (!ctx || !out || !h_count) return APBF_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    const FluidBufs &f = ctx->fl[ctx->fcur];
+    const size_t n = std::min(max_count, ctx->cfg.particle_capacity);
+    APBF_CUDA(cudaMemcpyAsync(h_count, ctx->d_len + kLenParticles, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    const struct {
+        void *dst;
+        const void *src;
+        size_t bytes;
+    } fields[] = {{out->position, f.pos, 16}, {out->velocity, f.vel, 16}, {out->inverse_mass, f.inv_mass, 4},
+                  {out->radius, f.radius, 4}, {out->pos_backup, f.pos_backup, 16},
+                  {out->transferring, f.transferring, 4}, {out->target_radius, f.target_radius, 4},
+                  {out->kernel_width, f.kernel_width, 4}, {out->boundariness, f.boundariness, 4},
+                  {out->boundary_distance, f.boundary_distance, 4}, {out->lambda_prev, f.lambda_prev, 4}};
+    for (const auto &fd : fields)
+        if (fd.dst && n) APBF_CUDA(cudaMemcpyAsync(fd.dst, fd.src, n * fd.bytes, cudaMemcpyDeviceToHost, s));
     return APBF_OK;
 }
 

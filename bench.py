@@ -725,34 +725,44 @@ def run_batch_e2e(batch, ctxs, args, dt) -> dict:
 
 
 def run_e2e(ctx, spec, args, local) -> dict:
-    """Per step: H2D of the full particle state from pinned host memory, one substep,
-    D2H of the full resulting state into pinned host memory."""
+    """Per step, through the C ABI's host-buffer calls: apbf_fluid_write of the full
+    particle state (the ten lists and the warm start's lambda history) from pinned
+    host memory, one apbf_substep, the new particle count (an emitter or split/merge
+    changes it), apbf_fluid_read of the full resulting state back into pinned host
+    memory, then a stream synchronisation."""
     import torch
 
     from apbf_gb300.api import FLUID_FIELDS
 
-    st, _ = ctx.download()
-    n = st["position"].shape[0]
-    host = {k: torch.from_numpy(np.ascontiguousarray(st[k]).view(np.int32 if FLUID_FIELDS[k][0] == torch.int32
-                                                                  else np.float32)).pin_memory()
-            for k in FLUID_FIELDS}
-    h2d = sum(t.numel() * 4 for t in host.values())
-    steps = max(3, min(args.steps, 10))
+    cap = ctx.capacity
+    host = {}
+    for k, (dt, comp) in FLUID_FIELDS.items():
+        host[k] = torch.empty((cap, comp) if comp > 1 else (cap,), dtype=dt).pin_memory()
+    host["lambda_prev"] = torch.empty(cap, dtype=torch.float32).pin_memory()
+    per_particle = sum(t[0].numel() * t.element_size() for t in host.values())
+    count = torch.zeros(1, dtype=torch.int32).pin_memory()
     stream = torch.cuda.current_stream()
+    n, _ = ctx.lengths()
+    ctx.fluid_read(host, n, count)  # the current state, as a host-driven caller holds it
+    stream.synchronize()
+    steps = max(3, min(args.steps, 10))
+    h2d = d2h = 0
+    done = 0
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(steps):
-        v = ctx.fluid_view()
-        for k, t in host.items():
-            v[k][:n].copy_(t.view(v[k][:n].shape), non_blocking=True)
+        ctx.fluid_write(host, n)
+        h2d += n * per_particle
         ctx.substep(spec.dt)
-        v = ctx.fluid_view()
-        for k, t in host.items():
-            t.view(v[k][:n].shape).copy_(v[k][:n], non_blocking=True)
+        n, _ = ctx.lengths()  # synchronises: the count the read needs
+        ctx.fluid_read(host, n, count)
+        d2h += n * per_particle + 4
+        done += n
         stream.synchronize()
     el = time.perf_counter() - t0
-    return {"value": n * steps / el, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(h2d),
-            "steps": steps}
+    return {"value": done / el, "unit": UNIT, "h2d_bytes_per_step": int(h2d / steps),
+            "d2h_bytes_per_step": int(d2h / steps), "steps": steps,
+            "api": "apbf_fluid_write + apbf_substep + apbf_get_lengths + apbf_fluid_read (C ABI, pinned host buffers)"}
 
 
 def main() -> None:

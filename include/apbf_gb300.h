@@ -130,6 +130,23 @@ typedef struct apbf_fluid_view {
     uint32_t *boundary_distance;
 } apbf_fluid_view;
 
+/* The particle lists in host memory (structure of arrays, one entry per particle);
+ * a null field is not copied.  lambda_prev is the warm start's per-particle history
+ * (no reference counterpart). */
+typedef struct apbf_host_fluid {
+    int32_t *position;     /* int4 (w: library scratch, see apbf_fluid_view) */
+    float *velocity;       /* float4 */
+    float *inverse_mass;
+    float *radius;
+    int32_t *pos_backup;   /* int4 */
+    uint32_t *transferring;
+    float *target_radius;
+    float *kernel_width;
+    float *boundariness;
+    uint32_t *boundary_distance;
+    float *lambda_prev;
+} apbf_host_fluid;
+
 /* transfers = indexed_list<hidden_transfers> (source/list_definitions.h:16-18). */
 typedef struct apbf_transfers_view {
     uint32_t capacity;
@@ -232,6 +249,17 @@ apbf_status apbf_neighbors_get_view(apbf_ctx *ctx, apbf_neighbors_view *out);
 apbf_status apbf_set_lengths(apbf_ctx *ctx, uint32_t n_particles, uint32_t n_transfers, void *stream);
 /* Reads the device lengths (synchronises the stream). */
 apbf_status apbf_get_lengths(apbf_ctx *ctx, uint32_t *n_particles, uint32_t *n_transfers, void *stream);
+/* gpu_list::write().buffer() filled from the host + set_length (source/gpu_list.h:82-91,
+ * 173-180) for every particle list at once: enqueues the copies of `count` particles
+ * from host memory and sets the particle length; nothing else of the state changes
+ * (transfers, lambda history unless given).  Stream-ordered, no synchronisation; with
+ * pinned host memory the copies are asynchronous. */
+apbf_status apbf_fluid_write(apbf_ctx *ctx, const apbf_host_fluid *in, uint32_t count, void *stream);
+/* gpu_list::read (source/gpu_list.h:153-170) for every particle list at once: enqueues
+ * the copy of the particle length into *h_count and of the first max_count entries of
+ * every non-null field into host memory.  After the stream is synchronised, *h_count
+ * is the number of particles (entries past min(*h_count, max_count) are not state). */
+apbf_status apbf_fluid_read(apbf_ctx *ctx, apbf_host_fluid *out, uint32_t max_count, uint32_t *h_count, void *stream);
 
 /* ---- stages (each replaces one reference stage's apply()) ---- */
 /* velocity_handling::apply (source/velocity_handling.cpp:15-31). */
