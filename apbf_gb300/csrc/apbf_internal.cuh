@@ -186,6 +186,7 @@ struct apbf_ctx {
     int4 *filt = nullptr;          // per particle: gradient sum and boundariness > 0, for the deferred filter
     // learned warm start
     float *mlp_params = nullptr;   // FP32 parameter vector (mlp.cu)
+    unsigned char *mlp_image = nullptr;  // its packed BF16 form for the tensor-core inference (mlp.cu)
     float *features = nullptr;     // per particle: 8 features of the first density pass
     float4 *selfdir = nullptr;     // per particle: self-shift direction (xyz), inverse mass (w)
     float *lam_acc = nullptr;      // per particle: sum of min(0, lambda) over the recorded iterations
@@ -383,6 +384,10 @@ apbf_status mlp_train_step(float *P, float *m, float *v, float *partials, const 
                            float *loss_out, cudaStream_t s);
 uint32_t mlp_partials_floats(uint32_t nrows);
 apbf_status mlp_lambda(apbf_ctx *ctx, cudaStream_t s, bool early_exit);
+// Packs a parameter vector into the inference kernel's shared-memory image
+// (mlp_image_bytes() bytes, 16-byte aligned).
+apbf_status mlp_pack(const float *P, void *image, cudaStream_t s);
+size_t mlp_image_bytes();
 apbf_status record_samples(apbf_ctx *ctx, cudaStream_t s);
 apbf_status kw_from_boundary_distance(apbf_ctx *ctx, cudaStream_t s);
 apbf_status spread_kernel_width(apbf_ctx *ctx, cudaStream_t s);

@@ -176,6 +176,7 @@ apbf_status apbf_create(const apbf_config *cfg, apbf_ctx **out) {
     A(ctx->solve_pk, cap);
     A(ctx->filt, cap);
     A(ctx->mlp_params, kMlpParams);
+    A(ctx->mlp_image, mlp_image_bytes());
     A(ctx->features, (size_t)cap * 8);
     A(ctx->selfdir, cap);
     A(ctx->lam_acc, cap);
@@ -752,6 +753,8 @@ apbf_status apbf_mlp_load(apbf_ctx *ctx, const float *d_params, void *stream) {
     if (!ctx || !d_params) return APBF_ERR_INVALID_ARG;
     APBF_CUDA(cudaMemcpyAsync(ctx->mlp_params, d_params, kMlpParams * sizeof(float), cudaMemcpyDeviceToDevice,
                               (cudaStream_t)stream));
+    apbf_status r = mlp_pack(ctx->mlp_params, ctx->mlp_image, (cudaStream_t)stream);
+    if (r != APBF_OK) return r;
     ctx->mlp_loaded = 1;
     return APBF_OK;
 }

@@ -5,7 +5,8 @@
 // lambda, velocity divergence, the previous substep's applied lambda sum and its
 // neighbour mean) to an initial lambda that replaces the plain one in the first
 // position update.  Weights are BF16 on the tensor cores with FP32
-// accumulation (mma.sync m16n8k16); the master copy is FP32.
+// accumulation: inference with tcgen05.mma into TMEM (k_mlp_tc), training with
+// mma.sync m16n8k16 (k_mlp_grad); the master copy is FP32.
 //
 // Parameter vector (FP32), offsets in floats:
 //   0 mu[8]  8 inv_sigma[8]  16 W1[64][8]  528 b1[64]  592 W2[64][64]  4688 b2[64]
@@ -26,6 +27,8 @@
 // so the accumulators of n-tiles 2s and 2s+1 are exactly the A fragment of k-step s
 // of the next layer.
 #include <cuda_bf16.h>
+
+#include <algorithm>
 
 #include "apbf_internal.cuh"
 
@@ -178,74 +181,328 @@ __device__ __forceinline__ void forward_warp(const SmemW &w, const float *__rest
     }
 }
 
-// Inference over a batch: out[r] = y(r) in physical units (y * y_scale + y_mean).
-__global__ void __launch_bounds__(kRowsCta) k_mlp_forward(const float *__restrict__ P, const float *__restrict__ X,
-                                                           uint32_t nrows, float *__restrict__ out) {
-    __shared__ SmemW w;
-    load_weights(w, P);
-    __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, q = lane & 3;
-    for (uint32_t base = blockIdx.x * kRowsCta; base < nrows; base += gridDim.x * kRowsCta) {
-        const uint32_t row0 = base + warp * kRowsWarp;
-        Acts A;
-        forward_warp(w, X, row0, nrows, A);
-        if (q == 0) {
+// ---- inference on the 5th-generation tensor cores (tcgen05, accumulators in TMEM) ----
+//
+// A CTA of 128 threads runs tiles of 128 rows; thread t owns row t.  The operands
+// of the two hidden layers sit in shared memory in the canonical K-major layout
+// without swizzle: 8-row x 16-byte core matrices, K-adjacent cores 128 B apart
+// (leading byte offset), 8-row groups 16 B x K apart (stride byte offset).  One
+// thread issues tcgen05.mma (M 128, N 64, K 16 per instruction, BF16 in, FP32
+// accumulators in 64 TMEM columns that both layers reuse), tcgen05.commit arrives
+// on an mbarrier, and every warp reads its 32 TMEM lanes back with tcgen05.ld.
+// Bias, ReLU, the 64 -> 1 output layer and the solver's guards run on the CUDA
+// cores in FP32.  Waits are bounded: a wait that gives up marks the outputs NaN
+// (and the status word, in the solver hook) and the kernel frees its TMEM.
+
+constexpr int kTcRows = 128;
+constexpr uint32_t kTcCols = 64;  // TMEM columns per CTA
+constexpr uint32_t kTcIdesc = (1u << 4)                // D: FP32
+                              | (1u << 7) | (1u << 10)  // A, B: BF16
+                              | ((64u >> 3) << 17)      // N = 64
+                              | ((128u >> 4) << 24);    // M = 128; A and B K-major
+
+// The network as the kernel keeps it in shared memory: BF16 weights in the operand
+// layout and the FP32 vectors.  Built once per parameter vector (k_mlp_pack) so
+// that a CTA fetches it with one bulk copy.
+struct TcImage {
+    unsigned char w1[kH * 16 * 2];  // B of layer 1: N 64 x K 16
+    unsigned char w2[kH * kH * 2];  // B of layer 2: N 64 x K 64
+    float b1[kH], b2[kH], w3[kH], mu[kF], is[kF];
+    float b3, ys, ym, om, nmin, pad[3];
+};
+static_assert(sizeof(TcImage) % 16 == 0, "bulk copies move multiples of 16 bytes");
+constexpr uint32_t kTcImageBytes = sizeof(TcImage);
+constexpr size_t kTcA1 = (sizeof(TcImage) + 1023) / 1024 * 1024;
+
+struct __align__(1024) TcSmem {
+    TcImage img;
+    unsigned char pad_[kTcA1 - sizeof(TcImage)];
+    unsigned char a1[kTcRows * 16 * 2];  // A of layer 1: M 128 x K 16 (normalised features)
+    unsigned char a2[kTcRows * kH * 2];  // A of layer 2: M 128 x K 64 (relu(layer 1))
+    unsigned long long bar;              // MMA completion
+    unsigned long long bar_w;            // arrival of the weight image
+    uint32_t tmem;
+};
+
+// Byte offset of element (row, k) of a K-major operand with K columns.
+__device__ __forceinline__ uint32_t core_off(uint32_t row, uint32_t k, uint32_t K) {
+    return (row >> 3) * (K * 16u) + (k >> 3) * 128u + (row & 7u) * 16u + (k & 7u) * 2u;
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Shared-memory matrix descriptor: start, leading and stride byte offsets (>> 4),
+// the descriptor version bit 46, no swizzle.
+__device__ __forceinline__ uint64_t tc_desc(const void *p, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((smem_u32(p) & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
+           (1ull << 46);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(kTcIdesc), "r"(accumulate));
+}
+__device__ __forceinline__ void tc_commit(unsigned long long *bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// Bounded wait for the mbarrier phase `parity`.
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, uint32_t parity) {
+    const uint32_t b = smem_u32(bar);
+    for (uint32_t it = 0; it < (1u << 20); ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(b), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// 16 FP32 columns of this thread's TMEM lane; the wait is tied to the registers so
+// that no use is scheduled before the load has completed.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                   "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]),
+                   "+r"(r[15])
+                 :
+                 : "memory");
 #pragma unroll
-            for (int t = 0; t < 2; ++t) {
-                const uint32_t r0 = row0 + 16 * t + g, r1 = r0 + 8;
-                if (r0 < nrows) out[r0] = A.y[t][0] * w.ys + w.ym;
-                if (r1 < nrows) out[r1] = A.y[t][1] * w.ys + w.ym;
-            }
-        }
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// Builds the image from the FP32 parameter vector, thread t of nt.
+__device__ __forceinline__ void build_image(TcImage &img, const float *__restrict__ P, int t0, int nt) {
+    for (int t = t0; t < kH * 16; t += nt) {
+        const int n = t >> 4, k = t & 15;
+        *reinterpret_cast<__nv_bfloat16 *>(img.w1 + core_off(n, k, 16)) =
+            __float2bfloat16_rn(k < kF ? P[kP_W1 + n * kF + k] : 0.0f);
+    }
+    for (int t = t0; t < kH * kH; t += nt) {
+        const int n = t >> 6, k = t & 63;
+        *reinterpret_cast<__nv_bfloat16 *>(img.w2 + core_off(n, k, kH)) = __float2bfloat16_rn(P[kP_W2 + t]);
+    }
+    for (int t = t0; t < kH; t += nt) {
+        img.b1[t] = P[kP_B1 + t];
+        img.b2[t] = P[kP_B2 + t];
+        img.w3[t] = P[kP_W3 + t];
+    }
+    for (int t = t0; t < kF; t += nt) {
+        img.mu[t] = P[kP_MU + t];
+        img.is[t] = P[kP_IS + t];
+    }
+    if (t0 == 0) {
+        img.b3 = P[kP_B3];
+        img.ys = P[kP_YS];
+        img.ym = P[kP_YM];
+        img.om = P[kP_OM];
+        img.nmin = P[kP_NMIN];
+        img.pad[0] = img.pad[1] = img.pad[2] = 0.0f;
     }
 }
 
-// The learned first correction: lambda_hat from the features of the first
-// density pass replaces the plain lambda in the solve record and in the self
-// shift (incompressibility_2.comp:106-109 with lambda_hat).
-__global__ void __launch_bounds__(kRowsCta) k_mlp_lambda(const float *__restrict__ P, const float *__restrict__ X,
-                                                          const float4 *__restrict__ selfdir, float4 *rec, int4 *pk,
-                                                          int4 *shift,
-                                                          const uint32_t *d_len, const Status *st, int early_exit) {
-    if (early_exit && *(volatile const uint32_t *)&st->converged) return;
-    __shared__ SmemW w;
-    load_weights(w, P);
-    __syncthreads();
-    const uint32_t n = d_len[kLenParticles];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, q = lane & 3;
-    for (uint32_t base = blockIdx.x * kRowsCta; base < n; base += gridDim.x * kRowsCta) {
-        const uint32_t row0 = base + warp * kRowsWarp;
-        Acts A;
-        forward_warp(w, X, row0, n, A);
-        // quad lane q writes row g of tile q/2 (q even: row g, odd: row g+8)
-#pragma unroll
-        for (int t = 0; t < 2; ++t)
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                if (q != 2 * t + h) continue;
-                const uint32_t r = row0 + 16 * t + g + 8 * h;
-                if (r >= n) continue;
-                float lam = A.y[t][h] * w.ys + w.ym;
-                const float l0 = X[(size_t)r * kF + 3];  // the plain lambda of this pass
-                if (w.om > 0.0f) lam = l0 < 0.0f ? fminf(fmaxf(lam, w.om * l0), l0) : 0.0f;
-                if (X[(size_t)r * kF] < w.nmin) lam = l0;  // too few neighbours: the plain lambda
-                lam = fminf(lam, 0.0f);
-                float4 rc = rec[r];
-                rc.x = lam;
-                rec[r] = rc;
-                pk[r].w = __float_as_int(lam);
-                const float4 sd = selfdir[r];  // selfGrad (xyz), inverse mass (w)
-                int4 sh = make_int4(0, 0, 0, 0);
-                if (lam < 0.0f) {
-                    const float sc = lam * sd.w * APBF_FIX;
-                    sh.x = f2i(sd.x * sc);
-                    sh.y = f2i(sd.y * sc);
-                    sh.z = f2i(sd.z * sc);
-                }
-                sh.w = shift[r].w;  // the density pass's deferred-filter flag
-                shift[r] = sh;
-            }
+__global__ void k_mlp_pack(const float *__restrict__ P, TcImage *img) { build_image(*img, P, threadIdx.x, blockDim.x); }
+
+struct TcOut {
+    // MODE 0: out[r] = the network's output in physical units
+    float *out;
+    // MODE 1 (the solver hook): lambda_hat with the guards replaces the plain lambda in
+    // the solve record, the packed record and the self shift
+    const float4 *selfdir;
+    float4 *rec;
+    int4 *pk;
+    int4 *shift;
+    Status *st;
+};
+
+// image != null: the weights arrive by one bulk copy (cp.async.bulk) of the packed
+// image; else every CTA builds them from the FP32 parameters.
+template <int MODE>
+__global__ void __launch_bounds__(kTcRows) k_mlp_tc(const float *__restrict__ P, const TcImage *image,
+                                                    const float *__restrict__ X, uint32_t nrows, const uint32_t *d_len,
+                                                    int early_exit, TcOut o) {
+    __shared__ TcSmem sm;
+    if (MODE == 1 && early_exit && *(volatile const uint32_t *)&o.st->converged) return;  // uniform
+    const uint32_t n = MODE == 1 ? d_len[kLenParticles] : nrows;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&sm.bar)) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&sm.bar_w)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        if (image) {
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(&sm.bar_w)),
+                         "r"(kTcImageBytes)
+                         : "memory");
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                    smem_u32(&sm.img)),
+                "l"(image), "r"(kTcImageBytes), "r"(smem_u32(&sm.bar_w))
+                : "memory");
+        }
     }
+    if (!image) build_image(sm.img, P, tid, blockDim.x);
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sm.tmem)),
+                     "r"(kTcCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+        tc_fence_before();
+    }
+    __syncthreads();
+    tc_fence_after();
+    bool ok = true;
+    unsigned long long *pending = &sm.bar_w;  // the barrier of a wait that gave up, and its phase
+    uint32_t pending_parity = 0;
+    if (image) ok = __syncthreads_and(mbar_wait(&sm.bar_w, 0u)) != 0;  // the weights are in
+    const uint32_t tmem = sm.tmem;
+    const uint32_t lane_tmem = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's 32 lanes
+    const uint64_t a1 = tc_desc(sm.a1, 128u, 256u), b1 = tc_desc(sm.img.w1, 128u, 256u);
+    uint32_t phase = 0;
+    for (uint32_t base = blockIdx.x * kTcRows; base < n && ok; base += gridDim.x * kTcRows) {
+        const uint32_t r = base + tid;
+        const bool valid = r < n;
+        // layer 1 operand: the normalised features (slots 8..15 zero)
+        float x[kF];
+#pragma unroll
+        for (int f = 0; f < kF; ++f) x[f] = valid ? (X[(size_t)r * kF + f] - sm.img.mu[f]) * sm.img.is[f] : 0.0f;
+        uint4 lo;
+        lo.x = pack_bf16(x[0], x[1]);
+        lo.y = pack_bf16(x[2], x[3]);
+        lo.z = pack_bf16(x[4], x[5]);
+        lo.w = pack_bf16(x[6], x[7]);
+        *reinterpret_cast<uint4 *>(sm.a1 + core_off(tid, 0, 16)) = lo;
+        *reinterpret_cast<uint4 *>(sm.a1 + core_off(tid, 8, 16)) = make_uint4(0u, 0u, 0u, 0u);
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (tid == 0) {
+            tc_mma(tmem, a1, b1, 0u);
+            tc_commit(&sm.bar);
+        }
+        ok = __syncthreads_and(mbar_wait(&sm.bar, phase)) != 0;
+        if (!ok) {
+            pending = &sm.bar;
+            pending_parity = phase;
+            break;
+        }
+        phase ^= 1u;
+        tc_fence_after();
+        // relu(layer 1 + b1) -> the layer-2 operand
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            float v[16];
+            tmem_ld16(lane_tmem + 16u * c, v);
+            uint4 h0, h1;
+            h0.x = pack_bf16(fmaxf(v[0] + sm.img.b1[16 * c + 0], 0.f), fmaxf(v[1] + sm.img.b1[16 * c + 1], 0.f));
+            h0.y = pack_bf16(fmaxf(v[2] + sm.img.b1[16 * c + 2], 0.f), fmaxf(v[3] + sm.img.b1[16 * c + 3], 0.f));
+            h0.z = pack_bf16(fmaxf(v[4] + sm.img.b1[16 * c + 4], 0.f), fmaxf(v[5] + sm.img.b1[16 * c + 5], 0.f));
+            h0.w = pack_bf16(fmaxf(v[6] + sm.img.b1[16 * c + 6], 0.f), fmaxf(v[7] + sm.img.b1[16 * c + 7], 0.f));
+            h1.x = pack_bf16(fmaxf(v[8] + sm.img.b1[16 * c + 8], 0.f), fmaxf(v[9] + sm.img.b1[16 * c + 9], 0.f));
+            h1.y = pack_bf16(fmaxf(v[10] + sm.img.b1[16 * c + 10], 0.f), fmaxf(v[11] + sm.img.b1[16 * c + 11], 0.f));
+            h1.z = pack_bf16(fmaxf(v[12] + sm.img.b1[16 * c + 12], 0.f), fmaxf(v[13] + sm.img.b1[16 * c + 13], 0.f));
+            h1.w = pack_bf16(fmaxf(v[14] + sm.img.b1[16 * c + 14], 0.f), fmaxf(v[15] + sm.img.b1[16 * c + 15], 0.f));
+            *reinterpret_cast<uint4 *>(sm.a2 + core_off(tid, 16 * c, kH)) = h0;
+            *reinterpret_cast<uint4 *>(sm.a2 + core_off(tid, 16 * c + 8, kH)) = h1;
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (tid == 0) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                tc_mma(tmem, tc_desc(sm.a2 + 256 * k, 128u, 1024u), tc_desc(sm.img.w2 + 256 * k, 128u, 1024u),
+                       k > 0 ? 1u : 0u);
+            tc_commit(&sm.bar);
+        }
+        ok = __syncthreads_and(mbar_wait(&sm.bar, phase)) != 0;
+        if (!ok) {
+            pending = &sm.bar;
+            pending_parity = phase;
+            break;
+        }
+        phase ^= 1u;
+        tc_fence_after();
+        // layer 3 on the CUDA cores: y = relu(layer 2 + b2) . w3 + b3
+        float y = sm.img.b3;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            float v[16];
+            tmem_ld16(lane_tmem + 16u * c, v);
+#pragma unroll
+            for (int i = 0; i < 16; ++i) y += fmaxf(v[i] + sm.img.b2[16 * c + i], 0.0f) * sm.img.w3[16 * c + i];
+        }
+        tc_fence_before();  // this tile's TMEM reads are done before the next tile's MMA
+        if (!valid) continue;
+        if (MODE == 0) {
+            o.out[r] = y * sm.img.ys + sm.img.ym;
+        } else {
+            float lam = y * sm.img.ys + sm.img.ym;
+            const float l0 = X[(size_t)r * kF + 3];  // the plain lambda of this pass
+            if (sm.img.om > 0.0f) lam = l0 < 0.0f ? fminf(fmaxf(lam, sm.img.om * l0), l0) : 0.0f;
+            if (X[(size_t)r * kF] < sm.img.nmin) lam = l0;  // too few neighbours: the plain lambda
+            lam = fminf(lam, 0.0f);
+            float4 rc = o.rec[r];
+            rc.x = lam;
+            o.rec[r] = rc;
+            o.pk[r].w = __float_as_int(lam);
+            const float4 sd = o.selfdir[r];  // selfGrad (xyz), inverse mass (w)
+            int4 sh = make_int4(0, 0, 0, 0);
+            if (lam < 0.0f) {
+                const float sc = lam * sd.w * APBF_FIX;
+                sh.x = f2i(sd.x * sc);
+                sh.y = f2i(sd.y * sc);
+                sh.z = f2i(sd.z * sc);
+            }
+            sh.w = o.shift[r].w;  // the density pass's deferred-filter flag
+            o.shift[r] = sh;
+        }
+    }
+    if (!ok) {
+        // a copy or an MMA that did not complete in time: its results are not used; wait
+        // (bounded) for it before the TMEM is freed, and report
+        mbar_wait(pending, pending_parity);
+        if (tid == 0) {
+            if (MODE == 1) set_flag(o.st, APBF_FLAG_SPIN_LIMIT);
+        }
+        if (MODE == 0)
+            for (uint32_t r = blockIdx.x * kTcRows + tid; r < n; r += gridDim.x * kTcRows) o.out[r] = __int_as_float(0x7fc00000);
+    }
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcCols) : "memory");
+    }
+}
+
+// Persistent grid: a few CTAs per SM, each loading the weights once.
+static int tc_grid(uint32_t rows) {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 152;
+    }
+    const uint32_t tiles = (rows + kTcRows - 1) / kTcRows;
+    const uint32_t cap = (uint32_t)sms * 6u;  // 6 x 64 TMEM columns of 512 per SM
+    return (int)std::max(1u, std::min(tiles, cap));
 }
 
 constexpr size_t kGradOffT = (sizeof(SmemW) + 15) / 16 * 16;
@@ -491,8 +748,9 @@ static_assert(kP_N == kMlpParams, "parameter vector size");
 
 apbf_status mlp_forward(const float *P, const float *X, uint32_t nrows, float *out, cudaStream_t s) {
     if (nrows == 0) return APBF_OK;
-    const uint32_t ctas = (nrows + kRowsCta - 1) / kRowsCta;
-    k_mlp_forward<<<ctas < 4096u ? ctas : 4096u, kRowsCta, 0, s>>>(P, X, nrows, out);
+    TcOut o = {};
+    o.out = out;
+    k_mlp_tc<0><<<tc_grid(nrows), kTcRows, 0, s>>>(P, nullptr, X, nrows, nullptr, 0, o);
     APBF_CUDA(cudaGetLastError());
     return APBF_OK;
 }
@@ -519,13 +777,25 @@ apbf_status mlp_train_step(float *P, float *m, float *v, float *partials, const 
 
 uint32_t mlp_partials_floats(uint32_t nrows) { return ((nrows + kRowsCta - 1) / kRowsCta) * (uint32_t)kP_N; }
 
+apbf_status mlp_pack(const float *P, void *image, cudaStream_t s) {
+    k_mlp_pack<<<1, 256, 0, s>>>(P, reinterpret_cast<TcImage *>(image));
+    APBF_CUDA(cudaGetLastError());
+    return APBF_OK;
+}
+
+size_t mlp_image_bytes() { return sizeof(TcImage); }
+
 apbf_status mlp_lambda(apbf_ctx *ctx, cudaStream_t s, bool early_exit) {
-    const uint32_t cap = ctx->cfg.particle_capacity;
-    const uint32_t ctas = (cap + kRowsCta - 1) / kRowsCta;
+    TcOut o = {};
+    o.selfdir = ctx->selfdir;
+    o.rec = ctx->solve_rec;
+    o.pk = ctx->solve_pk;
+    o.shift = ctx->shift;
+    o.st = ctx->status;
     APBF_BEFORE_LAUNCH(ctx, s, "k_mlp_lambda");
-    k_mlp_lambda<<<ctas < 2048u ? ctas : 2048u, kRowsCta, 0, s>>>(ctx->mlp_params, ctx->features, ctx->selfdir,
-                                                                  ctx->solve_rec, ctx->solve_pk, ctx->shift, ctx->d_len,
-                                                                  ctx->status, early_exit ? 1 : 0);
+    k_mlp_tc<1><<<tc_grid(ctx->cfg.particle_capacity), kTcRows, 0, s>>>(
+        ctx->mlp_params, reinterpret_cast<const TcImage *>(ctx->mlp_image), ctx->features, 0u, ctx->d_len,
+        early_exit ? 1 : 0, o);
     APBF_AFTER_LAUNCH(ctx, s, "k_mlp_lambda");
     return APBF_OK;
 }
