@@ -210,6 +210,7 @@ SIGNATURES = {
     "apbf_set_solve_graph": (_ST, [_P, C.c_int]),
     "apbf_set_persistent_solve": (_ST, [_P, C.c_int]),
     "apbf_fluid_write": (_ST, [_P, _P, C.c_uint32, _P]),
+    "apbf_batch_set_persistent_solve": (_ST, [_P, C.c_int]),
     "apbf_fluid_read": (_ST, [_P, _P, C.c_uint32, _P, _P]),
     "apbf_batch_create": (_ST, [_P, C.c_uint32, _P]),
     "apbf_batch_substep": (_ST, [_P, C.c_float, _P]),

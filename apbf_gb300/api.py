@@ -755,7 +755,8 @@ class algorithms:
 
 class Batch:
     """Independent scenes (contexts) advanced together: one graph launch per substep
-    whose parallel branches are the contexts' substeps."""
+    whose parallel branches are the contexts' substeps (optionally around one batched
+    persistent solve of their Jacobi passes after the first)."""
 
     def __init__(self, contexts: list):
         self.contexts = list(contexts)
@@ -768,6 +769,11 @@ class Batch:
     def substep(self, dt: float, stream=None) -> None:
         N.check(self.lib.apbf_batch_substep(self.handle, C.c_float(dt), _stream_handle(stream)),
                 "apbf_batch_substep")
+
+    def set_persistent_solve(self, enable: bool = True) -> None:
+        """True: the batched persistent solve; False (default): each scene's solve loop in its branch."""
+        N.check(self.lib.apbf_batch_set_persistent_solve(self.handle, 1 if enable else 0),
+                "apbf_batch_set_persistent_solve")
 
     def close(self) -> None:
         if getattr(self, "handle", None):

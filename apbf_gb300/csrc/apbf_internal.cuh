@@ -363,6 +363,17 @@ apbf_status incompressibility(apbf_ctx *ctx, cudaStream_t s, const SolveOpts &o 
 apbf_status solve_persistent(apbf_ctx *ctx, cudaStream_t s, const SolveOpts &o);
 bool solve_persistent_eligible(const apbf_ctx *ctx, const SolveOpts &o);
 int solve_persistent_blocks(int device, int num_sms);
+// The solve loops of a batch of scenes as one persistent cooperative kernel over a
+// device table of scenes (solver.cu): eligibility, table entry size and filling,
+// launch, resident grid.
+bool batch_solve_eligible(const apbf_ctx *ctx, const SolveOpts &o);
+size_t batch_scene_bytes();
+size_t batch_sync_bytes();
+uint32_t batch_max_scenes();
+void batch_scene_fill(apbf_ctx *ctx, const SolveOpts &o, void *entry);
+apbf_status solve_batch_launch(const void *d_table, uint32_t n_scenes, void *d_sync, unsigned long long *d_acc,
+                               int grid, cudaStream_t s);
+int solve_batch_blocks(int device, int num_sms);
 // Passes 1.. of a substep as one graph launch (a device-side while loop).
 apbf_status solve_loop(apbf_ctx *ctx, cudaStream_t s, const SolveOpts &o);
 // The same loop as a conditional node of the graph that stream s is capturing.
@@ -371,7 +382,12 @@ void destroy_solve_graphs(apbf_ctx *ctx);
 void destroy_substep_graphs(apbf_ctx *ctx);
 // Whole substeps as graphs (graph.cu): one context, or a batch of contexts as the
 // parallel branches of one graph.
-apbf_status substep_body(apbf_ctx *ctx, float dt, cudaStream_t s, bool capture);
+// defer_loop non-null: when the substep's passes 1.. qualify for a batched solve,
+// the body stops after the first pass, fills *defer_loop, sets *deferred and leaves
+// the passes and substep_post to the caller.
+apbf_status substep_body(apbf_ctx *ctx, float dt, cudaStream_t s, bool capture, SolveOpts *defer_loop = nullptr,
+                         bool *deferred = nullptr);
+apbf_status substep_post(apbf_ctx *ctx, cudaStream_t s);
 bool substep_graph_eligible(const apbf_ctx *ctx);
 apbf_status substep_graph(apbf_ctx *ctx, float dt, cudaStream_t s);
 HostState host_state(const apbf_ctx *ctx);

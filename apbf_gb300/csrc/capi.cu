@@ -506,7 +506,9 @@ namespace apbf {
 // The body of pool::update (pool.cpp:67-106) on stream s.  capture: s is being
 // captured into a substep graph, so the solve loop becomes a conditional node of
 // that graph instead of a launch of its own.
-apbf_status substep_body(apbf_ctx *ctx, float dt, cudaStream_t s, bool capture) {
+apbf_status substep_body(apbf_ctx *ctx, float dt, cudaStream_t s, bool capture, SolveOpts *defer_loop,
+                         bool *deferred) {
+    if (deferred) *deferred = false;
     const apbf_settings &st = ctx->settings;
     apbf_status r = emit(ctx, dt, s);  // new particles first (no reference counterpart)
     if (r != APBF_OK) return r;
@@ -567,6 +569,11 @@ apbf_status substep_body(apbf_ctx *ctx, float dt, cudaStream_t s, bool capture) 
         if (it == 1 && st.solver_iterations >= 2 && !recording) {
             SolveOpts q = o;
             q.max_passes = (uint32_t)st.solver_iterations;
+            if (defer_loop && deferred && batch_solve_eligible(ctx, q)) {  // passes 1.. in the batch's launch
+                *defer_loop = q;
+                *deferred = true;
+                return APBF_OK;
+            }
             if (solve_persistent_eligible(ctx, q)) {  // passes 1.. in one persistent launch
                 r = solve_persistent(ctx, s, q);
                 if (r != APBF_OK) return r;
@@ -582,6 +589,15 @@ apbf_status substep_body(apbf_ctx *ctx, float dt, cudaStream_t s, bool capture) 
         r = incompressibility(ctx, s, o);
         if (r != APBF_OK) return r;
     }
+    return substep_post(ctx, s);
+}
+
+// The end of a substep after its Jacobi passes: sample recording, update_transfers.
+apbf_status substep_post(apbf_ctx *ctx, cudaStream_t s) {
+    const apbf_settings &st = ctx->settings;
+    const bool adaptive = !st.basic_pbf;
+    const bool recording = ctx->rec_iterations > 0;
+    apbf_status r = APBF_OK;
     if (recording) {
         if (st.solver_iterations > 0) {
             r = record_samples(ctx, s);

@@ -282,12 +282,21 @@ struct apbf_batch {
     cudaStream_t stream = nullptr;
     cudaEvent_t fork = nullptr;
     std::vector<cudaEvent_t> join;
+    // batched solve: the scenes' passes 1.. in one persistent cooperative launch
+    int persistent = 0;  // apbf_batch_set_persistent_solve
+    int coop_grid = 0;                   // resident grid of that kernel (0: not available)
+    void *d_table = nullptr;             // device table of the scenes (one entry per context)
+    void *d_sync = nullptr;              // its grid barrier
+    unsigned long long *d_acc = nullptr; // the scenes' error sums
+    cudaEvent_t solved = nullptr;
+    std::vector<cudaEvent_t> pre;
     struct Entry {
         cudaGraph_t graph = nullptr;
         cudaGraphExec_t exec = nullptr;
         std::vector<HostState> before, after;
         std::vector<unsigned long long> version, mode, kernels;
         float dt = 0.0f;
+        void *h_table = nullptr;  // pinned host copy of the scene table this graph uploads
     };
     Entry cache[kSubstepGraphs];
     int next = 0;
@@ -296,6 +305,7 @@ struct apbf_batch {
 static void release(apbf_batch::Entry &e) {
     if (e.exec) cudaGraphExecDestroy(e.exec);
     if (e.graph) cudaGraphDestroy(e.graph);
+    if (e.h_table) cudaFreeHost(e.h_table);
     e = apbf_batch::Entry();
 }
 
@@ -316,11 +326,21 @@ extern "C" apbf_status apbf_batch_create(apbf_ctx *const *ctxs, uint32_t n, apbf
     apbf_batch *b = new apbf_batch();
     b->ctx.assign(ctxs, ctxs + n);
     b->join.resize(n, nullptr);
+    b->pre.resize(n, nullptr);
     bool ok = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) == cudaSuccess &&
-              cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) == cudaSuccess;
+              cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) == cudaSuccess &&
+              cudaEventCreateWithFlags(&b->solved, cudaEventDisableTiming) == cudaSuccess;
     for (uint32_t i = 0; ok && i < n; ++i)
         ok = cudaEventCreateWithFlags(&b->join[i], cudaEventDisableTiming) == cudaSuccess &&
+             cudaEventCreateWithFlags(&b->pre[i], cudaEventDisableTiming) == cudaSuccess &&
              ensure_streams(ctxs[i]) == APBF_OK;
+    if (ok && n <= batch_max_scenes()) {
+        b->coop_grid = solve_batch_blocks(ctxs[0]->device, ctxs[0]->num_sms);
+        if (b->coop_grid > 0)
+            ok = cudaMalloc(&b->d_table, (size_t)n * batch_scene_bytes()) == cudaSuccess &&
+                 cudaMalloc(&b->d_sync, batch_sync_bytes()) == cudaSuccess &&
+                 cudaMalloc((void **)&b->d_acc, (size_t)2 * n * sizeof(unsigned long long)) == cudaSuccess;
+    }
     if (!ok) {
         apbf_batch_destroy(b);
         set_error("apbf_batch_create: stream or event creation failed");
@@ -335,9 +355,22 @@ extern "C" apbf_status apbf_batch_destroy(apbf_batch *b) {
     for (auto &e : b->cache) release(e);
     for (auto ev : b->join)
         if (ev) cudaEventDestroy(ev);
+    for (auto ev : b->pre)
+        if (ev) cudaEventDestroy(ev);
+    if (b->solved) cudaEventDestroy(b->solved);
+    if (b->d_table) cudaFree(b->d_table);
+    if (b->d_sync) cudaFree(b->d_sync);
+    if (b->d_acc) cudaFree(b->d_acc);
     if (b->fork) cudaEventDestroy(b->fork);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
+    return APBF_OK;
+}
+
+extern "C" apbf_status apbf_batch_set_persistent_solve(apbf_batch *b, int enable) {
+    if (!b) return APBF_ERR_INVALID_ARG;
+    b->persistent = enable ? 1 : 0;
+    for (auto &e : b->cache) release(e);
     return APBF_OK;
 }
 
@@ -381,10 +414,18 @@ extern "C" apbf_status apbf_batch_substep(apbf_batch *b, float dt, void *stream)
     apbf_batch::Entry &e = b->cache[b->next];
     b->next = (b->next + 1) % kSubstepGraphs;
     release(e);
+    const bool batched = b->persistent && b->coop_grid > 0;
+    if (batched) APBF_CUDA(cudaMallocHost(&e.h_table, n * batch_scene_bytes()));  // before the capture
     apbf_status r = APBF_OK;
     APBF_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeRelaxed));
     APBF_CUDA(cudaEventRecord(b->fork, b->stream));
     e.kernels.assign(n, 0);
+    // Each context's substep up to its first Jacobi pass as a parallel branch; passes
+    // 1.. of every context that qualifies in one batched persistent launch; then the
+    // rest of each substep as a branch again.  Contexts that do not qualify run their
+    // whole substep in their branch.
+    std::vector<SolveOpts> opts(n);
+    std::vector<uint8_t> deferred(n, 0);
     for (size_t i = 0; i < n && r == APBF_OK; ++i) {
         apbf_ctx *c = b->ctx[i];
         cudaStream_t cs = c->capture_stream;
@@ -393,14 +434,43 @@ extern "C" apbf_status apbf_batch_substep(apbf_batch *b, float dt, void *stream)
             break;
         }
         c->capturing = true;
-        c->in_batch = true;  // parallel branches: no persistent solve (each would want the whole GPU)
-        r = substep_body(c, dt, cs, true);
+        c->in_batch = true;  // parallel branches: no persistent solve of their own
+        bool d = false;
+        r = substep_body(c, dt, cs, true, batched ? &opts[i] : nullptr, &d);
         c->in_batch = false;
-        c->capturing = false;
-        if (r == APBF_OK && (cudaEventRecord(b->join[i], cs) != cudaSuccess ||
-                             cudaStreamWaitEvent(b->stream, b->join[i], 0) != cudaSuccess))
+        deferred[i] = d ? 1 : 0;
+        if (!d) c->capturing = false;
+        cudaEvent_t ev = d ? b->pre[i] : b->join[i];
+        if (r == APBF_OK &&
+            (cudaEventRecord(ev, cs) != cudaSuccess || cudaStreamWaitEvent(b->stream, ev, 0) != cudaSuccess))
             r = APBF_ERR_CUDA;
     }
+    uint32_t m = 0;
+    for (size_t i = 0; i < n && r == APBF_OK; ++i)
+        if (deferred[i])
+            batch_scene_fill(b->ctx[i], opts[i], static_cast<char *>(e.h_table) + (size_t)m++ * batch_scene_bytes());
+    if (r == APBF_OK && m > 0) {
+        if (cudaMemcpyAsync(b->d_table, e.h_table, (size_t)m * batch_scene_bytes(), cudaMemcpyHostToDevice,
+                            b->stream) != cudaSuccess)
+            r = APBF_ERR_CUDA;
+        if (r == APBF_OK) r = solve_batch_launch(b->d_table, m, b->d_sync, b->d_acc, b->coop_grid, b->stream);
+        if (r == APBF_OK && cudaEventRecord(b->solved, b->stream) != cudaSuccess) r = APBF_ERR_CUDA;
+        for (size_t i = 0; i < n && r == APBF_OK; ++i) {
+            if (!deferred[i]) continue;
+            apbf_ctx *c = b->ctx[i];
+            cudaStream_t cs = c->capture_stream;
+            if (cudaStreamWaitEvent(cs, b->solved, 0) != cudaSuccess) {
+                r = APBF_ERR_CUDA;
+                break;
+            }
+            r = substep_post(c, cs);
+            c->capturing = false;
+            if (r == APBF_OK && (cudaEventRecord(b->join[i], cs) != cudaSuccess ||
+                                 cudaStreamWaitEvent(b->stream, b->join[i], 0) != cudaSuccess))
+                r = APBF_ERR_CUDA;
+        }
+    }
+    for (auto *c : b->ctx) c->capturing = false;
     cudaError_t ce = cudaStreamEndCapture(b->stream, &e.graph);
     if (r == APBF_OK && ce != cudaSuccess) r = cuda_check(ce, "cudaStreamEndCapture (batch)");
     if (r == APBF_OK && cudaGraphInstantiate(&e.exec, e.graph, 0) != cudaSuccess)

@@ -205,12 +205,12 @@ struct PassSums {
 // incompressibility_0..2 and the boundariness filter of incompressibility_3.
 // Every lane of the group must call it (group shuffles).
 template <bool GAUSS, int L, bool XTRA>
-__device__ __forceinline__ void density_one(const PassA &a, uint32_t i_raw, uint32_t n, uint32_t sub, bool defer,
-                                            bool write_rec, PassSums &ps) {
+__device__ __forceinline__ void density_one(const PassA &a, const int4 *__restrict__ pos, uint32_t i_raw, uint32_t n,
+                                            uint32_t sub, bool defer, bool write_rec, PassSums &ps) {
     {
         const bool valid = i_raw < n;
         const uint32_t i = valid ? i_raw : 0u;
-        const int4 p = a.pos[i];
+        const int4 p = pos[i];
         const float kw = a.kw[i];
         const KConst c = gauss_consts(kw);
         uint32_t dens = 0u;
@@ -238,7 +238,7 @@ __device__ __forceinline__ void density_one(const PassA &a, uint32_t i_raw, uint
                 jj[u] = k < cnt ? row[(size_t)k * a.stride] : i;
             }
 #pragma unroll
-            for (int u = 0; u < kUnroll; ++u) qq[u] = a.pos[jj[u]];
+            for (int u = 0; u < kUnroll; ++u) qq[u] = pos[jj[u]];
 #pragma unroll
             for (int u = 0; u < kUnroll; ++u) {
                 if (k0 + u * L >= cnt) break;
@@ -364,7 +364,7 @@ __device__ __forceinline__ void density_one(const PassA &a, uint32_t i_raw, uint
             if (filter_dir(gx, gy, gz, ed)) {
                 for (uint32_t k = 0; k < cnt; ++k) {
                     const uint32_t j = a.idx[(size_t)k * a.stride + i];
-                    const float3 d = fdiff(p, a.pos[j]);
+                    const float3 d = fdiff(p, pos[j]);
                     if (GAUSS) {
                         if (gauss_filter_hit(ed, d)) {
                             b = 0.0f;
@@ -460,7 +460,7 @@ __global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) 
     // the block iterates as a whole (uniform trip count: the group shuffles need every lane)
     const uint32_t gpb = blockDim.x / L;
     for (uint32_t base = blockIdx.x * gpb; base < n; base += gridDim.x * gpb)
-        density_one<GAUSS, L, XTRA>(a, base + threadIdx.x / L, n, sub, defer, write_rec, ps);
+        density_one<GAUSS, L, XTRA>(a, a.pos, base + threadIdx.x / L, n, sub, defer, write_rec, ps);
     const PassSums bs = block_pass_sums(ps);
     __shared__ bool s_last;
     if (threadIdx.x == 0) {
@@ -525,7 +525,8 @@ __device__ __forceinline__ void accumulate(float *dst, int mode, uint32_t j, flo
 // filter.  PACKED: the neighbours' packed records (position, applied lambda) with
 // j's own Gauss constants cj; else the solve records and the positions.
 template <bool GAUSS, int L, bool PACKED>
-__device__ __forceinline__ int3 delta_row(const PassB &a, const uint32_t *row, uint32_t cnt, uint32_t j, uint32_t sub,
+__device__ __forceinline__ int3 delta_row(const PassB &a, const int4 *__restrict__ pos, const uint32_t *row, uint32_t cnt,
+                                          uint32_t j, uint32_t sub,
                                           int4 p, KConst cj, bool fil, float3 ed, bool &hit, int4 start) {
     int32_t ax = start.x, ay = start.y, az = start.z;
     for (uint32_t k0 = sub; k0 < cnt; k0 += L * kUnroll) {
@@ -543,7 +544,7 @@ __device__ __forceinline__ int3 delta_row(const PassB &a, const uint32_t *row, u
                 qq[u] = a.pk[ii[u]];
             } else {
                 rr[u] = a.rec[ii[u]];
-                qq[u] = a.pos[ii[u]];
+                qq[u] = pos[ii[u]];
             }
         }
 #pragma unroll
@@ -583,13 +584,13 @@ __device__ __forceinline__ int3 delta_row(const PassB &a, const uint32_t *row, u
 // collision (nboxes > 0) and the lambda bookkeeping.  Every lane of the group
 // must call it (group shuffles).
 template <bool GAUSS, int L>
-__device__ __forceinline__ void delta_one(const PassB &a, uint32_t j_raw, uint32_t n, uint32_t sub, bool packed,
-                                          bool filter, const uint32_t *cnt_arr, const uint32_t *idx_arr,
-                                          uint32_t nboxes) {
+__device__ __forceinline__ void delta_one(const PassB &a, const int4 *__restrict__ pos, int4 *pos_out, uint32_t j_raw,
+                                          uint32_t n, uint32_t sub, bool packed, bool filter, const uint32_t *cnt_arr,
+                                          const uint32_t *idx_arr, uint32_t nboxes) {
     {
         const bool valid = j_raw < n;
         const uint32_t j = valid ? j_raw : 0u;
-        const int4 p = a.pos[j];
+        const int4 p = pos[j];
         const KConst cj = gauss_consts(packed ? a.kw[j] : 1.0f);
         int32_t ax, ay, az;
         const uint32_t cnt = valid ? cnt_arr[j] : 0u;
@@ -606,8 +607,8 @@ __device__ __forceinline__ void delta_one(const PassB &a, uint32_t j_raw, uint32
         // are order-free, and the load is in flight with the particle's other data
         const int4 sh = sub == 0 ? shj : make_int4(0, 0, 0, 0);
         const float rj = a.radius[j];
-        int3 acc = packed ? delta_row<GAUSS, L, true>(a, row, cnt, j, sub, p, cj, fil, ed, hit, sh)
-                          : delta_row<GAUSS, L, false>(a, row, cnt, j, sub, p, cj, fil, ed, hit, sh);
+        int3 acc = packed ? delta_row<GAUSS, L, true>(a, pos, row, cnt, j, sub, p, cj, fil, ed, hit, sh)
+                          : delta_row<GAUSS, L, false>(a, pos, row, cnt, j, sub, p, cj, fil, ed, hit, sh);
         ax = acc.x;
         ay = acc.y;
         az = acc.z;
@@ -626,7 +627,7 @@ __device__ __forceinline__ void delta_one(const PassB &a, uint32_t j_raw, uint32
         if (hit) a.bness[j] = 0.0f;
         int4 out = make_int4(wadd(p.x, ax), wadd(p.y, ay), wadd(p.z, az), p.w);
         if (nboxes) out = box_push(out, rj, j, a.bmin, a.bmax, a.rot, nboxes);
-        a.pos_out[j] = out;
+        pos_out[j] = out;
         if (a.prev_mode | a.acc_mode) {
             const float lj = __int_as_float(a.pk[j].w);  // applied (learned) lambda
             accumulate(a.lam_prev, a.prev_mode, j, lj);
@@ -637,14 +638,14 @@ __device__ __forceinline__ void delta_one(const PassB &a, uint32_t j_raw, uint32
 
 // A converged pass (no position update) of particle j: the deferred filter still
 // belongs to it, the positions are copied through and nothing is applied.
-__device__ __forceinline__ void delta_skip_filter(const PassB &a, uint32_t j) {
+__device__ __forceinline__ void delta_skip_filter(const PassB &a, const int4 *__restrict__ pos, uint32_t j) {
     if (!a.shift[j].w) return;
     const int4 fj = a.filt[j];
     float3 ed;
     if (!filter_dir(fj.x, fj.y, fj.z, ed)) return;
-    const int4 p = a.pos[j];
+    const int4 p = pos[j];
     for (uint32_t k = 0; k < a.count[j]; ++k)
-        if (gauss_filter_hit(ed, fdiff(p, a.pos[a.idx[(size_t)k * a.stride + j]]))) {
+        if (gauss_filter_hit(ed, fdiff(p, pos[a.idx[(size_t)k * a.stride + j]]))) {
             a.bness[j] = 0.0f;
             break;
         }
@@ -670,7 +671,7 @@ __global__ void __launch_bounds__(256, 4) k_delta(PassB a) {
     if (skip) {
         if (filter)  // converged: no position update, but the filter still belongs to this pass
             for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
-                delta_skip_filter(a, j);
+                delta_skip_filter(a, a.pos, j);
         for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
             delta_skip_copy(a, j);
         return;
@@ -685,7 +686,8 @@ __global__ void __launch_bounds__(256, 4) k_delta(PassB a) {
     const uint32_t sub = threadIdx.x % L;
     const uint32_t gpb = blockDim.x / L;
     for (uint32_t base = blockIdx.x * gpb; base < n; base += gridDim.x * gpb)
-        delta_one<GAUSS, L>(a, base + threadIdx.x / L, n, sub, packed, filter, cnt_arr, idx_arr, nboxes);
+        delta_one<GAUSS, L>(a, a.pos, a.pos_out, base + threadIdx.x / L, n, sub, packed, filter, cnt_arr, idx_arr,
+                            nboxes);
 }
 
 // ---- the solve loop as one persistent cooperative kernel ----
@@ -767,28 +769,26 @@ __global__ void __launch_bounds__(256, 4) k_solve_loop(PassA a, PassB b, LoopArg
     const uint32_t T = gridDim.x * blockDim.x, t0 = blockIdx.x * blockDim.x + threadIdx.x;
     int4 *cur = l.pos_a, *nxt = l.pos_b;
     for (uint32_t pass = l.first; pass < l.max_passes; ++pass) {
-        a.pos = cur;
         PassSums ps;
-        for (uint32_t i = t0; i < n; i += T) density_one<GAUSS, 1, false>(a, i, n, 0u, defer, !packed, ps);
+        for (uint32_t i = t0; i < n; i += T) density_one<GAUSS, 1, false>(a, cur, i, n, 0u, defer, !packed, ps);
         const PassSums bs = block_pass_sums(ps);
         if (threadIdx.x == 0) {
             atomicAdd(&st->loop_e1, (unsigned long long)bs.e1);
             atomicAdd(&st->loop_e2, (unsigned long long)bs.e2);
         }
         if (!grid_barrier(st, gen, &a, n)) return;
-        b.pos = cur;
-        b.pos_out = nxt;
         if (*(volatile uint32_t *)&st->converged != 0u) {
             // converged: no position update (the positions stay in cur), the deferred
             // filter still belongs to this pass
             for (uint32_t j = t0; j < n; j += T) {
-                if (defer) delta_skip_filter(b, j);
+                if (defer) delta_skip_filter(b, cur, j);
                 accumulate(b.lam_prev, b.prev_mode, j, 0.0f);
             }
             break;
         }
         const uint32_t nb = pass + 1u < l.max_passes ? l.nboxes : 0u;
-        for (uint32_t j = t0; j < n; j += T) delta_one<GAUSS, 1>(b, j, n, 0u, packed, defer, cnt_arr, idx_arr, nb);
+        for (uint32_t j = t0; j < n; j += T)
+            delta_one<GAUSS, 1>(b, cur, nxt, j, n, 0u, packed, defer, cnt_arr, idx_arr, nb);
         if (!grid_barrier(st, gen, nullptr, n)) return;
         int4 *t = cur;
         cur = nxt;
@@ -796,6 +796,197 @@ __global__ void __launch_bounds__(256, 4) k_solve_loop(PassA a, PassB b, LoopArg
     }
     if (cur != l.pos_a)  // an odd number of updates: bring the positions back to the caller's buffer
         for (uint32_t j = t0; j < n; j += T) l.pos_a[j] = cur[j];
+}
+
+// ---- the solve loops of a batch of scenes as one persistent cooperative kernel ----
+
+// One scene of a batched solve: its pass arguments, its two position buffers and
+// its loop limits (LoopArgs per scene).
+struct BatchScene {
+    PassA a;
+    PassB b;
+    LoopArgs l;
+};
+
+struct BatchSync {
+    uint32_t bar_arrive;  // blocks arrived at the current grid barrier
+    uint32_t bar_gen;     // grid barriers released so far
+    uint32_t pad[2];
+};
+
+// Grid barrier of the batched solve (bounded like grid_barrier).  fin: the last
+// block to arrive finishes the density pass of every scene that ran one (its
+// threads one scene each: error means from the scenes' integer sums, convergence).
+__device__ __forceinline__ bool batch_barrier(BatchSync *sy, uint32_t &gen, const BatchScene *tab, uint32_t S,
+                                              unsigned long long *acc, const uint32_t *s_n, const uint8_t *s_run,
+                                              bool fin) {
+    __syncthreads();
+    __shared__ uint32_t s_last, s_ok;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        s_last = atomicAdd(&sy->bar_arrive, 1u) + 1u == gridDim.x ? 1u : 0u;
+        s_ok = 1u;
+    }
+    __syncthreads();
+    if (s_last) {
+        __threadfence();
+        if (fin)
+            for (uint32_t sc = threadIdx.x; sc < S; sc += blockDim.x) {
+                if (!s_run[sc]) continue;
+                const unsigned long long t1 = *(volatile unsigned long long *)&acc[2 * sc];
+                const unsigned long long t2 = *(volatile unsigned long long *)&acc[2 * sc + 1];
+                acc[2 * sc] = 0ull;
+                acc[2 * sc + 1] = 0ull;
+                finish_pass(tab[sc].a, s_n[sc], (long long)t1, (long long)t2);
+            }
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            sy->bar_arrive = 0u;
+            __threadfence();
+            atomicAdd(&sy->bar_gen, 1u);  // release
+        }
+    } else if (threadIdx.x == 0) {
+        uint32_t spins = 0;
+        while (*(volatile uint32_t *)&sy->bar_gen == gen) {
+            if (++spins > kBarrierSpins) {
+                for (uint32_t sc = 0; sc < S; ++sc) set_flag(tab[sc].a.st, APBF_FLAG_SPIN_LIMIT);
+                s_ok = 0u;
+                break;
+            }
+            __nanosleep(64);
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    ++gen;
+    return s_ok != 0u;
+}
+
+constexpr uint32_t kBatchScenes = 256;  // scenes per batched solve (a finishing thread each)
+
+// Jacobi passes 1.. of every scene in the table (each until its own error target or
+// pass limit), the scenes' particles cut into units of one block: per pass the
+// density phase of every running scene, a grid barrier whose last block finishes
+// those scenes' passes, the position phase, a second barrier.  The per-particle
+// arithmetic is density_one / delta_one, as in the per-scene forms, so each scene
+// ends bit-identical to a solve of its own.
+__global__ void __launch_bounds__(256, 4) k_solve_batch(const BatchScene *__restrict__ tab, uint32_t S,
+                                                        BatchSync *sy, unsigned long long *acc) {
+    __shared__ uint32_t s_n[kBatchScenes], s_unit[kBatchScenes + 1], s_max[kBatchScenes];
+    __shared__ uint8_t s_run[kBatchScenes], s_conv[kBatchScenes], s_upd[kBatchScenes], s_done[kBatchScenes];
+    __shared__ uint8_t s_defer[kBatchScenes], s_packed[kBatchScenes], s_sym[kBatchScenes];
+    __shared__ uint32_t s_maxpass;
+    uint32_t gen = *(volatile uint32_t *)&sy->bar_gen;  // read before this block's first arrival
+    for (uint32_t sc = threadIdx.x; sc < S; sc += blockDim.x) {
+        const BatchScene &b = tab[sc];
+        const Status *st = b.a.st;
+        s_n[sc] = b.a.d_len[kLenParticles];
+        s_max[sc] = b.l.max_passes;
+        s_sym[sc] = st->range_min == st->range_max ? 1 : 0;
+        s_defer[sc] = (b.l.defer != 0 && s_sym[sc]) ? 1 : 0;
+        s_packed[sc] = st->kw_uniform != 0u ? 1 : 0;
+        s_done[sc] = (b.a.early_exit && *(volatile const uint32_t *)&st->converged) ? 1 : 0;  // pass 0 met the target
+        s_upd[sc] = 0;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {  // units of blockDim particles per scene, and the largest pass limit
+        uint32_t u = 0, mp = 0;
+        for (uint32_t sc = 0; sc < S; ++sc) {
+            s_unit[sc] = u;
+            u += (s_n[sc] + blockDim.x - 1) / blockDim.x;
+            mp = max(mp, s_max[sc]);
+        }
+        s_unit[S] = u;
+        s_maxpass = mp;
+    }
+    __syncthreads();
+    const uint32_t units = s_unit[S];
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint32_t pass = 1; pass < s_maxpass; ++pass) {
+        bool any = false;
+        for (uint32_t sc = 0; sc < S; ++sc) any = any || (!s_done[sc] && pass < s_max[sc]);
+        if (!any) break;  // uniform: every block holds the same flags
+        __syncthreads();
+        for (uint32_t sc = threadIdx.x; sc < S; sc += blockDim.x) s_run[sc] = (!s_done[sc] && pass < s_max[sc]) ? 1 : 0;
+        __syncthreads();
+        // density phase
+        for (uint32_t u = blockIdx.x; u < units; u += gridDim.x) {
+            uint32_t lo = 0, hi = S;  // the scene of unit u: s_unit[sc] <= u < s_unit[sc + 1]
+            while (hi - lo > 1) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (s_unit[mid] <= u) lo = mid;
+                else hi = mid;
+            }
+            const uint32_t sc = lo;
+            if (!s_run[sc]) continue;  // uniform over the block
+            const BatchScene &bs = tab[sc];
+            const int4 *cur = (s_upd[sc] & 1u) ? bs.l.pos_b : bs.l.pos_a;
+            const uint32_t i = (u - s_unit[sc]) * blockDim.x + threadIdx.x;
+            PassSums ps;
+            density_one<true, 1, false>(bs.a, cur, i, s_n[sc], 0u, s_defer[sc] != 0, !s_packed[sc], ps);
+            long long e1 = ps.e1, e2 = ps.e2;
+            for (int off = 16; off > 0; off >>= 1) {
+                e1 += __shfl_down_sync(0xffffffffu, e1, off);
+                e2 += __shfl_down_sync(0xffffffffu, e2, off);
+            }
+            if (lane == 0 && (e1 | e2)) {
+                atomicAdd(&acc[2 * sc], (unsigned long long)e1);
+                atomicAdd(&acc[2 * sc + 1], (unsigned long long)e2);
+            }
+        }
+        if (!batch_barrier(sy, gen, tab, S, acc, s_n, s_run, true)) return;
+        for (uint32_t sc = threadIdx.x; sc < S; sc += blockDim.x)
+            s_conv[sc] = (s_run[sc] && *(volatile const uint32_t *)&tab[sc].a.st->converged) ? 1 : 0;
+        __syncthreads();
+        // position phase
+        for (uint32_t u = blockIdx.x; u < units; u += gridDim.x) {
+            uint32_t lo = 0, hi = S;
+            while (hi - lo > 1) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (s_unit[mid] <= u) lo = mid;
+                else hi = mid;
+            }
+            const uint32_t sc = lo;
+            if (!s_run[sc]) continue;
+            const BatchScene &bs = tab[sc];
+            const PassB &b = bs.b;
+            const int4 *cur = (s_upd[sc] & 1u) ? bs.l.pos_b : bs.l.pos_a;
+            int4 *nxt = (s_upd[sc] & 1u) ? bs.l.pos_a : bs.l.pos_b;
+            const uint32_t j = (u - s_unit[sc]) * blockDim.x + threadIdx.x;
+            if (s_conv[sc]) {  // converged: the deferred filter of this pass, nothing applied
+                if (j < s_n[sc]) {
+                    if (s_defer[sc]) delta_skip_filter(b, cur, j);
+                    accumulate(b.lam_prev, b.prev_mode, j, 0.0f);
+                }
+                continue;
+            }
+            const uint32_t nb = pass + 1u < s_max[sc] ? bs.l.nboxes : 0u;
+            const uint32_t *cnt_arr = s_sym[sc] ? b.count : b.rcount;
+            const uint32_t *idx_arr = s_sym[sc] ? b.idx : b.ridx;
+            delta_one<true, 1>(b, cur, nxt, j, s_n[sc], 0u, s_packed[sc] != 0, s_defer[sc] != 0, cnt_arr, idx_arr, nb);
+        }
+        if (!batch_barrier(sy, gen, tab, S, acc, s_n, s_run, false)) return;
+        for (uint32_t sc = threadIdx.x; sc < S; sc += blockDim.x) {
+            if (!s_run[sc]) continue;
+            if (s_conv[sc]) s_done[sc] = 1;
+            else s_upd[sc] = (uint8_t)(s_upd[sc] + 1);
+        }
+        __syncthreads();
+    }
+    // scenes that end after an odd number of updates: positions back to their pos_a
+    for (uint32_t u = blockIdx.x; u < units; u += gridDim.x) {
+        uint32_t lo = 0, hi = S;
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (s_unit[mid] <= u) lo = mid;
+            else hi = mid;
+        }
+        const uint32_t sc = lo;
+        if (!(s_upd[sc] & 1u)) continue;
+        const uint32_t j = (u - s_unit[sc]) * blockDim.x + threadIdx.x;
+        if (j < s_n[sc]) tab[sc].l.pos_a[j] = tab[sc].l.pos_b[j];
+    }
 }
 
 __global__ void k_mass_volume(const float *inv_mass, const float *radius, const uint32_t *d_len, double *partials) {
@@ -1035,6 +1226,60 @@ int solve_persistent_blocks(int device, int num_sms) {
     if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device) != cudaSuccess || !coop) return 0;
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve_loop<true>, 256, 0) != cudaSuccess) return 0;
+    return per_sm * num_sms;
+}
+
+bool batch_solve_eligible(const apbf_ctx *ctx, const SolveOpts &o) {
+    const apbf_settings &st = ctx->settings;
+    return ctx->coop_blocks > 0 && st.height_kernel_id == 1 && st.gradient_kernel_id == 1 &&
+           st.boundariness_calculation_method != 1 && !o.feature_mode && !o.learned && !o.acc_mode && !ctx->debug &&
+           !ctx->prof_on && o.max_passes >= 2;
+}
+
+size_t batch_scene_bytes() { return sizeof(BatchScene); }
+size_t batch_sync_bytes() { return sizeof(BatchSync); }
+uint32_t batch_max_scenes() { return kBatchScenes; }
+
+void batch_scene_fill(apbf_ctx *ctx, const SolveOpts &o, void *entry) {
+    SolveOpts q = o;
+    q.loop_offset = -1;
+    q.box_after = true;  // decided per pass in the kernel
+    BatchScene &e = *reinterpret_cast<BatchScene *>(entry);
+    e.a = make_pass_a(ctx, q);
+    e.a.features = nullptr;
+    e.b = make_pass_b(ctx, q);
+    e.l.pos_a = ctx->fl[ctx->fcur].pos;
+    e.l.pos_b = ctx->fl[ctx->fcur ^ 1].pos;
+    e.l.first = 1u;
+    e.l.max_passes = o.max_passes;
+    e.l.nboxes = ctx->n_boxes;
+    e.l.defer = (e.a.filt && e.a.method == 2) ? 1 : 0;
+}
+
+apbf_status solve_batch_launch(const void *d_table, uint32_t n_scenes, void *d_sync, unsigned long long *d_acc,
+                               int grid, cudaStream_t s) {
+    if (n_scenes == 0 || n_scenes > kBatchScenes || grid <= 0) return APBF_ERR_INVALID_ARG;
+    APBF_CUDA(cudaMemsetAsync(d_sync, 0, sizeof(BatchSync), s));
+    APBF_CUDA(cudaMemsetAsync(d_acc, 0, (size_t)2 * n_scenes * sizeof(unsigned long long), s));
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(256);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    APBF_CUDA(cudaLaunchKernelEx(&cfg, k_solve_batch, reinterpret_cast<const BatchScene *>(d_table), n_scenes,
+                                 reinterpret_cast<BatchSync *>(d_sync), d_acc));
+    return APBF_OK;
+}
+
+int solve_batch_blocks(int device, int num_sms) {
+    int coop = 0;
+    if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device) != cudaSuccess || !coop) return 0;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve_batch, 256, 0) != cudaSuccess) return 0;
     return per_sm * num_sms;
 }
 

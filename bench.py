@@ -622,6 +622,7 @@ def run_batch(args) -> None:
     mode = N.WARM_LEARNED | N.WARM_PROJECTED
     ctxs = [make(sp, mode, net) for sp in specs]
     batch = Batch(ctxs)
+    batch.set_persistent_solve(args.batch_persistent)
     for _ in range(args.presteps if args.presteps >= 0 else 40):
         batch.substep(dt)
     for c in ctxs:
@@ -706,7 +707,9 @@ def run_batch(args) -> None:
                        "iterations": f"until mean density error <= {args.error_target} (max {args.max_iterations})",
                        "density_passes_per_scene_substep": passes,
                        "converged_scene_substeps": f"{conv}/{len(ctxs) * args.steps}",
-                       "launch": "one CUDA graph per substep, scenes as parallel branches",
+                       "launch": ("one CUDA graph per substep, scenes as parallel branches" +
+                                  (" around one persistent cooperative launch of every scene's Jacobi passes 1.."
+                                   if args.batch_persistent else "")),
                        "l2": "flushed between timed steps (256 MB write)"},
             "sequential": {"ms_per_step": seq_ms / args.steps,
                            "value": n_total * args.steps / (seq_ms / 1000.0),
@@ -813,6 +816,8 @@ def main() -> None:
     ap.add_argument("--graph-mode", type=int, default=2, choices=(0, 1, 2),
                     help="0 per-kernel launches, 1 solve loop as a graph, 2 whole substep as a graph")
     ap.add_argument("--prof-steps", type=int, default=8, help="traced substeps after the timed ones (kernel shares)")
+    ap.add_argument("--batch-persistent", action="store_true",
+                    help="batch64: every scene's Jacobi passes 1.. in one persistent cooperative launch")
     ap.add_argument("--persistent", action="store_true",
                     help="Jacobi passes 1.. as one persistent cooperative kernel (apbf_set_persistent_solve)")
     ap.add_argument("--ws-min-neighbors", type=float, default=16.0)

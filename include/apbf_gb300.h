@@ -338,15 +338,23 @@ apbf_status apbf_set_solve_graph(apbf_ctx *ctx, int mode);
  * APBF_ERR_INVALID_ARG on a device without cooperative launches. */
 apbf_status apbf_set_persistent_solve(apbf_ctx *ctx, int enable);
 
-/* A batch of contexts (independent scenes on one device) whose substeps run as the
- * parallel branches of one CUDA graph: apbf_batch_substep advances every context
- * by one substep with one graph launch (each scene keeps its own solve loop and
- * convergence).  The contexts stay usable on their own; no context may be in two
- * batches that run at the same time.  No counterpart in the reference. */
+/* A batch of contexts (independent scenes on one device) advanced by one CUDA graph
+ * launch per substep (apbf_batch_substep): every context's substep is a parallel
+ * branch of the graph, each scene with its own solve loop and convergence.  The
+ * contexts stay usable on their own; no context may be in two batches that run at
+ * the same time.  No counterpart in the reference. */
 typedef struct apbf_batch apbf_batch;
 apbf_status apbf_batch_create(apbf_ctx *const *ctxs, uint32_t n, apbf_batch **out);
 apbf_status apbf_batch_substep(apbf_batch *batch, float dt, void *stream);
 apbf_status apbf_batch_destroy(apbf_batch *batch);
+/* 1: the Jacobi passes 1.. of every context whose solve qualifies (see
+ * apbf_set_persistent_solve) run as one persistent cooperative launch over a device
+ * table of the scenes, between the branches' first passes and the rest of their
+ * substeps (each scene keeps its own target, pass limit and convergence; results
+ * bit-identical).  0 (default): each scene's solve loop stays in its branch, which
+ * overlaps the scenes' loops instead of running every pass of every scene in
+ * lockstep. */
+apbf_status apbf_batch_set_persistent_solve(apbf_batch *batch, int enable);
 
 /* Launch shapes (no counterpart in the reference).  apbf_autotune times every
  * candidate shape of the Jacobi passes on the context's current particle state and

@@ -76,6 +76,20 @@ def test_graph_runs_every_pass_without_target_after_converged_substeps(mode):
     ctx.close()
 
 
+def _warm_params(seed=0):
+    from oracle import mlp_oracle as M
+
+    rng = np.random.default_rng(seed)
+    p = np.zeros(M.P_N, np.float32)
+    p[M.P_IS:M.P_IS + 6] = 0.1
+    p[M.P_W1:M.P_B1] = rng.normal(size=M.H * M.F) * 0.3
+    p[M.P_W2:M.P_B2] = rng.normal(size=M.H * M.H) * 0.1
+    p[M.P_W3:M.P_B3] = rng.normal(size=M.H) * 0.05
+    p[M.P_YS] = 0.2
+    p[M.P_YM] = -0.3
+    return p
+
+
 def test_graph_matches_launches_with_warm_start():
     from oracle import mlp_oracle as M
 
@@ -150,30 +164,43 @@ def test_whole_substep_graph_with_warm_start():
     assert a[2:] == b[2:]
 
 
-def test_batch_matches_separate_contexts():
-    """Scenes of different sizes and kinds advanced by one graph launch per substep
-    end bit-identical to the same scenes advanced one context at a time."""
+@pytest.mark.parametrize("persistent", [True, False])
+def test_batch_matches_separate_contexts(persistent):
+    """Scenes of different sizes and kinds (plain and adaptive, different pass limits
+    and targets, one with the learned warm start and projected passes) advanced by
+    one graph launch per substep -- their solves as one batched persistent launch or
+    as loops in the scenes' branches -- end bit-identical to the same scenes advanced
+    one context at a time."""
+    import torch
+
+    from apbf_gb300 import _native as N
     from apbf_gb300.api import Batch, Context
 
     specs = [(scenes.dam_break(n_side=12), 128, 30, 1e-3), (scenes.dam_break(n_side=16, seed=2), 128, 30, 1e-3),
              (scenes.water_drop(total=20_000, seed=4, basic_pbf=True), 160, 40, 1e-3),
-             (scenes.water_drop(total=15_000, seed=5, basic_pbf=False), 256, 8, 0.0)]
+             (scenes.water_drop(total=15_000, seed=5, basic_pbf=False), 256, 8, 0.0),
+             (scenes.water_drop(total=12_000, seed=6, basic_pbf=True), 160, 12, 2e-3)]
+    warm = _warm_params()
 
-    def make(spec, maxn, it, tg):
+    def make(spec, maxn, it, tg, k):
         ctx = Context(particle_capacity=int(spec.n * 1.3) + 64, max_neighbors=maxn,
                       max_log2res=max(spec.log2res, 3))
         ctx.set_settings(basic_pbf=1 if spec.basic_pbf else 0, solver_iterations=it, density_error_target=tg)
         ctx.set_scene(spec.grid_min, spec.grid_max, spec.log2res, spec.acceleration)
         ctx.set_boxes(spec.box_min, spec.box_max)
         ctx.upload(spec.state)
+        if k == 4:  # the learned warm start and projected passes
+            ctx.mlp_load(torch.from_numpy(warm).cuda())
+            ctx.set_warm_start(N.WARM_LEARNED | N.WARM_PROJECTED)
         return ctx
 
     dt = specs[0][0].dt
-    batched = [make(*s) for s in specs]
+    batched = [make(*s, k) for k, s in enumerate(specs)]
     batch = Batch(batched)
+    batch.set_persistent_solve(persistent)
     for _ in range(8):
         batch.substep(dt)
-    single = [make(*s) for s in specs]
+    single = [make(*s, k) for k, s in enumerate(specs)]
     for c in single:
         for _ in range(8):
             c.substep(dt)
