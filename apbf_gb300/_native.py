@@ -152,7 +152,8 @@ class Emitter(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("gather_lanes", C.c_uint32), ("pass_block", C.c_uint32), ("pass_blocks_per_sm", C.c_uint32),
-                ("build_tiled", C.c_uint32), ("filter_in_density", C.c_uint32), ("reserved", C.c_uint32 * 3)]
+                ("build_tiled", C.c_uint32), ("filter_in_density", C.c_uint32), ("sort_digit_bits", C.c_uint32),
+                ("search_log2res", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class KernelTime(C.Structure):
@@ -210,6 +211,7 @@ SIGNATURES = {
     "apbf_set_solve_graph": (_ST, [_P, C.c_int]),
     "apbf_set_persistent_solve": (_ST, [_P, C.c_int]),
     "apbf_fluid_write": (_ST, [_P, _P, C.c_uint32, _P]),
+    "apbf_autotune_search": (_ST, [_P, _P, _P, _P]),
     "apbf_batch_set_persistent_solve": (_ST, [_P, C.c_int]),
     "apbf_fluid_read": (_ST, [_P, _P, C.c_uint32, _P, _P]),
     "apbf_batch_create": (_ST, [_P, C.c_uint32, _P]),

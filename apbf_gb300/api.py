@@ -176,7 +176,8 @@ class Context:
         N.check(self.lib.apbf_get_tuning(self.handle, C.byref(t)), "apbf_get_tuning")
         return {"gather_lanes": t.gather_lanes, "pass_block": t.pass_block,
                 "pass_blocks_per_sm": t.pass_blocks_per_sm, "build_tiled": t.build_tiled,
-                "filter_in_density": t.filter_in_density}
+                "filter_in_density": t.filter_in_density, "sort_digit_bits": t.sort_digit_bits,
+                "search_log2res": t.search_log2res}
 
     def set_neighborhood_search(self, method: int | str) -> None:
         """The neighbour search of substep(): "green" (the default) or "binary_search",
@@ -203,7 +204,8 @@ class Context:
 
     def set_tuning(self, gather_lanes: int | None = None, pass_block: int | None = None,
                    pass_blocks_per_sm: int | None = None, build_tiled: int | None = None,
-                   filter_in_density: int | None = None) -> None:
+                   filter_in_density: int | None = None, sort_digit_bits: int | None = None,
+                   search_log2res: int | None = None) -> None:
         t = N.Tuning()
         N.check(self.lib.apbf_get_tuning(self.handle, C.byref(t)), "apbf_get_tuning")
         if gather_lanes is not None:
@@ -216,6 +218,10 @@ class Context:
             t.build_tiled = build_tiled
         if filter_in_density is not None:
             t.filter_in_density = filter_in_density
+        if sort_digit_bits is not None:
+            t.sort_digit_bits = sort_digit_bits
+        if search_log2res is not None:
+            t.search_log2res = search_log2res
         N.check(self.lib.apbf_set_tuning(self.handle, C.byref(t)), "apbf_set_tuning")
 
     def autotune(self, stream=None) -> dict:
@@ -227,8 +233,20 @@ class Context:
         keys = [f"L{l}/B{b}/S{p}" for l in (1, 2, 4, 8) for b in (128, 256) for p in (2, 4, 8)]
         return {"gather_lanes": t.gather_lanes, "pass_block": t.pass_block,
                 "pass_blocks_per_sm": t.pass_blocks_per_sm, "build_tiled": t.build_tiled,
-                "filter_in_density": t.filter_in_density,
+                "filter_in_density": t.filter_in_density, "sort_digit_bits": t.sort_digit_bits,
+                "search_log2res": t.search_log2res,
                 "pass_ms": {k: round(float(v), 5) for k, v in zip(keys, ms)}}
+
+    def autotune_search(self, stream=None) -> dict:
+        """apbf_autotune_search: the sort digit width and the search grid of substep()
+        from timed candidates (state restored); returns the choice and the times (ms)."""
+        t = N.Tuning()
+        ms = (C.c_float * 6)()
+        N.check(self.lib.apbf_autotune_search(self.handle, _stream_handle(stream), C.byref(t), ms),
+                "apbf_autotune_search")
+        return {"sort_digit_bits": t.sort_digit_bits, "search_log2res": t.search_log2res,
+                "sort_ms": {f"{b} bits": round(float(ms[i]), 5) for i, b in enumerate((6, 7, 8))},
+                "search_ms": {f"L{d:+d}": round(float(ms[3 + i]), 5) for i, d in enumerate((-1, 0, 1))}}
 
     def set_solve_graph(self, mode: int | bool) -> None:
         """0: per-kernel launches; 1 (default): the Jacobi passes 1.. as one graph launch with a

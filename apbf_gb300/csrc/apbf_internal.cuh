@@ -249,7 +249,7 @@ struct apbf_ctx {
     apbf::ProfSlot *prof_open = nullptr;
     bool capturing = false;        // launches go into a graph being built: not counted
 
-    apbf_tuning tuning = {1u, 256u, 8u, 0u, 0u, {0u, 0u, 0u}};  // launch shapes (apbf_set_tuning / apbf_autotune)
+    apbf_tuning tuning = {1u, 256u, 8u, 0u, 0u, 0u, 0u, 0u};  // launch shapes (apbf_set_tuning / apbf_autotune)
 
     // solve loop graphs (graph.cu)
     int use_graphs = 1;

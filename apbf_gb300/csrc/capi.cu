@@ -533,7 +533,9 @@ apbf_status substep_body(apbf_ctx *ctx, float dt, cudaStream_t s, bool capture, 
     if (ctx->search_method == APBF_NEIGHBORHOOD_BINARY_SEARCH)
         r = neighborhood_binary_search(ctx, scale, s, fuse_first);
     else
-        r = neighborhood_green(ctx, scale, ctx->scene.min_pos, ctx->scene.max_pos, ctx->scene.log2res, s, fuse_first);
+        r = neighborhood_green(ctx, scale, ctx->scene.min_pos, ctx->scene.max_pos,
+                               ctx->tuning.search_log2res ? ctx->tuning.search_log2res : ctx->scene.log2res, s,
+                               fuse_first);
     if (r != APBF_OK) return r;
     if (spread) {
         r = spread_kernel_width(ctx, s);

@@ -29,47 +29,60 @@ constexpr uint32_t kValMask = (1u << 30) - 1u;
 __device__ __forceinline__ uint32_t ld_volatile(const uint32_t *p) { return *(const volatile uint32_t *)p; }
 __device__ __forceinline__ void st_volatile(uint32_t *p, uint32_t v) { *(volatile uint32_t *)p = v; }
 
-// Counts the 8-bit digits of every pass.  hist: passes x 256.
+// Digit widths of the radix sort (bits per pass); the tuner picks one per context.
+constexpr int kMaxSortPasses = 6;  // 32-bit keys at 6-bit digits
+
+// Counts the BITS-bit digits of every pass.  hist: passes x 2^BITS.
+template <int BITS>
 __global__ void __launch_bounds__(256) k_sort_hist(const uint32_t *__restrict__ keys, const uint32_t *d_count,
                                                    uint32_t max_count, uint32_t key_mask, int passes,
                                                    uint32_t *__restrict__ hist) {
-    __shared__ uint32_t sh[4][256];
-    for (int p = 0; p < 4; ++p) sh[p][threadIdx.x] = 0u;
+    constexpr uint32_t NB = 1u << BITS;
+    constexpr int PM = (32 + BITS - 1) / BITS;
+    __shared__ uint32_t sh[PM][NB];
+    for (uint32_t q = threadIdx.x; q < PM * NB; q += blockDim.x) (&sh[0][0])[q] = 0u;
     __syncthreads();
     uint32_t n = min(*d_count, max_count);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         uint32_t k = keys[i] & key_mask;
-        for (int p = 0; p < passes; ++p) atomicAdd(&sh[p][(k >> (8 * p)) & 255u], 1u);
+        for (int p = 0; p < passes; ++p) atomicAdd(&sh[p][(k >> (BITS * p)) & (NB - 1u)], 1u);
     }
     __syncthreads();
     for (int p = 0; p < passes; ++p)
-        if (sh[p][threadIdx.x]) atomicAdd(&hist[p * 256 + threadIdx.x], sh[p][threadIdx.x]);
+        for (uint32_t b = threadIdx.x; b < NB; b += blockDim.x)
+            if (sh[p][b]) atomicAdd(&hist[p * NB + b], sh[p][b]);
 }
 
-// One 8-bit digit pass.  tile_status: tiles x 256 words (flag << 30 | count).
+// One BITS-bit digit pass.  tile_status: tiles x 2^BITS words (flag << 30 | count).
+// Thread t < 2^BITS owns digit t.
+template <int BITS>
 __global__ void __launch_bounds__(256) k_onesweep(const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin,
                                                   uint32_t *__restrict__ kout, uint32_t *__restrict__ vout,
                                                   const uint32_t *d_count, uint32_t max_count, uint32_t key_mask,
                                                   int shift, const uint32_t *__restrict__ hist,
                                                   uint32_t *tile_counter, uint32_t *tile_status, Status *st) {
+    constexpr uint32_t NB = 1u << BITS;
     __shared__ uint32_t s_tile;
-    __shared__ uint32_t s_cnt[kSortWarps][256];
-    __shared__ uint32_t s_base[256];
-    __shared__ uint32_t s_scan[256];
+    __shared__ uint32_t s_cnt[kSortWarps][NB];
+    __shared__ uint32_t s_base[NB];
+    __shared__ uint32_t s_scan[NB];
 
     const int t = threadIdx.x, w = t >> 5, l = t & 31;
+    const bool owner = (uint32_t)t < NB;
     if (t == 0) s_tile = atomicAdd(tile_counter, 1u);
-    for (int k = 0; k < kSortWarps; ++k) s_cnt[k][t] = 0u;
+    if (owner)
+        for (int k = 0; k < kSortWarps; ++k) s_cnt[k][t] = 0u;
     // exclusive scan of the global digit histogram (same in every tile)
-    s_scan[t] = hist[t];
+    const uint32_t hist_t = owner ? hist[t] : 0u;
+    if (owner) s_scan[t] = hist_t;
     __syncthreads();
-    for (int off = 1; off < 256; off <<= 1) {
-        uint32_t v = t >= off ? s_scan[t - off] : 0u;
+    for (uint32_t off = 1; off < NB; off <<= 1) {
+        uint32_t v = (owner && (uint32_t)t >= off) ? s_scan[t - off] : 0u;
         __syncthreads();
-        s_scan[t] += v;
+        if (owner) s_scan[t] += v;
         __syncthreads();
     }
-    const uint32_t digit_excl = s_scan[t] - hist[t];
+    const uint32_t digit_excl = owner ? s_scan[t] - hist_t : 0u;
 
     const uint32_t n = min(*d_count, max_count);
     const uint32_t ntiles = (n + kSortTile - 1) / kSortTile;
@@ -90,7 +103,7 @@ __global__ void __launch_bounds__(256) k_onesweep(const uint32_t *__restrict__ k
     for (int k = 0; k < kSortItems; ++k) {
         uint32_t idx = base + k * 32 + l;
         bool valid = idx < n;
-        uint32_t d = valid ? ((keys[k] & key_mask) >> shift) & 255u : 256u + (uint32_t)l;
+        uint32_t d = valid ? ((keys[k] & key_mask) >> shift) & (NB - 1u) : NB + (uint32_t)l;
         uint32_t peers = __match_any_sync(0xffffffffu, d);
         uint32_t before = valid ? s_cnt[w][d] : 0u;
         rank[k] = before + __popc(peers & lt);
@@ -101,22 +114,25 @@ __global__ void __launch_bounds__(256) k_onesweep(const uint32_t *__restrict__ k
     __syncthreads();
     // thread t owns digit t: warp exclusive offsets and the tile total
     uint32_t run = 0;
+    if (owner) {
 #pragma unroll
-    for (int k = 0; k < kSortWarps; ++k) {
-        uint32_t c = s_cnt[k][t];
-        s_cnt[k][t] = run;
-        run += c;
+        for (int k = 0; k < kSortWarps; ++k) {
+            uint32_t c = s_cnt[k][t];
+            s_cnt[k][t] = run;
+            run += c;
+        }
     }
-    uint32_t *my = tile_status + (size_t)tile * 256 + t;
+    uint32_t *my = tile_status + (size_t)tile * NB + t;
     uint32_t excl = 0;
-    if (tile == 0) {
+    if (!owner) {
+    } else if (tile == 0) {
         st_volatile(my, kFlagIncl | run);
     } else {
         st_volatile(my, kFlagAgg | run);
         int j = (int)tile - 1;
         uint32_t spins = 0;
         while (j >= 0) {
-            uint32_t v = ld_volatile(tile_status + (size_t)j * 256 + t);
+            uint32_t v = ld_volatile(tile_status + (size_t)j * NB + t);
             uint32_t f = v & ~kValMask;
             if (f == 0u) {
                 if (++spins > kSpinLimit) {
@@ -133,13 +149,13 @@ __global__ void __launch_bounds__(256) k_onesweep(const uint32_t *__restrict__ k
         }
         st_volatile(my, kFlagIncl | ((excl + run) & kValMask));
     }
-    s_base[t] = digit_excl + excl;
+    if (owner) s_base[t] = digit_excl + excl;
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < kSortItems; ++k) {
         uint32_t idx = base + k * 32 + l;
         if (idx < n) {
-            uint32_t d = ((keys[k] & key_mask) >> shift) & 255u;
+            uint32_t d = ((keys[k] & key_mask) >> shift) & (NB - 1u);
             uint32_t pos = s_base[d] + s_cnt[w][d] + rank[k];
             kout[pos] = keys[k];
             vout[pos] = vals[k];
@@ -245,7 +261,11 @@ apbf_status sort_pairs_device(apbf_ctx *ctx, const uint32_t *keys_in, const uint
     if (nib > 8u) nib = 8u;
     uint32_t bits = nib * 4u;
     uint32_t key_mask = bits >= 32u ? 0xffffffffu : ((1u << bits) - 1u);
-    int passes = (int)((bits + 7u) / 8u);
+    const uint32_t dbits = ctx->tuning.sort_digit_bits == 6u || ctx->tuning.sort_digit_bits == 7u
+                               ? ctx->tuning.sort_digit_bits
+                               : 8u;  // digit width: the tuner's choice, 8 by default
+    const uint32_t nb = 1u << dbits;
+    int passes = (int)((bits + dbits - 1u) / dbits);
     uint32_t tiles = (max_count + kSortTile - 1) / kSortTile;
     if (tiles > ctx->sort_tiles) return APBF_ERR_INVALID_ARG;
     if (passes == 0) {
@@ -253,12 +273,18 @@ apbf_status sort_pairs_device(apbf_ctx *ctx, const uint32_t *keys_in, const uint
         APBF_CUDA(cudaMemcpyAsync(vals_out, vals_in, (size_t)max_count * 4, cudaMemcpyDeviceToDevice, s));
         return APBF_OK;
     }
-    APBF_CUDA(cudaMemsetAsync(ctx->sort_hist, 0, 4 * 256 * sizeof(uint32_t), s));
+    // scratch: hist passes x nb <= 4 x 256 words, status passes x tiles x nb <= 4 x tiles x 256
+    APBF_CUDA(cudaMemsetAsync(ctx->sort_hist, 0, (size_t)passes * nb * sizeof(uint32_t), s));
     APBF_CUDA(cudaMemsetAsync(ctx->sort_counters, 0, 8 * sizeof(uint32_t), s));
-    APBF_CUDA(cudaMemsetAsync(ctx->sort_status, 0, (size_t)passes * tiles * 256 * sizeof(uint32_t), s));
+    APBF_CUDA(cudaMemsetAsync(ctx->sort_status, 0, (size_t)passes * tiles * nb * sizeof(uint32_t), s));
     APBF_BEFORE_LAUNCH(ctx, s, "k_sort_hist");
-    k_sort_hist<<<grid_for(ctx, max_count, 256, 4), 256, 0, s>>>(keys_in, d_count, max_count, key_mask, passes,
-                                                                 ctx->sort_hist);
+    const int hgrid = grid_for(ctx, max_count, 256, 4);
+    if (dbits == 6u)
+        k_sort_hist<6><<<hgrid, 256, 0, s>>>(keys_in, d_count, max_count, key_mask, passes, ctx->sort_hist);
+    else if (dbits == 7u)
+        k_sort_hist<7><<<hgrid, 256, 0, s>>>(keys_in, d_count, max_count, key_mask, passes, ctx->sort_hist);
+    else
+        k_sort_hist<8><<<hgrid, 256, 0, s>>>(keys_in, d_count, max_count, key_mask, passes, ctx->sort_hist);
     APBF_AFTER_LAUNCH(ctx, s, "k_sort_hist");
     // Ping-pong between the output (A) and scratch (B) so that the last pass lands
     // in the output: pass p writes A when (passes - 1 - p) is even.  An input that
@@ -275,9 +301,17 @@ apbf_status sort_pairs_device(apbf_ctx *ctx, const uint32_t *keys_in, const uint
         uint32_t *dk = to_out ? keys_out : ctx->keys[1];
         uint32_t *dv = to_out ? vals_out : ctx->vals[1];
         APBF_BEFORE_LAUNCH(ctx, s, "k_onesweep");
-        k_onesweep<<<tiles, 256, 0, s>>>(src_k, src_v, dk, dv, d_count, max_count, key_mask, 8 * p,
-                                         ctx->sort_hist + p * 256, ctx->sort_counters + p,
-                                         ctx->sort_status + (size_t)p * tiles * 256, ctx->status);
+        const int sh = (int)dbits * p;
+        uint32_t *hp = ctx->sort_hist + p * nb, *tp = ctx->sort_status + (size_t)p * tiles * nb;
+        if (dbits == 6u)
+            k_onesweep<6><<<tiles, 256, 0, s>>>(src_k, src_v, dk, dv, d_count, max_count, key_mask, sh, hp,
+                                                ctx->sort_counters + p, tp, ctx->status);
+        else if (dbits == 7u)
+            k_onesweep<7><<<tiles, 256, 0, s>>>(src_k, src_v, dk, dv, d_count, max_count, key_mask, sh, hp,
+                                                ctx->sort_counters + p, tp, ctx->status);
+        else
+            k_onesweep<8><<<tiles, 256, 0, s>>>(src_k, src_v, dk, dv, d_count, max_count, key_mask, sh, hp,
+                                                ctx->sort_counters + p, tp, ctx->status);
         APBF_AFTER_LAUNCH(ctx, s, "k_onesweep");
         src_k = dk;
         src_v = dv;
@@ -409,14 +443,14 @@ extern "C" apbf_status apbf_sort_pairs_noalloc(const uint32_t *d_keys, const uin
     APBF_CUDA(cudaMemsetAsync(&sc->status, 0, sizeof(Status), s));
     uint64_t need = ((uint64_t)max_count + 255) / 256;
     const int hist_grid = (int)std::min<uint64_t>(std::max<uint64_t>(need, 1), (uint64_t)sms * 4);
-    k_sort_hist<<<hist_grid, 256, 0, s>>>(d_keys, d_count, max_count, key_mask, passes, sc->hist);
+    k_sort_hist<8><<<hist_grid, 256, 0, s>>>(d_keys, d_count, max_count, key_mask, passes, sc->hist);
     APBF_CUDA(cudaGetLastError());
     const uint32_t *src_k = d_keys, *src_v = d_values;
     for (int p = 0; p < passes; ++p) {
         const bool to_out = ((passes - 1 - p) & 1) == 0;
         uint32_t *dk = to_out ? d_out_keys : sc->keys;
         uint32_t *dv = to_out ? d_out_values : sc->vals;
-        k_onesweep<<<tiles, 256, 0, s>>>(src_k, src_v, dk, dv, d_count, max_count, key_mask, 8 * p,
+        k_onesweep<8><<<tiles, 256, 0, s>>>(src_k, src_v, dk, dv, d_count, max_count, key_mask, 8 * p,
                                          sc->hist + p * 256, sc->counters + p,
                                          sc->tile_status + (size_t)p * tiles * 256, &sc->status);
         APBF_CUDA(cudaGetLastError());

@@ -378,7 +378,12 @@ def run_arm(spec, args, local, mode: int, net, dist, headline: bool) -> tuple[di
     presteps = args.presteps if args.presteps >= 0 else spec.meta.get("presteps", 0)
     for _ in range(presteps):  # untimed: bring the scene into its violent regime (after impact)
         ctx.substep(spec.dt)
-    tuning = ctx.autotune() if not args.no_autotune else ctx.tuning()  # untimed, state restored
+    if not args.no_autotune:  # untimed, state restored
+        search_tuning = ctx.autotune_search() if spec.meta.get("glue") is None else None
+        tuning = ctx.autotune()
+        tuning["search"] = search_tuning
+    else:
+        tuning = ctx.tuning()
     for _ in range(args.warmup):
         ctx.substep(spec.dt)
     ctx.check_status()
@@ -446,6 +451,29 @@ def run_arm(spec, args, local, mode: int, net, dist, headline: bool) -> tuple[di
     return r, ctx
 
 
+def oracle_check(ctx, spec) -> dict:
+    """The reported density error against the FP64 oracle: on the final state, the
+    device's neighbour search and one density pass (its mean compression error, FP32
+    sums) next to the oracle's FP64 neighbour search and density error of the same
+    downloaded state."""
+    from apbf_gb300.api import incompressibility, neighborhood_green
+    from oracle import oracle as orc
+
+    scale = 1.0 if spec.basic_pbf else 1.5
+    st, _ = ctx.download()
+    t0 = time.perf_counter()
+    neighborhood_green().set_data(ctx).set_range_scale(scale).set_position_range(
+        spec.grid_min, spec.grid_max, spec.log2res).apply()
+    incompressibility().set_data(ctx).apply()
+    e_dev = float(ctx.reduce_fp64()[2])
+    fs = orc.FluidState(st)
+    orc.neighborhood_green(fs, scale, spec.grid_min, spec.grid_max, spec.log2res, int(st["position"].shape[0] * 160))
+    e_or = float(orc.density_error(fs, orc.settings_from(ctx.settings))[0])
+    return {"particles": int(st["position"].shape[0]), "device_fp32": e_dev, "oracle_fp64": e_or,
+            "abs_diff": abs(e_dev - e_or), "seconds": round(time.perf_counter() - t0, 2),
+            "what": "mean compression error of one density pass on the final state"}
+
+
 def run_ours(args) -> None:
     import torch
 
@@ -508,6 +536,7 @@ def run_ours(args) -> None:
 
     # e2e: the same substep driven from pinned host buffers through the C ABI
     e2e = run_e2e(ctx, spec, args, local)
+    check = oracle_check(ctx, spec) if rank == 0 and not args.no_oracle_check else None
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -537,6 +566,7 @@ def run_ours(args) -> None:
             "roofline": roof, "kernel_share": kernel_share, "kernel_us": kernel_us,
             "gpu_launches": head["gpu_launches"],
             "profiler_dropped": int(dropped), "clocks": clk, "e2e": e2e, "cpu_baseline": cpu,
+            "oracle_check": check,
         }
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -809,6 +839,7 @@ def main() -> None:
     ap.add_argument("--presteps", type=int, default=-1, help="untimed substeps before warm-up (-1: scene default)")
     ap.add_argument("--max-neighbors", type=int, default=192)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-oracle-check", action="store_true", help="skip the FP64 oracle check of the final state")
     ap.add_argument("--no-warm-start", action="store_true", help="headline = the reference Jacobi rule")
     ap.add_argument("--no-plain", action="store_true", help="skip the two plain-solver comparison runs")
     ap.add_argument("--ws-epochs", type=int, default=3)

@@ -189,7 +189,11 @@ typedef struct apbf_tuning {
                                      candidates in shared memory, 2 one warp per particle (same rows) */
     uint32_t filter_in_density;   /* 1: the boundariness filter always runs in the density pass (else, with
                                      symmetric rows and the Gauss kernel, in the position pass) */
-    uint32_t reserved[3];
+    uint32_t sort_digit_bits;     /* radix sort digit width: 6, 7 or 8 bits per pass (0: 8); same order */
+    uint32_t search_log2res;      /* apbf_substep's search grid: 2^L cells per axis over the scene's box
+                                     (0: the scene's log2res); the same neighbour sets, particle order
+                                     and row order follow the grid */
+    uint32_t reserved;
 } apbf_tuning;
 
 typedef struct apbf_ctx apbf_ctx;
@@ -365,6 +369,16 @@ apbf_status apbf_batch_set_persistent_solve(apbf_batch *batch, int enable);
 apbf_status apbf_set_tuning(apbf_ctx *ctx, const apbf_tuning *t);
 apbf_status apbf_get_tuning(apbf_ctx *ctx, apbf_tuning *t);
 apbf_status apbf_autotune(apbf_ctx *ctx, void *stream, apbf_tuning *chosen, float *pass_ms);
+/* The neighbour search's tuning (no counterpart in the reference): times the radix
+ * sort of apbf_substep's search for 6-, 7- and 8-bit digits, then the whole search
+ * on grids of 2^(L-1), 2^L and 2^(L+1) cells per axis (L the current search grid;
+ * only levels up to max_log2res), keeps the fastest digit width and grid in the
+ * tuning (sort_digit_bits, search_log2res) and restores the particle state, the
+ * transfer list and the status it ran on.  ms (may be NULL) receives six times:
+ * the sort per digit width, the search per grid level (0 where not timed).  The
+ * choice leaves the neighbour sets unchanged; the particle order follows the grid.
+ * Not with a glue list. */
+apbf_status apbf_autotune_search(apbf_ctx *ctx, void *stream, apbf_tuning *chosen, float *ms);
 /* Per-particle intermediates of the last incompressibility iteration (debug):
  * density and squared-gradient sums (2^18 fixed point), weighted gradient sums
  * (int4), lambda.  Any pointer may be NULL. */

@@ -99,3 +99,24 @@ def test_prefix_sum_large(ctx, orc, n, bits):  # test.cpp:199-267
     algorithms.prefix_sum(ctx, t, torch.tensor([n], dtype=torch.int32, device="cuda"), n)
     ctx.check_status()
     assert np.array_equal(t.cpu().numpy().view(np.uint32), orc.prefix_sum(v))
+
+
+@pytest.mark.parametrize("bits", [6, 7, 8])
+def test_sort_digit_widths_give_the_same_order(ctx, orc, bits):
+    """The tuned digit width (6, 7 or 8 bits per pass) changes the passes, not the
+    stable order."""
+    rng = np.random.default_rng(bits)
+    n = 300_001
+    keys = rng.integers(0, 1 << 32, size=n, dtype=np.uint64).astype(np.uint32)
+    keys[: n // 2] &= 0xFFF  # many equal keys: stability matters
+    vals = np.arange(n, dtype=np.uint32)
+    ctx.set_tuning(sort_digit_bits=bits)
+    try:
+        k, i = _sort(ctx, keys, vals)
+        k21, i21 = _sort(ctx, keys & ((1 << 21) - 1), vals, ub=1 << 21)
+    finally:
+        ctx.set_tuning(sort_digit_bits=0)
+    ok, oi = orc.sort_pairs(keys, vals)
+    assert np.array_equal(k, ok) and np.array_equal(i, oi)
+    ok21, oi21 = orc.sort_pairs(keys & ((1 << 21) - 1), vals)
+    assert np.array_equal(k21, ok21) and np.array_equal(i21, oi21)

@@ -31,7 +31,7 @@ def test_gather_lanes_bit_identical(name):
         ctx = _ctx(spec, 5, maxn=maxn)
         ctx.set_tuning(gather_lanes=lanes, pass_block=block, pass_blocks_per_sm=per_sm)
         assert ctx.tuning() == {"gather_lanes": lanes, "pass_block": block, "pass_blocks_per_sm": per_sm,
-                                "build_tiled": 0, "filter_in_density": 0}
+                                "build_tiled": 0, "filter_in_density": 0, "sort_digit_bits": 0, "search_log2res": 0}
         for _ in range(8):
             ctx.substep(spec.dt)
         ctx.check_status()
@@ -52,8 +52,7 @@ def test_autotune_keeps_state():
     res = ctx.autotune()
     assert res["gather_lanes"] in (1, 2, 4, 8) and res["pass_block"] in (128, 256)
     assert len(res["pass_ms"]) == 24 and all(v > 0 for v in res["pass_ms"].values())
-    assert ctx.tuning() == {k: res[k] for k in ("gather_lanes", "pass_block", "pass_blocks_per_sm", "build_tiled",
-                                                "filter_in_density")}
+    assert ctx.tuning() == {k: v for k, v in res.items() if k != "pass_ms"}
     after, _ = ctx.download()
     for k in before:
         assert np.array_equal(before[k], after[k]), k
@@ -148,3 +147,36 @@ def test_deferred_filter_identical(lanes):
     assert np.any(a["boundariness"] == 0) and np.any(a["boundariness"] > 0)
     for k in a:
         assert np.array_equal(a[k], b[k]), k
+
+
+def test_search_tuning_restores_the_state_and_keeps_results():
+    """apbf_autotune_search times sort digit widths and search grids, leaves the state
+    it ran on unchanged, and its choice gives the same neighbour sets."""
+    from apbf_gb300.api import Context
+
+    spec = scenes.water_drop(total=30_000, seed=5, basic_pbf=True)
+
+    def make():
+        c = Context(particle_capacity=spec.n + 512, max_neighbors=160, max_log2res=spec.log2res + 1)
+        c.set_settings(basic_pbf=1, solver_iterations=12, density_error_target=1e-3)
+        c.set_scene(spec.grid_min, spec.grid_max, spec.log2res, spec.acceleration)
+        c.set_boxes(spec.box_min, spec.box_max)
+        c.upload(spec.state)
+        for _ in range(3):
+            c.substep(spec.dt)
+        return c
+
+    ctx, ref = make(), make()
+    before, _ = ctx.download()
+    choice = ctx.autotune_search()
+    assert choice["sort_digit_bits"] in (6, 7, 8)
+    assert all(v > 0 for v in choice["sort_ms"].values())
+    after, _ = ctx.download()
+    for k in before:
+        assert np.array_equal(before[k], after[k]), k
+    # the next substep's search (on the same positions in both) finds the same pairs
+    ctx.substep(spec.dt)
+    ref.substep(spec.dt)
+    assert ctx.check_status().pairs == ref.check_status().pairs, choice
+    ctx.close()
+    ref.close()
