@@ -12,12 +12,16 @@ lambda that the first position update uses:
               previous substep (carried through the sort and split/merge),
               f6 the mean of f5 over the particle's neighbours
     target    sum of min(0, lambda) over the first K plain passes of the substep
-    network   7 -> 64 -> 64 -> 1 ReLU, BF16 weights, FP32 accumulation (mma.sync)
+    network   7 -> 64 -> 64 -> 1 ReLU, BF16 weights, FP32 accumulation (inference
+              on tcgen05.mma in the substep, training on mma.sync)
 
 Only the first update changes; the following passes are the plain solve, which
 keeps measuring the mean compression error and stops at density_error_target.
 The network therefore decides how many passes a substep needs, never the error
-the substep ends with.
+the substep ends with.  Two guards bound what the solver takes from it (an
+over-relaxation bound and a neighbour minimum); select_warm_start picks the
+network and the bound by the pass count on validation scenes, among those that
+leave the fluid no more energetic than the plain solve.
 
 Everything runs on the GPU through the C ABI: the substep appends samples to
 device buffers (apbf_record_samples), training calls the project's forward /
@@ -29,6 +33,7 @@ from __future__ import annotations
 import ctypes as C
 from dataclasses import dataclass
 from pathlib import Path
+from typing import Callable
 
 import numpy as np
 import torch
@@ -236,3 +241,102 @@ def density_passes(ctx, dt: float, substeps: int) -> float:
     for _ in range(substeps):
         ctx.substep(dt)
     return ctx.check_status().density_passes / max(substeps, 1)
+
+
+@dataclass
+class ValidationCase:
+    """A validation scene for select_warm_start: `make(mode, params)` returns a new
+    context at the scene's start with warm-start `mode` (params: a network's
+    parameter vector, or None); `before` substeps run uncounted, then `counted`
+    substeps are measured."""
+
+    make: Callable
+    dt: float
+    before: int
+    counted: int
+
+
+def run_case(case: ValidationCase, mode: int, params: torch.Tensor | None = None) -> dict:
+    """Runs a validation scene from its start: density passes per counted substep,
+    substeps that reached the error target, and at the end the mean squared particle
+    speed (twice the kinetic energy per unit mass) and the 99th percentile of the
+    particle heights (y, length units: the splash)."""
+    ctx = case.make(mode, params)
+    for _ in range(case.before):
+        ctx.substep(case.dt)
+    ctx.check_status()
+    for _ in range(case.counted):
+        ctx.substep(case.dt)
+    info = ctx.check_status()
+    n, _ = ctx.lengths()
+    view = ctx.fluid_view()
+    v = view["velocity"][:n, :3].double()
+    e = float((v * v).sum(1).mean().item()) if n else 0.0
+    y = view["position"][:n, 1].double() / 262144.0
+    h = float(torch.sort(y).values[min(n - 1, int(0.99 * n))].item()) if n else 0.0
+    ctx.close()
+    return {"passes": info.density_passes / max(case.counted, 1), "converged": int(info.converged_substeps),
+            "mean_v2": e, "y_p99": h, "particles": int(n)}
+
+
+# over-relaxation bounds that select_warm_start compares for every network
+OMEGA_CANDIDATES = (1.5, 2.0, 3.0, 4.0, 6.0)
+
+
+def select_warm_start(nets: dict, cases: list, omegas=OMEGA_CANDIDATES, min_neighbors: float = 16.0,
+                      energy_slack: float = 1.05, height_slack: float = 1.25) -> tuple[dict | None, dict]:
+    """Chooses a trained network and its over-relaxation bound by validation.
+
+    A learned first update that pushes too hard still meets the density-error
+    target (the following passes only correct compression) but leaves the fluid
+    with extra kinetic energy: particles move apart faster than the plain solve
+    would move them, and thrown-off particles have no neighbours and no error.
+    So every candidate (each network of `nets` x each bound of `omegas`) runs each
+    validation scene from its start, and is admissible only if all its counted
+    substeps reach the target, its final mean squared speed is at most
+    `energy_slack` times, and its final 99th-percentile particle height at most
+    `height_slack` times, the largest of the plain rules that reached the target in
+    every counted substep (the reference Jacobi rule and the projected rule, run
+    on the same scenes; with neither, the larger of the two).  Of the admissible
+    candidates the one with the fewest density passes per substep, weighted by the
+    scenes' particle counts, wins (ties: the smaller bound).  A slack <= 0 drops
+    its condition.
+
+    Returns ({"net": key, "omega_max", "min_neighbors", "params": tensor} or None
+    when no candidate is admissible, and a table of every run)."""
+    plain = []
+    for c in cases:
+        plain.append({"reference_rule": run_case(c, 0), "projected_rule": run_case(c, N.WARM_PROJECTED)})
+    def bound(key, slack):
+        out = []
+        for c, p in zip(cases, plain):
+            conv = [r[key] for r in p.values() if r["converged"] == c.counted]
+            ref = max(conv) if conv else max(r[key] for r in p.values())
+            out.append(slack * ref if slack > 0 else float("inf"))
+        return out
+
+    bounds, hbounds = bound("mean_v2", energy_slack), bound("y_p99", height_slack)
+    weights = [max(p["reference_rule"]["particles"], 1) for p in plain]
+    table: dict = {"plain": plain, "energy_bound": bounds, "height_bound": hbounds, "candidates": {}}
+    best = None
+    for key, net in nets.items():
+        for om in omegas:
+            net.omega_max, net.min_neighbors = om, min_neighbors
+            params = net.params.clone()
+            runs = [run_case(c, N.WARM_LEARNED | N.WARM_PROJECTED, params) for c in cases]
+            ok = all(r["converged"] == c.counted and r["mean_v2"] <= b and r["y_p99"] <= hb
+                     for r, c, b, hb in zip(runs, cases, bounds, hbounds))
+            score = sum(w * r["passes"] for w, r in zip(weights, runs)) / sum(weights)
+            table["candidates"][f"{key} / omega {om:g}"] = {
+                "passes": round(score, 3), "admissible": ok,
+                "energy_ratio": [round(r["mean_v2"] / max(p["reference_rule"]["mean_v2"], 1e-30), 3)
+                                 for r, p in zip(runs, plain)],
+                "height_ratio": [round(r["y_p99"] / max(p["reference_rule"]["y_p99"], 1e-30), 3)
+                                 for r, p in zip(runs, plain)]}
+            if ok and (best is None or (score, om) < (best[0], best[2])):
+                best = (score, key, om, params)
+    if best is None:
+        return None, table
+    _, key, om, params = best
+    nets[key].omega_max, nets[key].min_neighbors = om, min_neighbors
+    return {"net": key, "omega_max": om, "min_neighbors": min_neighbors, "params": params}, table

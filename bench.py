@@ -303,7 +303,9 @@ def _make_ctx(spec, args, local, mode: int = 0, net=None):
 
     cap = max(int(spec.n * 1.25) + 1024, int(spec.meta.get("capacity", 0) * 1.15))
     maxn = args.max_neighbors if spec.basic_pbf else max(args.max_neighbors, 256)
-    ctx = Context(particle_capacity=cap, max_neighbors=maxn, max_log2res=max(spec.log2res, 3), device=local)
+    # the search tuner may try grids up to search_levels finer than the scene's
+    levels = min(9, max(spec.log2res, 3) + max(0, getattr(args, "search_levels", 0)))
+    ctx = Context(particle_capacity=cap, max_neighbors=maxn, max_log2res=levels, device=local)
     # iterate every substep until the mean density error is at most the target
     ctx.set_settings(basic_pbf=1 if spec.basic_pbf else 0, solver_iterations=args.max_iterations,
                      density_error_target=args.error_target)
@@ -312,25 +314,68 @@ def _make_ctx(spec, args, local, mode: int = 0, net=None):
     if getattr(args, "persistent", False):
         ctx.set_persistent_solve(True)
     if net is not None:
-        ctx.mlp_load(net.params)
+        ctx.mlp_load(net.params if hasattr(net, "params") else net)
     if mode:
         ctx.set_warm_start(mode)
     return ctx
 
 
+VALIDATION_SUBSTEPS = 40  # counted substeps of each validation scene per warm-start candidate
+
+
+def _ws_choices(args) -> tuple[tuple, tuple]:
+    """Loss weights of the networks to train and over-relaxation bounds to compare
+    (one of each when given on the command line)."""
+    from apbf_gb300.warmstart import OMEGA_CANDIDATES
+
+    ows = (args.ws_over_weight,) if args.ws_over_weight is not None else (4.0, 8.0, 16.0)
+    oms = (args.ws_omega,) if args.ws_omega is not None else OMEGA_CANDIDATES
+    return ows, oms
+
+
+def _fit_nets(X, T, args, local: int, over_weights) -> dict:
+    from apbf_gb300.warmstart import WarmStartNet
+
+    nets = {}
+    for ow in over_weights:
+        net = WarmStartNet(device=local, seed=0)
+        net.set_normalization(X, T)
+        hist = net.fit(X, T, epochs=args.ws_epochs, batch=32768, lr=2e-3, lr_final=2e-4, over_weight=ow)
+        nets[f"over_weight {ow:g}"] = (net, hist)
+    return nets
+
+
+def _selection_info(choice, table, seeds, args) -> dict:
+    return {
+        "chosen": ({k: v for k, v in choice.items() if k != "params"} if choice else
+                   "none within the kinetic-energy bound: the reference Jacobi rule runs"),
+        "selection": (None if table is None else
+                      {"validation_seeds": seeds, "counted_substeps": VALIDATION_SUBSTEPS,
+                       "energy_slack": args.ws_energy_slack, "height_slack": args.ws_height_slack,
+                       "rule": "fewest passes among candidates that converge in every counted substep and end "
+                               "with mean |v|^2 and the 99th-percentile height within the slacks x the largest "
+                               "of the converging plain rules",
+                       "plain": table["plain"], "candidates": table["candidates"]})}
+
+
 def train_warm_start(args, local: int, rank: int) -> tuple[object, dict]:
     """Untimed: samples from projected-rule rollouts of two scenes with seeds that the
-    timed scene does not use, then minibatch Adam with the project's kernels."""
+    timed scene does not use; minibatch Adam with the project's kernels, one network
+    per overshoot weight of the loss; then the network and over-relaxation bound
+    chosen on one or two further seeds (fewest passes within the plain solve's kinetic
+    energy).  Returns (None, info) when no candidate passes: the headline then runs
+    the reference Jacobi rule."""
     import torch
 
     from apbf_gb300 import _native as N
-    from apbf_gb300.warmstart import SampleBuffer, WarmStartNet, record_rollout
+    from apbf_gb300.warmstart import SampleBuffer, ValidationCase, record_rollout, select_warm_start
 
     t0 = time.perf_counter()
     seeds = [1000 + 10 * rank + k for k in (1, 2)]
     specs = [make_spec(args.workload, seed=s) for s in seeds]
     per = [sp.meta.get("presteps", 0) + 60 for sp in specs]
-    every = 3 if max(sp.n for sp in specs) < 500_000 else 12  # bounds the sample count of growing scenes
+    large = max(sp.n for sp in specs) >= 500_000
+    every = 12 if large else 3  # bounds the sample count of growing scenes
     grown = [max(sp.n, int(sp.meta.get("capacity", 0))) for sp in specs]
     cap = min(sum(int(g * 1.3) * ((p + every - 1) // every + 1) for g, p in zip(grown, per)), 120_000_000)
     buf = SampleBuffer.allocate(cap, device=local)
@@ -342,21 +387,39 @@ def train_warm_start(args, local: int, rank: int) -> tuple[object, dict]:
     torch.cuda.synchronize()
     t1 = time.perf_counter()
     X, T = buf.view()
-    net = WarmStartNet(device=local, seed=0)
-    net.set_normalization(X, T)
-    hist = net.fit(X, T, epochs=args.ws_epochs, batch=32768, lr=2e-3, lr_final=2e-4)
+    n_samples = int(X.shape[0])
+    ows, oms = _ws_choices(args)
+    trained = _fit_nets(X, T, args, local, ows)
     torch.cuda.synchronize()
     t2 = time.perf_counter()
-    net.min_neighbors = args.ws_min_neighbors
-    net.omega_max = args.ws_omega
-    info = {"samples": int(X.shape[0]), "rollout_seeds": seeds, "substeps_per_rollout": per,
-            "target": "sum of the lambdas applied over all passes of a projected-rule substep",
-            "epochs": args.ws_epochs, "loss_per_epoch": [round(h, 5) for h in hist],
-            "collect_s": round(t1 - t0, 3), "train_s": round(t2 - t1, 3),
-            "guards": {"min_neighbors": args.ws_min_neighbors, "omega_max": args.ws_omega}}
     del buf, X, T
     torch.cuda.empty_cache()
-    return net, info
+
+    nets = {k: v[0] for k, v in trained.items()}
+    nmin = args.ws_min_neighbors if args.ws_min_neighbors is not None else 16.0
+    vseeds = [1000 + 10 * rank + k for k in ((3,) if large else (3, 4))]
+    table = None
+    if len(nets) * len(oms) > 1:
+        cases = []
+        for vs in vseeds:
+            vspec = make_spec(args.workload, seed=vs)
+            before = (args.presteps if args.presteps >= 0 else vspec.meta.get("presteps", 0)) + args.warmup
+            cases.append(ValidationCase(
+                make=lambda mode, params, vspec=vspec: _make_ctx(vspec, args, local, mode, params),
+                dt=vspec.dt, before=before, counted=VALIDATION_SUBSTEPS))
+        choice, table = select_warm_start(nets, cases, oms, nmin, args.ws_energy_slack, args.ws_height_slack)
+    else:
+        key = next(iter(nets))
+        nets[key].omega_max, nets[key].min_neighbors = oms[0], nmin
+        choice = {"net": key, "omega_max": oms[0], "min_neighbors": nmin}
+    t3 = time.perf_counter()
+    info = {"samples": n_samples, "rollout_seeds": seeds, "substeps_per_rollout": per,
+            "target": "sum of the lambdas applied over all passes of a projected-rule substep",
+            "epochs": args.ws_epochs,
+            "loss_per_epoch": {k: [round(h, 5) for h in v[1]] for k, v in trained.items()},
+            "collect_s": round(t1 - t0, 3), "train_s": round(t2 - t1, 3), "select_s": round(t3 - t2, 3),
+            **_selection_info(choice, table, vseeds, args)}
+    return (nets[choice["net"]] if choice else None), info
 
 
 def _state_summary(ctx) -> dict:
@@ -490,13 +553,14 @@ def run_ours(args) -> None:
 
     spec = make_spec(args.workload, seed=rank)
     n = spec.n
-    learned = not args.no_warm_start
-    net, train_info = train_warm_start(args, local, rank) if learned else (None, None)
+    wants_learned = not args.no_warm_start
+    net, train_info = train_warm_start(args, local, rank) if wants_learned else (None, None)
+    learned = net is not None  # no admissible warm start: the reference rule is the headline
     head_mode = (N.WARM_LEARNED | N.WARM_PROJECTED) if learned else 0
 
     # the plain forms first (same scene, same seed), then the headline form
     plain = {}
-    if learned and not args.no_plain:
+    if wants_learned and not args.no_plain:
         for name, mode in (("reference_rule", 0), ("projected_rule", N.WARM_PROJECTED)):
             r, c = run_arm(spec, args, local, mode, None, dist, headline=False)
             c.close()
@@ -544,7 +608,17 @@ def run_ours(args) -> None:
 
     if rank == 0:
         solver = ("learned warm start (BF16 MLP first update) + projected Jacobi passes" if learned
-                  else "reference Jacobi rule")
+                  else "reference Jacobi rule" + (" (no warm start within the kinetic-energy bound)"
+                                                  if wants_learned else ""))
+        fidelity = None
+        if plain and head.get("state_after"):
+            e = head["state_after"]["mean_v2"]
+            hy = head["state_after"]["y_p99"]
+            fidelity = {}
+            for k, v in plain.items():
+                if v.get("state_after"):
+                    fidelity[f"mean_v2_vs_{k}"] = round(e / max(v["state_after"]["mean_v2"], 1e-30), 3)
+                    fidelity[f"y_p99_vs_{k}"] = round(hy / max(v["state_after"]["y_p99"], 1e-30), 3)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -560,7 +634,7 @@ def run_ours(args) -> None:
                        "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas x{world}",
                        "graph_mode": args.graph_mode, "persistent_solve": bool(args.persistent),
                        "tuning": head["tuning"]},
-            "state_after": head["state_after"],
+            "state_after": head["state_after"], "fidelity": fidelity,
             "plain": plain or None,
             "warm_start_training": train_info,
             "roofline": roof, "kernel_share": kernel_share, "kernel_us": kernel_us,
@@ -599,7 +673,7 @@ def run_batch(args) -> None:
 
     from apbf_gb300 import _native as N
     from apbf_gb300.api import Batch, Context
-    from apbf_gb300.warmstart import SampleBuffer, WarmStartNet, record_rollout
+    from apbf_gb300.warmstart import SampleBuffer, ValidationCase, record_rollout, select_warm_start
 
     local = int(os.environ.get("LOCAL_RANK", "0"))
     rank = int(os.environ.get("RANK", "0"))
@@ -610,7 +684,7 @@ def run_batch(args) -> None:
     dt = 1.0 / 240.0  # one time step for the whole batch
 
     def make(spec, mode=0, net=None):
-        maxn = 128 if spec.basic_pbf and spec.name == "dam_break" else (192 if spec.basic_pbf else 256)
+        maxn = 160 if spec.basic_pbf and spec.name == "dam_break" else (192 if spec.basic_pbf else 256)
         ctx = Context(particle_capacity=int(spec.n * 1.3) + 1024, max_neighbors=maxn,
                       max_log2res=max(spec.log2res, 3), device=local)
         ctx.set_settings(basic_pbf=1 if spec.basic_pbf else 0, solver_iterations=args.max_iterations,
@@ -620,7 +694,7 @@ def run_batch(args) -> None:
         ctx.upload(spec.state)
         ctx.set_solve_graph(2)
         if net is not None:
-            ctx.mlp_load(net.params)
+            ctx.mlp_load(net if isinstance(net, torch.Tensor) else net.params)
         if mode:
             ctx.set_warm_start(mode)
         return ctx
@@ -639,18 +713,39 @@ def run_batch(args) -> None:
         c.check_status()
         c.close()
     X, T = buf.view()
-    net = WarmStartNet(device=local, seed=0)
-    net.set_normalization(X, T)
-    net.fit(X, T, epochs=args.ws_epochs, batch=32768)
-    net.min_neighbors = args.ws_min_neighbors
-    net.omega_max = args.ws_omega
     n_samples = int(X.shape[0])
+    ows, oms = _ws_choices(args)
+    nets = {k: v[0] for k, v in _fit_nets(X, T, args, local, ows).items()}
     del buf, X, T
     torch.cuda.empty_cache()
+    nmin = args.ws_min_neighbors if args.ws_min_neighbors is not None else 16.0
+
+    # one set of networks for the mixture; the network and bound per scene kind (each
+    # context loads its own parameter vector), chosen on a held-out scene of the kind
+    def kind(sp):
+        return f"{sp.name}{'' if sp.basic_pbf else ' adaptive'}"
+
+    val = [(911, S.dam_break(n_side=24, seed=911)), (912, S.water_drop(total=40_000, seed=912, basic_pbf=True)),
+           (913, S.water_drop(total=40_000, seed=913, basic_pbf=False))]
+    kind_params, selections = {}, {}
+    for vseed, sp in val:
+        if len(nets) * len(oms) > 1:
+            case = ValidationCase(make=lambda mode, params, sp=sp: make(sp, mode, params), dt=dt,
+                                  before=args.presteps if args.presteps >= 0 else 40, counted=VALIDATION_SUBSTEPS)
+            choice, table = select_warm_start(nets, [case], oms, nmin, args.ws_energy_slack,
+                                              args.ws_height_slack)
+        else:
+            key = next(iter(nets))
+            nets[key].omega_max, nets[key].min_neighbors = oms[0], nmin
+            choice, table = {"net": key, "omega_max": oms[0], "min_neighbors": nmin,
+                             "params": nets[key].params.clone()}, None
+        kind_params[kind(sp)] = choice["params"] if choice else None
+        selections[kind(sp)] = _selection_info(choice, table, [vseed], args)
     train_s = time.perf_counter() - t0
 
-    mode = N.WARM_LEARNED | N.WARM_PROJECTED
-    ctxs = [make(sp, mode, net) for sp in specs]
+    learned_mode = N.WARM_LEARNED | N.WARM_PROJECTED
+    ctxs = [make(sp, learned_mode if kind_params[kind(sp)] is not None else 0, kind_params[kind(sp)])
+            for sp in specs]
     batch = Batch(ctxs)
     batch.set_persistent_solve(args.batch_persistent)
     for _ in range(args.presteps if args.presteps >= 0 else 40):
@@ -733,7 +828,9 @@ def run_batch(args) -> None:
             "config": {"workload": args.workload, "scenes": len(specs), "particles_total": int(n_total),
                        "particles_min": int(min(sp.n for sp in specs)), "particles_max": int(max(sp.n for sp in specs)),
                        "adaptive_scenes": int(sum(not sp.basic_pbf for sp in specs)), "dt": dt,
-                       "solver": "learned warm start + projected Jacobi passes, per-scene convergence",
+                       "solver": ("learned warm start + projected Jacobi passes, per-scene convergence; "
+                                  "kinds without an admissible warm start: reference Jacobi rule: " +
+                                  (", ".join(k for k, v in kind_params.items() if v is None) or "none")),
                        "iterations": f"until mean density error <= {args.error_target} (max {args.max_iterations})",
                        "density_passes_per_scene_substep": passes,
                        "converged_scene_substeps": f"{conv}/{len(ctxs) * args.steps}",
@@ -746,7 +843,8 @@ def run_batch(args) -> None:
                            "note": "the same scenes, one whole-substep graph launch each, one after the other"},
             "scene_density_error_last_pass": {"min": min(errs), "max": max(errs), "mean": float(np.mean(errs))},
             "oracle_density_error_check": check,
-            "warm_start_training": {"samples": n_samples, "seconds": round(train_s, 2)},
+            "warm_start_training": {"samples": n_samples, "seconds": round(train_s, 2),
+                                    "per_scene_kind": selections},
             "roofline": None, "gpu_launches": int(launches), "clocks": clk, "e2e": e2e,
             "cpu_baseline": None,
         }
@@ -844,6 +942,8 @@ def main() -> None:
     ap.add_argument("--no-plain", action="store_true", help="skip the two plain-solver comparison runs")
     ap.add_argument("--ws-epochs", type=int, default=3)
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--search-levels", type=int, default=1,
+                    help="finer search grids than the scene's that the search tuner may try")
     ap.add_argument("--graph-mode", type=int, default=2, choices=(0, 1, 2),
                     help="0 per-kernel launches, 1 solve loop as a graph, 2 whole substep as a graph")
     ap.add_argument("--prof-steps", type=int, default=8, help="traced substeps after the timed ones (kernel shares)")
@@ -851,8 +951,18 @@ def main() -> None:
                     help="batch64: every scene's Jacobi passes 1.. in one persistent cooperative launch")
     ap.add_argument("--persistent", action="store_true",
                     help="Jacobi passes 1.. as one persistent cooperative kernel (apbf_set_persistent_solve)")
-    ap.add_argument("--ws-min-neighbors", type=float, default=16.0)
-    ap.add_argument("--ws-omega", type=float, default=2.0)
+    ap.add_argument("--ws-min-neighbors", type=float, default=None,
+                    help="warm-start guard: particles with fewer neighbours keep the plain lambda (default 16)")
+    ap.add_argument("--ws-omega", type=float, default=None,
+                    help="warm-start over-relaxation bound (default: chosen by validation on held-out seeds)")
+    ap.add_argument("--ws-over-weight", type=float, default=None,
+                    help="overshoot weight of the training loss (default: networks for 4, 8, 16, chosen by validation)")
+    ap.add_argument("--ws-energy-slack", type=float, default=1.05,
+                    help="validation admits a warm start whose final mean |v|^2 is at most this times the plain "
+                         "rule's (<= 0: no energy condition)")
+    ap.add_argument("--ws-height-slack", type=float, default=1.25,
+                    help="validation admits a warm start whose final 99th-percentile particle height is at most "
+                         "this times the plain rule's (<= 0: no height condition)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -400,26 +400,29 @@ def test_warm_start_needs_parameters():
 
 
 # ----------------------------------------------------------------- what it gains
+def _drop(seed):
+    from apbf_gb300.api import Context
+
+    spec = scenes.water_drop(total=60_000, seed=seed, basic_pbf=True)
+    ctx = Context(int(spec.n * 1.25) + 1024, max_neighbors=192, max_log2res=max(spec.log2res, 3))
+    ctx.set_settings(basic_pbf=1, solver_iterations=100, density_error_target=1e-3)
+    ctx.set_scene(spec.grid_min, spec.grid_max, spec.log2res, spec.acceleration)
+    ctx.set_boxes(spec.box_min, spec.box_max)
+    ctx.upload(spec.state)
+    return spec, ctx
+
+
 def test_trained_network_saves_passes_on_held_out_seed():
     """Train on projected-rule rollouts of two water drops (seeds 1, 2), then run a
     third (seed 0, never seen) after impact: at the same 0.1 % target every
     substep converges in each form, and the learned first update needs fewer
-    density passes than the same solve without it and than the reference rule."""
-    import torch
-
+    density passes than the same solve without it and than the reference rule.
+    The validation that picks the network and its over-relaxation bound on a
+    fourth seed (3) is reproducible and keeps to its kinetic-energy rule."""
     from apbf_gb300 import _native as N
-    from apbf_gb300.api import Context
-    from apbf_gb300.warmstart import SampleBuffer, WarmStartNet, density_passes, record_rollout
+    from apbf_gb300.warmstart import SampleBuffer, ValidationCase, WarmStartNet, record_rollout, select_warm_start
 
-    def make(seed):
-        spec = scenes.water_drop(total=60_000, seed=seed, basic_pbf=True)
-        ctx = Context(int(spec.n * 1.25) + 1024, max_neighbors=192, max_log2res=max(spec.log2res, 3))
-        ctx.set_settings(basic_pbf=1, solver_iterations=100, density_error_target=1e-3)
-        ctx.set_scene(spec.grid_min, spec.grid_max, spec.log2res, spec.acceleration)
-        ctx.set_boxes(spec.box_min, spec.box_max)
-        ctx.upload(spec.state)
-        return spec, ctx
-
+    make = _drop
     buf = SampleBuffer.allocate(12_000_000)
     for seed in (1, 2):
         spec, ctx = make(seed)
@@ -456,3 +459,39 @@ def test_trained_network_saves_passes_on_held_out_seed():
     assert learned[1] == projected[1] == reference[1] == 30, (learned, projected, reference)
     assert learned[0] < 0.8 * projected[0], (learned, projected)
     assert learned[0] < reference[0], (learned, reference)
+
+    # network and bound by validation on seed 3: every run starts from the scene's
+    # start, so the table repeats exactly; the winner is admissible and has the
+    # fewest passes among the admissible; with no energy allowance nothing is
+    def vmake(mode, params):
+        spec, ctx = make(3)
+        if params is not None:
+            ctx.mlp_load(params)
+        if mode:
+            ctx.set_warm_start(mode)
+        return ctx
+
+    vspec = scenes.water_drop(total=60_000, seed=3, basic_pbf=True)
+    case = ValidationCase(make=vmake, dt=vspec.dt, before=vspec.meta["presteps"], counted=12)
+    nets = {"a": net}
+    choice, table = select_warm_start(nets, [case], (1.5, 2.0, 4.0))
+    again, table2 = select_warm_start(nets, [case], (1.5, 2.0, 4.0))
+    assert table2 == table
+    cands = table["candidates"]
+    admissible = {k: v for k, v in cands.items() if v["admissible"]}
+    if choice is None:
+        assert not admissible and again is None
+    else:
+        assert again["omega_max"] == choice["omega_max"]
+        assert (net.omega_max, net.min_neighbors) == (choice["omega_max"], choice["min_neighbors"])
+        assert cands[f"a / omega {choice['omega_max']:g}"]["admissible"]
+        assert cands[f"a / omega {choice['omega_max']:g}"]["passes"] == min(v["passes"] for v in admissible.values())
+        ref = table["plain"][0]["reference_rule"]
+        assert all(r <= table["energy_bound"][0] / max(ref["mean_v2"], 1e-30) + 1e-3
+                   for v in admissible.values() for r in v["energy_ratio"])
+        assert all(r <= table["height_bound"][0] / max(ref["y_p99"], 1e-30) + 1e-3
+                   for v in admissible.values() for r in v["height_ratio"])
+        chosen = evaluate(N.WARM_LEARNED | N.WARM_PROJECTED)
+        assert chosen[1] == 30
+    none, _ = select_warm_start(nets, [case], (2.0,), energy_slack=1e-9)
+    assert none is None
