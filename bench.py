@@ -453,6 +453,7 @@ def run_arm(spec, args, local, mode: int, net, dist, headline: bool) -> tuple[di
     torch.cuda.synchronize()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    window = _window_snapshot(ctx) if headline else None  # the e2e run replays this window
     n_start, _ = ctx.lengths()
     ctx.check_status()  # clears the pass and convergence counters
     launches0 = ctx.launch_count()
@@ -510,7 +511,7 @@ def run_arm(spec, args, local, mode: int, net, dist, headline: bool) -> tuple[di
          "tuning": tuning,
          "state_after": _state_summary(ctx)}
     if headline:
-        r["_prof"], r["_dropped"], r["_clocks"] = prof, dropped, clk
+        r["_prof"], r["_dropped"], r["_clocks"], r["_window"] = prof, dropped, clk, window
     return r, ctx
 
 
@@ -581,6 +582,7 @@ def run_ours(args) -> None:
     prof = head.pop("_prof")
     dropped = head.pop("_dropped")
     clk = head.pop("_clocks")
+    window = head.pop("_window")
     dom = max(prof.items(), key=lambda kv: kv[1][1]) if prof else None
     roof = None
     if dom:
@@ -599,7 +601,7 @@ def run_ours(args) -> None:
     kernel_us = {k: round(v[1] / max(v[0], 1) * 1000.0, 2) for k, v in prof.items()}  # mean per launch
 
     # e2e: the same substep driven from pinned host buffers through the C ABI
-    e2e = run_e2e(ctx, spec, args, local)
+    e2e = run_e2e(ctx, spec, args, window)
     check = oracle_check(ctx, spec) if rank == 0 and not args.no_oracle_check else None
 
     cpu = None
@@ -756,6 +758,7 @@ def run_batch(args) -> None:
         batch.substep(dt)
     for c in ctxs:
         c.check_status()
+    windows = [_window_snapshot(c) for c in ctxs]  # the sequential and e2e runs replay this window
     n_total = sum(sp.n for sp in specs)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
     stream = torch.cuda.current_stream()
@@ -780,7 +783,10 @@ def run_batch(args) -> None:
     conv = sum(i.converged_substeps for i in infos)
     value = n_total * args.steps / (total_ms / 1000.0)
 
-    # the same scenes one after the other (each a whole-substep graph), same state
+    # the same scenes one after the other (each a whole-substep graph), the same
+    # window replayed from its start state
+    for c, w in zip(ctxs, windows):
+        _restore_window(c, w)
     ev2 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     torch.cuda.synchronize()
     for k in range(args.steps):
@@ -791,10 +797,11 @@ def run_batch(args) -> None:
         ev2[k][1].record(stream)
     torch.cuda.synchronize()
     seq_ms = float(np.sum([a.elapsed_time(b) for a, b in ev2]))
+    seq_passes = sum(c.check_status().density_passes for c in ctxs) / (len(ctxs) * args.steps)
 
     # per-scene density error: the device's FP64 value against the oracle's FP64
     # recomputation on the same (downloaded) state, for every 8th scene
-    e2e = run_batch_e2e(batch, ctxs, args, dt)
+    e2e = run_batch_e2e(batch, ctxs, args, dt, windows)
     check = []
     if rank == 0 and not args.no_cpu_baseline:
         from apbf_gb300.api import incompressibility, neighborhood_green
@@ -840,7 +847,9 @@ def run_batch(args) -> None:
                        "l2": "flushed between timed steps (256 MB write)"},
             "sequential": {"ms_per_step": seq_ms / args.steps,
                            "value": n_total * args.steps / (seq_ms / 1000.0),
-                           "note": "the same scenes, one whole-substep graph launch each, one after the other"},
+                           "density_passes_per_scene_substep": seq_passes,
+                           "note": "the same window of the same scenes replayed, one whole-substep graph launch "
+                                   "each, one after the other"},
             "scene_density_error_last_pass": {"min": min(errs), "max": max(errs), "mean": float(np.mean(errs))},
             "oracle_density_error_check": check,
             "warm_start_training": {"samples": n_samples, "seconds": round(train_s, 2),
@@ -851,77 +860,156 @@ def run_batch(args) -> None:
         print(json.dumps(line), flush=True)
 
 
-def run_batch_e2e(batch, ctxs, args, dt) -> dict:
-    """Per step: H2D of every scene's positions and velocities from pinned host memory,
-    one batched substep, D2H of the resulting positions and velocities."""
+def run_batch_e2e(batch, ctxs, args, dt, windows) -> dict:
+    """The batch's timed window again, driven from host memory, through the C ABI's
+    host-buffer calls for every scene: apbf_fluid_write of the scene's full particle
+    state from pinned host memory, one batched substep (one graph launch), each
+    scene's new particle count, and apbf_fluid_read of every full state back, then a
+    stream synchronisation.  Warm-up and timed steps each start from the window's
+    start state."""
     import torch
 
-    hosts = []
-    for c in ctxs:
-        n, _ = c.lengths()
-        v = c.fluid_view()
-        hosts.append((n, v["position"][:n].cpu().pin_memory(), v["velocity"][:n].cpu().pin_memory()))
-    nbytes = sum(p.numel() * 4 + q.numel() * 4 for _, p, q in hosts)
-    steps = max(3, min(args.steps, 10))
     stream = torch.cuda.current_stream()
+    hosts = [_host_lists(c) for c in ctxs]
+    counts = [torch.zeros(1, dtype=torch.int32).pin_memory() for _ in ctxs]
+    per_particle = sum(t[0].numel() * t.element_size() for t in hosts[0].values())
+
+    def step(ns):
+        for c, h, n in zip(ctxs, hosts, ns):
+            c.fluid_write(h, n)
+        batch.substep(dt)
+        out = []
+        for c, h, cnt in zip(ctxs, hosts, counts):
+            m, _ = c.lengths()
+            c.fluid_read(h, m, cnt)
+            out.append(m)
+        stream.synchronize()
+        return out
+
+    def restart():
+        for c, w, h in zip(ctxs, windows, hosts):
+            _restore_window(c, w, h)
+        return [w["n"] for w in windows]
+
+    steps = args.steps
+    ns = restart()
+    for _ in range(min(args.warmup, steps)):
+        ns = step(ns)
+    ns = restart()
+    for c in ctxs:
+        c.check_status()
+    h2d = d2h = total = 0
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    total = 0
     for _ in range(steps):
-        for c, (n, p, q) in zip(ctxs, hosts):
-            v = c.fluid_view()
-            v["position"][:n].copy_(p, non_blocking=True)
-            v["velocity"][:n].copy_(q, non_blocking=True)
-        batch.substep(dt)
-        for c, (n, p, q) in zip(ctxs, hosts):
-            v = c.fluid_view()
-            p.copy_(v["position"][:n], non_blocking=True)
-            q.copy_(v["velocity"][:n], non_blocking=True)
-            total += n
-        stream.synchronize()
+        h2d += sum(ns) * per_particle
+        ns = step(ns)
+        d2h += sum(ns) * per_particle + 4 * len(ns)
+        total += sum(ns)
     el = time.perf_counter() - t0
-    return {"value": total / el, "unit": UNIT, "h2d_bytes_per_step": int(nbytes), "d2h_bytes_per_step": int(nbytes),
-            "steps": steps}
+    infos = [c.check_status() for c in ctxs]
+    return {"value": total / el, "unit": UNIT, "h2d_bytes_per_step": int(h2d / steps),
+            "d2h_bytes_per_step": int(d2h / steps), "steps": steps, "warmup": min(args.warmup, steps),
+            "density_passes_per_scene_substep": sum(i.density_passes for i in infos) / (len(ctxs) * steps),
+            "window": "the device-resident timed window replayed from its start state",
+            "api": "per scene apbf_fluid_write, one batched substep, per scene apbf_get_lengths + apbf_fluid_read "
+                   "(C ABI, pinned host buffers)"}
 
 
-def run_e2e(ctx, spec, args, local) -> dict:
-    """Per step, through the C ABI's host-buffer calls: apbf_fluid_write of the full
-    particle state (the ten lists and the warm start's lambda history) from pinned
-    host memory, one apbf_substep, the new particle count (an emitter or split/merge
-    changes it), apbf_fluid_read of the full resulting state back into pinned host
-    memory, then a stream synchronisation."""
+def _host_lists(ctx) -> dict:
+    """Pinned host arrays for every particle list of `ctx` (capacity rows) and the
+    carried lambda sums: the layout apbf_fluid_write / apbf_fluid_read take."""
     import torch
 
     from apbf_gb300.api import FLUID_FIELDS
 
-    cap = ctx.capacity
-    host = {}
-    for k, (dt, comp) in FLUID_FIELDS.items():
-        host[k] = torch.empty((cap, comp) if comp > 1 else (cap,), dtype=dt).pin_memory()
-    host["lambda_prev"] = torch.empty(cap, dtype=torch.float32).pin_memory()
+    h = {k: torch.empty((ctx.capacity, c) if c > 1 else (ctx.capacity,), dtype=d).pin_memory()
+         for k, (d, c) in FLUID_FIELDS.items()}
+    h["lambda_prev"] = torch.empty(ctx.capacity, dtype=torch.float32).pin_memory()
+    return h
+
+
+def _window_snapshot(ctx) -> dict:
+    """Everything a substep carries to the next (the particle lists with the carried
+    lambda sums in pinned host memory, the transfer list on the device), taken at the
+    start of the timed window.  An emitter's phase is not part of it."""
+    import torch
+
+    n, nt = ctx.lengths()
+    host = _host_lists(ctx)
+    cnt = torch.zeros(1, dtype=torch.int32).pin_memory()
+    ctx.fluid_read(host, n, cnt)
+    tv = ctx.transfers_view()
+    tr = {k: tv[k][:nt].clone() for k in ("source", "target", "time_left")}
+    torch.cuda.synchronize()
+    return {"host": host, "n": n, "nt": nt, "transfers": tr}
+
+
+def _restore_window(ctx, w: dict, work: dict | None = None) -> None:
+    """Puts the transfer list back on the device and the snapshot's particle lists
+    into the caller's host arrays (`work`), or with work=None straight into the
+    device lists; untimed setup."""
+    import torch
+
+    tv = ctx.transfers_view()
+    for k, v in w["transfers"].items():
+        tv[k][:w["nt"]].copy_(v)
+    ctx.set_lengths(w["n"], w["nt"])
+    if work is None:
+        ctx.fluid_write(w["host"], w["n"])
+    else:
+        for k, v in w["host"].items():
+            work[k].copy_(v)
+    torch.cuda.synchronize()
+
+
+def run_e2e(ctx, spec, args, window: dict) -> dict:
+    """The timed window again, driven from host memory: per step, through the C ABI,
+    apbf_fluid_write of the full particle state (the ten lists and the warm start's
+    lambda history) from pinned host memory, one apbf_substep, the new particle count
+    (an emitter or split/merge changes it), apbf_fluid_read of the full resulting state
+    back into pinned host memory, then a stream synchronisation.  Warm-up and timed
+    steps each start from the state at the start of the device-resident timed window,
+    so both measurements time the same substeps (same pass counts, reported)."""
+    import torch
+
+    host = _host_lists(ctx)
     per_particle = sum(t[0].numel() * t.element_size() for t in host.values())
     count = torch.zeros(1, dtype=torch.int32).pin_memory()
     stream = torch.cuda.current_stream()
-    n, _ = ctx.lengths()
-    ctx.fluid_read(host, n, count)  # the current state, as a host-driven caller holds it
-    stream.synchronize()
-    steps = max(3, min(args.steps, 10))
+    steps = args.steps
+
+    def step(n):
+        ctx.fluid_write(host, n)
+        ctx.substep(spec.dt)
+        m, _ = ctx.lengths()  # synchronises: the count the read needs
+        ctx.fluid_read(host, m, count)
+        stream.synchronize()
+        return m
+
+    _restore_window(ctx, window, host)
+    n = window["n"]
+    for _ in range(min(args.warmup, steps)):  # untimed
+        n = step(n)
+    _restore_window(ctx, window, host)
+    n = window["n"]
+    ctx.check_status()  # clears the counters
     h2d = d2h = 0
     done = 0
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(steps):
-        ctx.fluid_write(host, n)
         h2d += n * per_particle
-        ctx.substep(spec.dt)
-        n, _ = ctx.lengths()  # synchronises: the count the read needs
-        ctx.fluid_read(host, n, count)
+        n = step(n)
         d2h += n * per_particle + 4
         done += n
-        stream.synchronize()
     el = time.perf_counter() - t0
+    info = ctx.check_status()
     return {"value": done / el, "unit": UNIT, "h2d_bytes_per_step": int(h2d / steps),
-            "d2h_bytes_per_step": int(d2h / steps), "steps": steps,
+            "d2h_bytes_per_step": int(d2h / steps), "steps": steps, "warmup": min(args.warmup, steps),
+            "density_passes_per_substep": info.density_passes / steps,
+            "converged_substeps": f"{info.converged_substeps}/{steps}",
+            "window": "the device-resident timed window replayed from its start state",
             "api": "apbf_fluid_write + apbf_substep + apbf_get_lengths + apbf_fluid_read (C ABI, pinned host buffers)"}
 
 
