@@ -792,11 +792,11 @@ apbf_status mlp_lambda(apbf_ctx *ctx, cudaStream_t s, bool early_exit) {
     o.pk = ctx->solve_pk;
     o.shift = ctx->shift;
     o.st = ctx->status;
-    APBF_BEFORE_LAUNCH(ctx, s, "k_mlp_lambda");
+    APBF_BEFORE_LAUNCH(ctx, s, "k_mlp_tc");
     k_mlp_tc<1><<<tc_grid(ctx->cfg.particle_capacity), kTcRows, 0, s>>>(
         ctx->mlp_params, reinterpret_cast<const TcImage *>(ctx->mlp_image), ctx->features, 0u, ctx->d_len,
         early_exit ? 1 : 0, o);
-    APBF_AFTER_LAUNCH(ctx, s, "k_mlp_lambda");
+    APBF_AFTER_LAUNCH(ctx, s, "k_mlp_tc");
     return APBF_OK;
 }
 
