@@ -36,6 +36,104 @@ apbf_status dalloc(T **p, size_t count, std::vector<void *> &owned) {
 
 // gpu_list::set_length from a host value, stream-ordered (no synchronisation).
 __global__ void k_set_length(uint32_t *d_len, uint32_t slot, uint32_t v) { d_len[slot] = v; }
+
+// Host <-> device copy of the particle lists in one launch.  Each field is a byte
+// range of a multiple of 4 bytes; host ranges are page-locked host memory that the
+// GPU addresses directly (pointers from cudaPointerGetAttributes), so the loads or
+// stores of this kernel cross the CPU-GPU link while the device side is HBM.  One
+// grid row (blockIdx.y) per field; 16-byte units where both ends are 16-byte aligned.
+struct CopyField {
+    char *dst;
+    const char *src;
+    unsigned long long bytes;
+    int vec16;
+};
+constexpr int kMaxCopyFields = 11;
+struct CopyList {
+    CopyField f[kMaxCopyFields];
+};
+
+__global__ void __launch_bounds__(256) k_copy_fields(CopyList list) {
+    const CopyField fd = list.f[blockIdx.y];
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    const unsigned long long t = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long done = 0;
+    if (fd.vec16) {
+        const unsigned long long n16 = fd.bytes >> 4;
+        const uint4 *src = reinterpret_cast<const uint4 *>(fd.src);
+        uint4 *dst = reinterpret_cast<uint4 *>(fd.dst);
+        // four independent 16-byte loads in flight per thread: the link's latency is long
+        for (unsigned long long i = t; i < n16; i += 4 * stride) {
+            uint4 v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (i + u * stride < n16) v[u] = src[i + u * stride];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (i + u * stride < n16) dst[i + u * stride] = v[u];
+        }
+        done = n16 << 4;
+    }
+    const unsigned long long n4 = (fd.bytes - done) >> 2;
+    const uint32_t *src = reinterpret_cast<const uint32_t *>(fd.src + done);
+    uint32_t *dst = reinterpret_cast<uint32_t *>(fd.dst + done);
+    for (unsigned long long i = t; i < n4; i += 4 * stride) {
+        uint32_t v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (i + u * stride < n4) v[u] = src[i + u * stride];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (i + u * stride < n4) dst[i + u * stride] = v[u];
+    }
+}
+
+// The device address of page-locked host memory at `p`, or nullptr when `p` is
+// ordinary (pageable) host memory or not host memory at all.
+void *mapped_host(const void *p) {
+    if (!p) return nullptr;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();  // clears the error of an unknown pointer
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+// Copies `nf` fields of `n` particles (bytes per particle each) between host and
+// device: one k_copy_fields launch for the page-locked host arrays, cudaMemcpyAsync
+// for the others.  to_device: host -> device.
+apbf_status copy_fluid_fields(apbf_ctx *ctx, void *const *dev, void *const *host, const size_t *bpp, int nf, size_t n,
+                              bool to_device, cudaStream_t s) {
+    CopyList list = {};
+    int nk = 0;
+    size_t largest = 0;
+    for (int k = 0; k < nf; ++k) {
+        if (!host[k] || !n) continue;
+        const size_t bytes = n * bpp[k];
+        void *mh = mapped_host(host[k]);
+        if (!mh) {
+            APBF_CUDA(to_device ? cudaMemcpyAsync(dev[k], host[k], bytes, cudaMemcpyHostToDevice, s)
+                                : cudaMemcpyAsync(host[k], dev[k], bytes, cudaMemcpyDeviceToHost, s));
+            continue;
+        }
+        CopyField &fd = list.f[nk++];
+        fd.dst = static_cast<char *>(to_device ? dev[k] : mh);
+        fd.src = static_cast<const char *>(to_device ? mh : dev[k]);
+        fd.bytes = bytes;
+        fd.vec16 = ((reinterpret_cast<uintptr_t>(fd.dst) | reinterpret_cast<uintptr_t>(fd.src)) & 15u) == 0;
+        largest = bytes > largest ? bytes : largest;
+    }
+    if (nk) {
+        const size_t units = (largest + 15) / 16;
+        const unsigned gx = (unsigned)std::max<size_t>(1, std::min<size_t>((units + 1023) / 1024,
+                                                                           (size_t)ctx->num_sms * 2));
+        APBF_BEFORE_LAUNCH(ctx, s, "k_copy_fields");
+        k_copy_fields<<<dim3(gx, (unsigned)nk), 256, 0, s>>>(list);
+        APBF_AFTER_LAUNCH(ctx, s, "k_copy_fields");
+    }
+    return APBF_OK;
+}
 }  // namespace apbf
 
 using namespace apbf;
@@ -399,6 +497,9 @@ apbf_status apbf_set_lengths(apbf_ctx *ctx, uint32_t np, uint32_t nt, void *stre
     return APBF_OK;
 }
 
+// Bytes per particle of the lists in apbf_host_fluid order.
+static const size_t kFluidFieldBytes[11] = {16, 16, 4, 4, 16, 4, 4, 4, 4, 4, 4};
+
 apbf_status apbf_fluid_write(apbf_ctx *ctx, const apbf_host_fluid *in, uint32_t count, void *stream) {
     if (!ctx || !in) return APBF_ERR_INVALID_ARG;
     if (count > ctx->cfg.particle_capacity) {
@@ -408,18 +509,13 @@ apbf_status apbf_fluid_write(apbf_ctx *ctx, const apbf_host_fluid *in, uint32_t 
     cudaSetDevice(ctx->device);
     cudaStream_t s = (cudaStream_t)stream;
     const FluidBufs &f = ctx->fl[ctx->fcur];
-    const size_t n = count;
-    const struct {
-        void *dst;
-        const void *src;
-        size_t bytes;
-    } fields[] = {{f.pos, in->position, 16}, {f.vel, in->velocity, 16}, {f.inv_mass, in->inverse_mass, 4},
-                  {f.radius, in->radius, 4}, {f.pos_backup, in->pos_backup, 16}, {f.transferring, in->transferring, 4},
-                  {f.target_radius, in->target_radius, 4}, {f.kernel_width, in->kernel_width, 4},
-                  {f.boundariness, in->boundariness, 4}, {f.boundary_distance, in->boundary_distance, 4},
-                  {f.lambda_prev, in->lambda_prev, 4}};
-    for (const auto &fd : fields)
-        if (fd.src && n) APBF_CUDA(cudaMemcpyAsync(fd.dst, fd.src, n * fd.bytes, cudaMemcpyHostToDevice, s));
+    void *const dev[] = {f.pos, f.vel, f.inv_mass, f.radius, f.pos_backup, f.transferring, f.target_radius,
+                         f.kernel_width, f.boundariness, f.boundary_distance, f.lambda_prev};
+    void *const host[] = {in->position,      in->velocity,    in->inverse_mass,      in->radius,
+                          in->pos_backup,    in->transferring, in->target_radius,    in->kernel_width,
+                          in->boundariness,  in->boundary_distance, in->lambda_prev};
+    apbf_status r = apbf::copy_fluid_fields(ctx, dev, host, kFluidFieldBytes, 11, count, true, s);
+    if (r != APBF_OK) return r;
     APBF_BEFORE_LAUNCH(ctx, s, "k_set_length");
     apbf::k_set_length<<<1, 1, 0, s>>>(ctx->d_len, kLenParticles, count);
     APBF_AFTER_LAUNCH(ctx, s, "k_set_length");
@@ -433,18 +529,12 @@ apbf_status apbf_fluid_read(apbf_ctx *ctx, apbf_host_fluid *out, uint32_t max_co
     const FluidBufs &f = ctx->fl[ctx->fcur];
     const size_t n = std::min(max_count, ctx->cfg.particle_capacity);
     APBF_CUDA(cudaMemcpyAsync(h_count, ctx->d_len + kLenParticles, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-    const struct {
-        void *dst;
-        const void *src;
-        size_t bytes;
-    } fields[] = {{out->position, f.pos, 16}, {out->velocity, f.vel, 16}, {out->inverse_mass, f.inv_mass, 4},
-                  {out->radius, f.radius, 4}, {out->pos_backup, f.pos_backup, 16},
-                  {out->transferring, f.transferring, 4}, {out->target_radius, f.target_radius, 4},
-                  {out->kernel_width, f.kernel_width, 4}, {out->boundariness, f.boundariness, 4},
-                  {out->boundary_distance, f.boundary_distance, 4}, {out->lambda_prev, f.lambda_prev, 4}};
-    for (const auto &fd : fields)
-        if (fd.dst && n) APBF_CUDA(cudaMemcpyAsync(fd.dst, fd.src, n * fd.bytes, cudaMemcpyDeviceToHost, s));
-    return APBF_OK;
+    void *const dev[] = {f.pos, f.vel, f.inv_mass, f.radius, f.pos_backup, f.transferring, f.target_radius,
+                         f.kernel_width, f.boundariness, f.boundary_distance, f.lambda_prev};
+    void *const host[] = {out->position, out->velocity, out->inverse_mass, out->radius, out->pos_backup,
+                          out->transferring, out->target_radius, out->kernel_width, out->boundariness,
+                          out->boundary_distance, out->lambda_prev};
+    return apbf::copy_fluid_fields(ctx, dev, host, kFluidFieldBytes, 11, n, false, s);
 }
 
 apbf_status apbf_get_lengths(apbf_ctx *ctx, uint32_t *np, uint32_t *nt, void *stream) {
