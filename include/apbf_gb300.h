@@ -256,13 +256,15 @@ apbf_status apbf_get_lengths(apbf_ctx *ctx, uint32_t *n_particles, uint32_t *n_t
 /* gpu_list::write().buffer() filled from the host + set_length (source/gpu_list.h:82-91,
  * 173-180) for every particle list at once: enqueues the copies of `count` particles
  * from host memory and sets the particle length; nothing else of the state changes
- * (transfers, lambda history unless given).  Stream-ordered, no synchronisation; with
- * pinned host memory the copies are asynchronous. */
+ * (transfers, lambda history unless given).  Stream-ordered, no synchronisation.
+ * Page-locked host arrays (cudaHostAlloc / cudaHostRegister) are read by one copy
+ * kernel for all of them; pageable arrays are copied with cudaMemcpyAsync. */
 apbf_status apbf_fluid_write(apbf_ctx *ctx, const apbf_host_fluid *in, uint32_t count, void *stream);
 /* gpu_list::read (source/gpu_list.h:153-170) for every particle list at once: enqueues
  * the copy of the particle length into *h_count and of the first max_count entries of
  * every non-null field into host memory.  After the stream is synchronised, *h_count
- * is the number of particles (entries past min(*h_count, max_count) are not state). */
+ * is the number of particles (entries past min(*h_count, max_count) are not state).
+ * Page-locked host arrays are written by one copy kernel for all of them. */
 apbf_status apbf_fluid_read(apbf_ctx *ctx, apbf_host_fluid *out, uint32_t max_count, uint32_t *h_count, void *stream);
 
 /* ---- stages (each replaces one reference stage's apply()) ---- */
