@@ -303,7 +303,9 @@ def select_warm_start(nets: dict, cases: list, omegas=OMEGA_CANDIDATES, min_neig
     its condition.
 
     Returns ({"net": key, "omega_max", "min_neighbors", "params": tensor} or None
-    when no candidate is admissible, and a table of every run)."""
+    when no candidate is admissible — the networks then keep the guards they came
+    with — and a table of every run)."""
+    guards = {k: (net.omega_max, net.min_neighbors) for k, net in nets.items()}
     plain = []
     for c in cases:
         plain.append({"reference_rule": run_case(c, 0), "projected_rule": run_case(c, N.WARM_PROJECTED)})
@@ -336,6 +338,8 @@ def select_warm_start(nets: dict, cases: list, omegas=OMEGA_CANDIDATES, min_neig
             if ok and (best is None or (score, om) < (best[0], best[2])):
                 best = (score, key, om, params)
     if best is None:
+        for k, net in nets.items():
+            net.omega_max, net.min_neighbors = guards[k]
         return None, table
     _, key, om, params = best
     nets[key].omega_max, nets[key].min_neighbors = om, min_neighbors

@@ -142,8 +142,11 @@ def test_bound_comes_from_the_converging_plain_rule():
 def test_no_admissible_candidate_and_slacks_off():
     t = {**PLAIN, (0, 2.0): (12.0, 1.0, 300.0, 200.0), (0, 3.0): (10.0, 1.0, 500.0, 400.0)}
     case, _ = _case(t)
-    choice, table = select_warm_start({"a": FakeNet(0)}, [case], (2.0, 3.0))
+    net = FakeNet(0)
+    net.omega_max, net.min_neighbors = 7.0, 9.0
+    choice, table = select_warm_start({"a": net}, [case], (2.0, 3.0))
     assert choice is None and not any(v["admissible"] for v in table["candidates"].values())
+    assert (net.omega_max, net.min_neighbors) == (7.0, 9.0)  # left as it came
     choice, _ = select_warm_start({"a": FakeNet(0)}, [case], (2.0, 3.0), energy_slack=0.0, height_slack=0.0)
     assert choice["omega_max"] == 3.0  # only convergence is left to check
 
