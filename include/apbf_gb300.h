@@ -412,8 +412,9 @@ apbf_status apbf_launch_count(apbf_ctx *ctx, unsigned long long *out);
  * neighbour count, rho/rho0 - 1, kernel width / radius, the plain Jacobi lambda,
  * velocity divergence / density, the sum of the lambdas applied to the particle
  * in the previous substep, and that sum's mean over the neighbours (8 slots, 7
- * used) -- to the lambda used by that substep's first position update.  Later iterations are the plain solve, which stays the judge of the
- * density error (density_error_target).  Parameters are one FP32 vector of
+ * used) -- to the lambda used by that substep's first position update.  Later
+ * iterations are the plain solve, which still measures the density error and
+ * stops at density_error_target.  Parameters are one FP32 vector of
  * apbf_mlp_param_count() floats: mu[8], 1/sigma[8], W1[64][8], b1[64],
  * W2[64][64], b2[64], w3[64], b3, y_scale, y_mean (lambda = y * y_scale + y_mean),
  * omega_max (> 0: the learned lambda is clamped to [omega_max * lambda, lambda]
