@@ -186,9 +186,11 @@ def oracle_boxes(spec) -> tuple:
     return (np.concatenate([spec.box_min, c]), np.concatenate([spec.box_max, h]), rot)
 
 
-def cpu_baseline(workload: str, budget_s: float = 15.0) -> dict:
-    """The single-threaded FP64 oracle on a bounded sample: the same scene at 1/8 of
-    the particle count (every length halved), substeps until the budget is spent."""
+def cpu_sample(workload: str, budget_s: float = 15.0) -> dict:
+    """The single-threaded oracle on a bounded sample: the same scene at 1/8 of the
+    particle count (every length halved), substeps until the budget is spent.  The
+    oracle library is the FP64 checker, or its FP32 build when the process was
+    started with APBF_ORACLE_VARIANT=f32."""
     from oracle import oracle as orc
 
     spec = make_spec(workload, scale=1.0 / 8.0)
@@ -210,11 +212,32 @@ def cpu_baseline(workload: str, budget_s: float = 15.0) -> dict:
         if time.perf_counter() - t0 > budget_s or steps >= 20:
             break
     el = time.perf_counter() - t0
-    return {"value": processed / el, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"{steps} substep(s) from the start of the {spec.n}-particle (1/8 scale) version of the "
-                      f"scene, reference Jacobi rule until {settings_dict(spec)['density_error_target']} "
-                      f"(max {settings_dict(spec)['solver_iterations']} passes), single-threaded FP64 oracle, "
-                      f"{el:.1f} s"}
+    return {"value": processed / el, "steps": steps, "particles": int(spec.n), "seconds": round(el, 1),
+            "library": orc.LIB.name}
+
+
+def cpu_baseline(workload: str, budget_s: float = 15.0) -> dict:
+    """The oracle timed on this host: the FP64 checker in this process, then the FP32
+    build of the same code in a child process (same sample, same single thread)."""
+    r64 = cpu_sample(workload, budget_s)
+    env = dict(os.environ, APBF_ORACLE_VARIANT="f32")
+    code = (f"import sys, json; sys.path.insert(0, {str(ROOT)!r}); import bench; "
+            f"print(json.dumps(bench.cpu_sample({workload!r}, {budget_s!r})))")
+    fp32 = None
+    try:
+        out = subprocess.run([sys.executable, "-c", code], env=env, cwd=str(ROOT), capture_output=True, text=True,
+                             timeout=budget_s * 10 + 120, check=True)
+        r32 = json.loads(out.stdout.strip().splitlines()[-1])
+        fp32 = {"value": r32["value"], "unit": UNIT, "cores": 1, "library": r32["library"],
+                "sample": f"the same sample, {r32['steps']} substep(s), {r32['seconds']} s"}
+    except (subprocess.SubprocessError, ValueError, IndexError) as e:
+        fp32 = {"unavailable": f"{type(e).__name__}: {str(e)[:200]}"}
+    s = settings_dict(make_spec(workload, scale=1.0 / 8.0))
+    return {"value": r64["value"], "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{r64['steps']} substep(s) from the start of the {r64['particles']}-particle (1/8 scale) "
+                      f"version of the scene, reference Jacobi rule until {s['density_error_target']} "
+                      f"(max {s['solver_iterations']} passes), single-threaded FP64 oracle, {r64['seconds']} s",
+            "fp32": fp32}
 
 
 def _replica_loop(conn, name, scale, seed):

@@ -47,6 +47,30 @@
 static const double kPi = F32(3.14159265);          /* kernels.glsl:1 */
 static const double kTwoThirds = F32(2.0f / 3.0f);  /* 2.0f / DIMENSIONS */
 
+/* The kernels and the incompressibility passes compute in or_real: double (the
+ * oracle), or float in the FP32 build (-DOR_FP32) that is only timed as a CPU
+ * baseline.  In the double build every macro below is the identity. */
+#ifdef OR_FP32
+#define RPOW powf
+#define REXP expf
+#define RSQRT sqrtf
+#define RFMIN fminf
+#else
+#define RPOW pow
+#define REXP exp
+#define RSQRT sqrt
+#define RFMIN fmin
+#endif
+#ifdef OR_FP32
+typedef float or_real;
+#else
+typedef double or_real;
+#endif
+#define RL(x) ((or_real)(x))
+#define F32R(x) ((or_real)(float)(x))
+#define PI_R ((or_real)kPi)
+#define TWO_THIRDS_R ((or_real)kTwoThirds)
+
 /* ------------------------------------------------------------------ */
 /* conversions (C4)                                                    */
 /* ------------------------------------------------------------------ */
@@ -488,90 +512,90 @@ uint64_t or_neighborhood_binary_search(or_fluid *f, or_transfers *t, float range
 }
 
 /* ------------------------------------------------------------------ */
-/* smoothing kernels (kernels.glsl), FP64                              */
+/* smoothing kernels (kernels.glsl), in or_real (FP64; FP32 build)   */
 /* ------------------------------------------------------------------ */
-static double dot3(const double a[3], const double b[3]) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
-static double len3(const double a[3]) { return sqrt(dot3(a, a)); }
+static or_real dot3(const or_real a[3], const or_real b[3]) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+static or_real len3(const or_real a[3]) { return RSQRT(dot3(a, a)); }
 
-static double gauss_height_param(double kw) {  /* kernels.glsl:104 */
-    double half = kw / 2.0;
-    return F32(0.6f) / (half * half * half);
+static or_real gauss_height_param(or_real kw) {  /* kernels.glsl:104 */
+    or_real half = kw / RL(2.0);
+    return F32R(0.6f) / (half * half * half);
 }
-static double gauss_height(const double r[3], double height) {  /* kernels.glsl:84-89 */
-    double ivw = pow(height, kTwoThirds);
-    double ivd = ivw * kPi;
-    return exp(-dot3(r, r) * ivd) * pow(ivw, 1.5);
+static or_real gauss_height(const or_real r[3], or_real height) {  /* kernels.glsl:84-89 */
+    or_real ivw = RPOW(height, TWO_THIRDS_R);
+    or_real ivd = ivw * PI_R;
+    return REXP(-dot3(r, r) * ivd) * RPOW(ivw, RL(1.5));
 }
 
-double or_kernel_height(int id, const double r[3], double h) {
-    double dist = len3(r);
+static or_real kheight(int id, const or_real r[3], or_real h) {
+    or_real dist = len3(r);
     switch (id) {
     case 0: { /* cubic, kernels.glsl:18-31 */
-        if (dist > h) return 0.0;
-        double q = dist / h;
-        double k = 8.0 / (kPi * h * h * h);
-        if (q <= 0.5) return k * (6.0 * q * q * q - 6.0 * q * q + 1.0);
-        return k * (2.0 * pow(1.0 - q, 3.0));
+        if (dist > h) return RL(0.0);
+        or_real q = dist / h;
+        or_real k = RL(8.0) / (PI_R * h * h * h);
+        if (q <= RL(0.5)) return k * (RL(6.0) * q * q * q - RL(6.0) * q * q + RL(1.0));
+        return k * (RL(2.0) * RPOW(RL(1.0) - q, RL(3.0)));
     }
     case 1: return gauss_height(r, gauss_height_param(h));
     case 2: { /* poly6, kernels.glsl:3-9 */
-        double r2 = dot3(r, r), h2 = h * h;
-        if (r2 > h2) return 0.0;
-        return 315.0 * pow(h2 - r2, 3.0) / (64.0 * kPi * pow(h, 9.0));
+        or_real r2 = dot3(r, r), h2 = h * h;
+        if (r2 > h2) return RL(0.0);
+        return RL(315.0) * RPOW(h2 - r2, RL(3.0)) / (RL(64.0) * PI_R * RPOW(h, RL(9.0)));
     }
     case 3: { /* cone, kernels.glsl:48-52 */
-        double height = 3.0 / (kPi * pow(h, 3.0));
-        double v = (1.0 - dist / h) * height;
-        return v > 0.0 ? v : 0.0;
+        or_real height = RL(3.0) / (PI_R * RPOW(h, RL(3.0)));
+        or_real v = (RL(1.0) - dist / h) * height;
+        return v > RL(0.0) ? v : RL(0.0);
     }
     case 4: { /* quadratic spike, kernels.glsl:62-70 (C12) */
-        double a = 15.0 / (2.0 * kPi * pow(h, 5.0));
-        if (dist >= h) return 0.0;
+        or_real a = RL(15.0) / (RL(2.0) * PI_R * RPOW(h, RL(5.0)));
+        if (dist >= h) return RL(0.0);
         return a * (h - dist) * (h - dist);
     }
-    default: return 0.0;
+    default: return RL(0.0);
     }
 }
 
-void or_kernel_gradient(int id, const double r[3], double h, double out[3]) {
-    double dist = len3(r);
-    out[0] = out[1] = out[2] = 0.0;
+static void kgrad(int id, const or_real r[3], or_real h, or_real out[3]) {
+    or_real dist = len3(r);
+    out[0] = out[1] = out[2] = RL(0.0);
     switch (id) {
     case 0: { /* kernels.glsl:33-46 */
-        if (dist > h || dist < F32(0.0001f)) return;
-        double q = dist / h;
-        double l = 48.0 / (kPi * h * h * h);
-        double s = q <= 0.5 ? l * q * (3.0 * q - 2.0) : l * (-(1.0 - q) * (1.0 - q));
-        double inv = 1.0 / (dist * h);
+        if (dist > h || dist < F32R(0.0001f)) return;
+        or_real q = dist / h;
+        or_real l = RL(48.0) / (PI_R * h * h * h);
+        or_real s = q <= RL(0.5) ? l * q * (RL(3.0) * q - RL(2.0)) : l * (-(RL(1.0) - q) * (RL(1.0) - q));
+        or_real inv = RL(1.0) / (dist * h);
         for (int d = 0; d < 3; ++d) out[d] = s * (r[d] * inv);
         return;
     }
     case 1: { /* kernels.glsl:91-97 */
-        if (dist < F32(0.0001f)) return;
-        double height = gauss_height_param(h);
-        double ivd = pow(height, kTwoThirds) * kPi;
-        double s = -gauss_height(r, height) * 2.0 * dist * ivd;
+        if (dist < F32R(0.0001f)) return;
+        or_real height = gauss_height_param(h);
+        or_real ivd = RPOW(height, TWO_THIRDS_R) * PI_R;
+        or_real s = -gauss_height(r, height) * RL(2.0) * dist * ivd;
         for (int d = 0; d < 3; ++d) out[d] = s * (r[d] / dist);
         return;
     }
     case 2: { /* spiky, kernels.glsl:11-16 */
-        if (dist > h || dist < F32(0.0001f)) return;
-        double s = -45.0 * (h - dist) * (h - dist) / (kPi * pow(h, 6.0));
+        if (dist > h || dist < F32R(0.0001f)) return;
+        or_real s = -RL(45.0) * (h - dist) * (h - dist) / (PI_R * RPOW(h, RL(6.0)));
         for (int d = 0; d < 3; ++d) out[d] = s * (r[d] / dist);
         return;
     }
     case 3: { /* cone, kernels.glsl:54-60 */
-        double st = 3.0 / (kPi * pow(h, 4.0));
-        if (dist > h || dist < F32(0.0001f)) return;
+        or_real st = RL(3.0) / (PI_R * RPOW(h, RL(4.0)));
+        if (dist > h || dist < F32R(0.0001f)) return;
         for (int d = 0; d < 3; ++d) out[d] = -r[d] * (st / dist);
         return;
     }
     case 4: { /* kernels.glsl:72-82 */
-        if (dist > h || dist < F32(0.0001f)) return;
-        double a = 15.0 / (2.0 * kPi * pow(h, 5.0));
-        double m = h - dist;
-        if (m < 0.0) m = 0.0;
-        double s = -2.0 * a * m / dist;
+        if (dist > h || dist < F32R(0.0001f)) return;
+        or_real a = RL(15.0) / (RL(2.0) * PI_R * RPOW(h, RL(5.0)));
+        or_real m = h - dist;
+        if (m < RL(0.0)) m = RL(0.0);
+        or_real s = -RL(2.0) * a * m / dist;
         for (int d = 0; d < 3; ++d) out[d] = s * r[d];
         return;
     }
@@ -579,11 +603,23 @@ void or_kernel_gradient(int id, const double r[3], double h, double out[3]) {
     }
 }
 
+double or_kernel_height(int id, const double r[3], double h) {
+    const or_real rr[3] = {(or_real)r[0], (or_real)r[1], (or_real)r[2]};
+    return (double)kheight(id, rr, (or_real)h);
+}
+
+void or_kernel_gradient(int id, const double r[3], double h, double out[3]) {
+    const or_real rr[3] = {(or_real)r[0], (or_real)r[1], (or_real)r[2]};
+    or_real o[3];
+    kgrad(id, rr, (or_real)h, o);
+    for (int d = 0; d < 3; ++d) out[d] = (double)o[d];
+}
+
 /* ------------------------------------------------------------------ */
-/* incompressibility (incompressibility.cpp:12-45), FP64               */
+/* incompressibility (incompressibility.cpp:12-45), in or_real        */
 /* ------------------------------------------------------------------ */
-static double move_towards_lin(double old_v, double new_v, double step) {  /* incompressibility_2.comp:37-41 */
-    double s = new_v - old_v;
+static or_real move_towards_lin(or_real old_v, or_real new_v, or_real step) {  /* incompressibility_2.comp:37-41 */
+    or_real s = new_v - old_v;
     if (s < -step) s = -step;
     if (s > step) s = step;
     return old_v + s;
@@ -595,105 +631,105 @@ void or_incompressibility_apply(or_fluid *f, const or_neighbors *nb, const or_se
     int32_t *gsum = (int32_t *)calloc(3 * (size_t)(n ? n : 1), sizeof(int32_t));
     uint32_t *sq = (uint32_t *)calloc(n ? n : 1, sizeof(uint32_t));
     int32_t *com = (int32_t *)calloc(4 * (size_t)(n ? n : 1), sizeof(int32_t));
-    double *lambda = (double *)calloc(n ? n : 1, sizeof(double));
-    double *div = (double *)calloc(n ? n : 1, sizeof(double));
+    or_real *lambda = (or_real *)calloc(n ? n : 1, sizeof(or_real));
+    or_real *div = (or_real *)calloc(n ? n : 1, sizeof(or_real));
     int32_t *shift = (int32_t *)calloc(3 * (size_t)(n ? n : 1), sizeof(int32_t));
-    const double R = OR_POS_RESOLUTION;
+    const or_real R = OR_POS_RESOLUTION;
 
     /* incompressibility_0.comp:32-45 */
     for (uint32_t i = 0; i < n; ++i) {
-        double zero[3] = {0, 0, 0};
-        dens[i] = f2u(or_kernel_height(s->height_kernel_id, zero, f->kernel_width[i]) / f->inv_mass[i] * R);
+        or_real zero[3] = {0, 0, 0};
+        dens[i] = f2u(kheight(s->height_kernel_id, zero, f->kernel_width[i]) / f->inv_mass[i] * R);
     }
     /* incompressibility_1.comp:37-69 (gather over row i; integer sums are order-free) */
     for (uint32_t i = 0; i < n; ++i) {
         const int32_t *p = f->pos + 4 * (size_t)i;
-        double kw = f->kernel_width[i];
+        or_real kw = f->kernel_width[i];
         for (uint32_t e = nb->offsets[i]; e < nb->offsets[i + 1]; ++e) {
             uint32_t j = nb->idx[e];
             const int32_t *q = f->pos + 4 * (size_t)j;
-            double imn = f->inv_mass[j];
-            double d[3], g[3];
-            for (int c = 0; c < 3; ++c) d[c] = (double)(int32_t)((uint32_t)q[c] - (uint32_t)p[c]) / R;
-            or_kernel_gradient(s->gradient_kernel_id, d, kw, g);
-            dens[i] += f2u(or_kernel_height(s->height_kernel_id, d, kw) / imn * R);
+            or_real imn = f->inv_mass[j];
+            or_real d[3], g[3];
+            for (int c = 0; c < 3; ++c) d[c] = (or_real)(int32_t)((uint32_t)q[c] - (uint32_t)p[c]) / R;
+            kgrad(s->gradient_kernel_id, d, kw, g);
+            dens[i] += f2u(kheight(s->height_kernel_id, d, kw) / imn * R);
             for (int c = 0; c < 3; ++c) gsum[3 * i + c] = wrap_add(gsum[3 * i + c], f2i(g[c] / imn * R));
             sq[i] += f2u(dot3(g, g) / imn * R);
-            for (int c = 0; c < 3; ++c) div[i] += ((double)f->vel[4 * (size_t)j + c] - f->vel[4 * (size_t)i + c]) * g[c] / imn;
+            for (int c = 0; c < 3; ++c) div[i] += ((or_real)f->vel[4 * (size_t)j + c] - f->vel[4 * (size_t)i + c]) * g[c] / imn;
             if (s->boundariness_calculation_method == 1) {
                 for (int c = 0; c < 3; ++c)
                     com[4 * i + c] = wrap_add(com[4 * i + c],
-                                              f2i((double)(int32_t)((uint32_t)q[c] - (uint32_t)p[c]) / (imn * kw)));
+                                              f2i((or_real)(int32_t)((uint32_t)q[c] - (uint32_t)p[c]) / (imn * kw)));
                 com[4 * i + 3] = wrap_add(com[4 * i + 3], f2i(R / imn));
             }
         }
     }
     /* incompressibility_2.comp:71-110 */
     for (uint32_t i = 0; i < n; ++i) {
-        double radius = f->radius[i], im = f->inv_mass[i], kw = f->kernel_width[i];
-        double ird = pow(2.0 * radius, 3.0) * im;
-        double density = (double)dens[i] / R;
-        double wgs[3] = {(double)gsum[3 * i] / R, (double)gsum[3 * i + 1] / R, (double)gsum[3 * i + 2] / R};
-        double sqs = (double)sq[i] / R;
-        double wgsq = dot3(wgs, wgs);
-        double sgl = sqrt(wgsq) * ird;
+        or_real radius = f->radius[i], im = f->inv_mass[i], kw = f->kernel_width[i];
+        or_real ird = RPOW(RL(2.0) * radius, RL(3.0)) * im;
+        or_real density = (or_real)dens[i] / R;
+        or_real wgs[3] = {(or_real)gsum[3 * i] / R, (or_real)gsum[3 * i + 1] / R, (or_real)gsum[3 * i + 2] / R};
+        or_real sqs = (or_real)sq[i] / R;
+        or_real wgsq = dot3(wgs, wgs);
+        or_real sgl = RSQRT(wgsq) * ird;
         sqs += wgsq * im;
-        double under = 1.0 - density * ird;
+        or_real under = RL(1.0) - density * ird;
         if (s->update_boundariness) {
-            double b;
+            or_real b;
             if (s->boundariness_calculation_method == 1) {
-                double tm = (double)com[4 * i + 3] / R + 1.0 / im;
-                double cv[3] = {(double)com[4 * i], (double)com[4 * i + 1], (double)com[4 * i + 2]};
-                b = len3(cv) / (R * tm) * (double)s->boundariness_self_grad_length_factor;
+                or_real tm = (or_real)com[4 * i + 3] / R + RL(1.0) / im;
+                or_real cv[3] = {(or_real)com[4 * i], (or_real)com[4 * i + 1], (or_real)com[4 * i + 2]};
+                b = len3(cv) / (R * tm) * (or_real)s->boundariness_self_grad_length_factor;
             } else {
-                double up = under > 0.0 ? under : 0.0;
-                b = sgl * kw * (double)s->boundariness_self_grad_length_factor +
-                    up * (double)s->boundariness_underpressure_factor;
+                or_real up = under > RL(0.0) ? under : RL(0.0);
+                b = sgl * kw * (or_real)s->boundariness_self_grad_length_factor +
+                    up * (or_real)s->boundariness_underpressure_factor;
             }
-            b = b >= 1.0 ? 1.0 : 0.0;
-            b = move_towards_lin((double)f->boundariness[i], b, (double)s->boundariness_adaption_speed);
-            f->boundariness[i] = (float)(b < 1.0 ? b : 1.0);
+            b = b >= RL(1.0) ? RL(1.0) : RL(0.0);
+            b = move_towards_lin((or_real)f->boundariness[i], b, (or_real)s->boundariness_adaption_speed);
+            f->boundariness[i] = (float)(b < RL(1.0) ? b : RL(1.0));
         }
-        double lam = under / (ird * ird * (sqs + F32(0.01f)));
-        double rmin2 = 2.0 * (double)s->smallest_target_radius;
+        or_real lam = under / (ird * ird * (sqs + F32R(0.01f)));
+        or_real rmin2 = RL(2.0) * (or_real)s->smallest_target_radius;
         lam /= (rmin2 * rmin2 * rmin2) / ird * im;
         /* the applied lambda: pushes only (incompressibility_2.comp:106) */
-        double applied = lam < 0.0 ? lam : 0.0;
+        or_real applied = lam < RL(0.0) ? lam : RL(0.0);
         if (out && out->lambda_in) {
             if (out->lambda) out->lambda[i] = (float)lam;  /* the computed one, before the override */
-            applied = (double)out->lambda_in[i];
-        } else if (out && out->projected_acc && lam > 0.0) {
-            double a = fmin(lam, -(double)out->projected_acc[i]);
-            applied = a > 0.0 ? a : 0.0;
+            applied = (or_real)out->lambda_in[i];
+        } else if (out && out->projected_acc && lam > RL(0.0)) {
+            or_real a = RFMIN(lam, -(or_real)out->projected_acc[i]);
+            applied = a > RL(0.0) ? a : RL(0.0);
         }
         if (out && out->lambda && !out->lambda_in) out->lambda[i] = (float)lam;
         if (out && out->applied) out->applied[i] = (float)applied;
         lambda[i] = applied;
-        if (applied != 0.0) {
+        if (applied != RL(0.0)) {
             for (int c = 0; c < 3; ++c) shift[3 * i + c] = wrap_add(shift[3 * i + c], f2i(-wgs[c] * ird * (applied * im * R)));
         }
     }
     /* incompressibility_3.comp:48-67 */
     for (uint32_t i = 0; i < n; ++i) {
         const int32_t *p = f->pos + 4 * (size_t)i;
-        double kw = f->kernel_width[i];
-        double gi[3] = {(double)gsum[3 * i], (double)gsum[3 * i + 1], (double)gsum[3 * i + 2]};
-        double gl = len3(gi);
+        or_real kw = f->kernel_width[i];
+        or_real gi[3] = {(or_real)gsum[3 * i], (or_real)gsum[3 * i + 1], (or_real)gsum[3 * i + 2]};
+        or_real gl = len3(gi);
         for (uint32_t e = nb->offsets[i]; e < nb->offsets[i + 1]; ++e) {
             uint32_t j = nb->idx[e];
             const int32_t *q = f->pos + 4 * (size_t)j;
-            double d[3], g[3];
-            for (int c = 0; c < 3; ++c) d[c] = (double)(int32_t)((uint32_t)q[c] - (uint32_t)p[c]) / R;
-            or_kernel_gradient(s->gradient_kernel_id, d, kw, g);
+            or_real d[3], g[3];
+            for (int c = 0; c < 3; ++c) d[c] = (or_real)(int32_t)((uint32_t)q[c] - (uint32_t)p[c]) / R;
+            kgrad(s->gradient_kernel_id, d, kw, g);
             if (s->boundariness_calculation_method == 2) {
-                double l = len3(g);
-                if (gl > 0.0 && l > 0.0) {
-                    double dd = 0.0;
+                or_real l = len3(g);
+                if (gl > RL(0.0) && l > RL(0.0)) {
+                    or_real dd = RL(0.0);
                     for (int c = 0; c < 3; ++c) dd += (-gi[c] / gl) * (g[c] / l);
-                    if (dd > F32(0.6f)) f->boundariness[i] = 0.0f;
+                    if (dd > F32R(0.6f)) f->boundariness[i] = 0.0f;
                 }
             }
-            if (lambda[i] == 0.0) continue;
+            if (lambda[i] == RL(0.0)) continue;
             for (int c = 0; c < 3; ++c) shift[3 * j + c] = wrap_add(shift[3 * j + c], f2i(g[c] * (lambda[i] * R)));
         }
     }

@@ -4,19 +4,26 @@ TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the CPU
 baseline legs of bench.py as the checker / timed CPU restatement.  The product
 (apbf_gb300) never imports this module.
 
+APBF_ORACLE_VARIANT=f32 in the environment (read when the library is first
+loaded) selects libapbf_oracle_f32.so instead: the same code with the kernels and
+the incompressibility passes in FP32, timed as a CPU baseline and checked against
+the FP64 library, never used as the checker.
+
 States are dicts of numpy arrays in the layout of apbf_gb300.scenes.make_state.
 Every function copies its inputs, so callers keep their arrays.
 """
 from __future__ import annotations
 
 import ctypes as C
+import os
 import subprocess
 from pathlib import Path
 
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
-LIB = HERE / "_build" / "libapbf_oracle.so"
+LIB = HERE / "_build" / ("libapbf_oracle_f32.so" if os.environ.get("APBF_ORACLE_VARIANT") == "f32"
+                         else "libapbf_oracle.so")
 
 _u32p = C.POINTER(C.c_uint32)
 _i32p = C.POINTER(C.c_int32)
