@@ -251,7 +251,7 @@ def _replica_loop(conn, name, scale, seed):
     sc = orc.make_scene(orc.settings_from(settings_dict(spec)), spec.grid_min, spec.grid_max, spec.log2res,
                         spec.acceleration)
     boxes = oracle_boxes(spec)
-    conn.send(int(fs.n))
+    conn.send((int(fs.n), orc.LIB.name))
     while True:
         k = conn.recv()
         if k is None:
@@ -266,8 +266,10 @@ def run_reference(args) -> None:
     """The reference arm: the CPU restatement of the reference's shader math (the
     reference has no CPU path of its own and cannot be built here) on every host core,
     as independent replicas of a bounded sample of the scene (1/8 of its particles).
-    Each replica builds its scene once; a step is one substep of every replica, timed
-    from the command to the last answer."""
+    By default the replicas run the oracle's FP32 build (the reference's shaders
+    compute in FP32, and it is the faster CPU form); --oracle-variant f64 runs the
+    FP64 checker.  Each replica builds its scene once; a step is one substep of every
+    replica, timed from the command to the last answer."""
     import multiprocessing as mp
 
     rank = int(os.environ.get("RANK", "0"))
@@ -277,13 +279,23 @@ def run_reference(args) -> None:
     scale = 1.0 / 8.0 if make_spec(args.workload, scale=1.0).n <= 300_000 else 1.0 / 32.0
     ctx = mp.get_context("spawn")
     pipes, procs = [], []
-    for s in range(cores):
-        a, b = ctx.Pipe()
-        p = ctx.Process(target=_replica_loop, args=(b, args.workload, scale, s), daemon=True)
-        p.start()
-        pipes.append(a)
-        procs.append(p)
-    counts = [c.recv() for c in pipes]  # scenes built
+    saved = os.environ.get("APBF_ORACLE_VARIANT")
+    os.environ["APBF_ORACLE_VARIANT"] = args.oracle_variant  # inherited by the spawned replicas
+    try:
+        for s in range(cores):
+            a, b = ctx.Pipe()
+            p = ctx.Process(target=_replica_loop, args=(b, args.workload, scale, s), daemon=True)
+            p.start()
+            pipes.append(a)
+            procs.append(p)
+    finally:
+        if saved is None:
+            os.environ.pop("APBF_ORACLE_VARIANT", None)
+        else:
+            os.environ["APBF_ORACLE_VARIANT"] = saved
+    built = [c.recv() for c in pipes]  # (particles, oracle library) once the scenes are built
+    counts = [b[0] for b in built]
+    libraries = sorted({b[1] for b in built})
 
     def step():
         for c in pipes:
@@ -306,15 +318,17 @@ def run_reference(args) -> None:
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * wall / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded scene generator)",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.oracle_variant == "f32" else "f64",
+        "data": "synthetic (seeded scene generator)",
         "config": {"workload": args.workload, "sample_particles": n_sample, "sample_scale": scale,
-                   "replicas": cores},
+                   "replicas": cores, "oracle_build": args.oracle_variant, "oracle_library": libraries},
         "impl": "reference",
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"{cores} independent replicas of the {n_sample}-particle ({scale:g}-scale) "
                                    f"version of the scene, each built once, one substep of every replica per "
                                    f"step (the reference has no CPU implementation and cannot be built here; the "
-                                   f"oracle restates its shader math in FP64)"},
+                                   f"oracle restates its shader math, here its "
+                                   f"{'FP32 build' if args.oracle_variant == 'f32' else 'FP64 checker'})"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -1053,6 +1067,8 @@ def main() -> None:
     ap.add_argument("--no-plain", action="store_true", help="skip the two plain-solver comparison runs")
     ap.add_argument("--ws-epochs", type=int, default=3)
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--oracle-variant", choices=("f32", "f64"), default="f32",
+                    help="reference arm: the oracle's FP32 build (default) or the FP64 checker")
     ap.add_argument("--search-levels", type=int, default=1,
                     help="finer search grids than the scene's that the search tuner may try")
     ap.add_argument("--graph-mode", type=int, default=2, choices=(0, 1, 2),
