@@ -821,3 +821,30 @@ class SubstepStages:
         self.kw_bd = kernel_width_from_boundary_distance().set_data(self.ctx)
         self.update_transfers = update_transfers().set_data(self.ctx)
         self.particle_transfer = particle_transfer().set_data(self.ctx)
+
+    def update(self, dt: float, stream=None) -> None:
+        """One substep as pool::update runs it (source/pool.cpp:67-106), stage by stage:
+        velocity handling; with adaptivity, particle transfer and the kernel width from the
+        boundary distance (or its spreading after the search); the neighbourhood; then
+        solver_iterations x (box collision, one incompressibility iteration); with
+        adaptivity, update_transfers.  The scene's range, resolution and acceleration come
+        from Context.set_scene.  apbf_substep runs the same stages with the box passes fused
+        into the kernels before them and gives the same state (no emitter, no error
+        target, no warm start)."""
+        s = self.ctx.settings
+        min_pos, max_pos, log2res, acc = self.ctx.scene
+        adaptive = not s.basic_pbf
+        self.velocity.set_acceleration(acc).apply(dt, stream)
+        if adaptive and (s.merge or s.split):
+            self.particle_transfer.apply(dt, stream)
+        if adaptive and s.base_kernel_width_on_boundary_distance:
+            self.kw_bd.apply(stream)
+        scale = 1.0 if (s.basic_pbf or s.base_kernel_width_on_boundary_distance) else 1.5
+        self.neighborhood.set_range_scale(scale).set_position_range(min_pos, max_pos, log2res).apply(stream)
+        if adaptive and not s.base_kernel_width_on_boundary_distance:
+            self.spread.apply(stream)
+        for _ in range(s.solver_iterations):
+            self.boxes.apply(stream)
+            self.incompressibility.apply(stream)
+        if adaptive:
+            self.update_transfers.apply(stream)
