@@ -575,6 +575,21 @@ def oracle_check(ctx, spec) -> dict:
             "what": "mean compression error of one density pass on the final state"}
 
 
+def reduce_over_ranks(total_ms: float, processed: float, dist, device) -> tuple[float, float]:
+    """Whole-job figures of independent replicas: the slowest rank's timed milliseconds
+    and the particle-substeps of all ranks (no collective on the data path; these two
+    numbers are the only exchange).  dist=None: one process, unchanged."""
+    import torch
+
+    if dist is None:
+        return total_ms, processed
+    t = torch.tensor([total_ms], dtype=torch.float64, device=device)
+    p = torch.tensor([processed], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(p, op=dist.ReduceOp.SUM)
+    return float(t[0]), float(p[0])
+
+
 def run_ours(args) -> None:
     import torch
 
@@ -607,12 +622,7 @@ def run_ours(args) -> None:
     total_ms = head["total_ms"]
     n = head["particles_mean"]  # particles per timed substep
     particles_processed = n * args.steps
-    if dist:
-        t = torch.tensor([total_ms, particles_processed], dtype=torch.float64, device=f"cuda:{local}")
-        tmax = t.clone()
-        dist.all_reduce(tmax[:1], op=dist.ReduceOp.MAX)
-        dist.all_reduce(t[1:], op=dist.ReduceOp.SUM)
-        total_ms, particles_processed = float(tmax[0]), float(t[1])
+    total_ms, particles_processed = reduce_over_ranks(total_ms, particles_processed, dist, f"cuda:{local}")
     value = particles_processed / (total_ms / 1000.0)
 
     # roofline of the dominant kernel (largest share of the timed kernel time)
@@ -718,6 +728,11 @@ def run_batch(args) -> None:
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     torch.cuda.set_device(local)
+    dist = None
+    if world > 1:  # replicas: every rank its own table of scenes
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device(f"cuda:{local}"))
     _, kw = WORKLOADS[args.workload]
     specs = batch_specs(kw["scenes"], kw["lo"], kw["hi"], seed=7 + rank)
     dt = 1.0 / 240.0  # one time step for the whole batch
@@ -804,6 +819,8 @@ def run_batch(args) -> None:
     clocks.start()
     time.sleep(0.3)
     l0 = sum(c.launch_count() for c in ctxs)
+    if dist:
+        dist.barrier()
     torch.cuda.synchronize()
     for k in range(args.steps):
         flush.zero_()
@@ -818,7 +835,10 @@ def run_batch(args) -> None:
     errs = [float(c.reduce_fp64()[2]) for c in ctxs]
     passes = sum(i.density_passes for i in infos) / (len(ctxs) * args.steps)
     conv = sum(i.converged_substeps for i in infos)
-    value = n_total * args.steps / (total_ms / 1000.0)
+    if dist:
+        dist.barrier()
+    total_ms, processed = reduce_over_ranks(total_ms, float(n_total * args.steps), dist, f"cuda:{local}")
+    value = processed / (total_ms / 1000.0)
 
     # the same scenes one after the other (each a whole-substep graph), the same
     # window replayed from its start state
@@ -895,6 +915,8 @@ def run_batch(args) -> None:
             "cpu_baseline": None,
         }
         print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
 
 
 def run_batch_e2e(batch, ctxs, args, dt, windows) -> dict:
