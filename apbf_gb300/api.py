@@ -848,3 +848,59 @@ class SubstepStages:
             self.incompressibility.apply(stream)
         if adaptive:
             self.update_transfers.apply(stream)
+
+
+# ---- save_particle_info files read back (host only) ----
+PARTICLE_INFO_LISTS = ("centerDist", "radius", "neighborCount", "kernelWidth", "targetRadius", "boundaryDistance")
+PARTICLE_INFO_COLUMNS = ("center distance", "boundary distance", "kernel width", "neighbor count", "radius",
+                         "target radius", "inverse mass", "x", "y", "z")
+
+
+def load_particle_info(folder) -> dict:
+    """Reads the files of save_particle_info (source/save_particle_info.cpp:22-125, as
+    Context.save_particle_info writes them): every ';'-separated list present, as
+    float64 arrays in particle order (neighborCount as int64), and data.csv's columns
+    (rows sorted by the distance to the centre) under "data"."""
+    from pathlib import Path
+
+    d = Path(folder)
+    out: dict = {}
+    for name in PARTICLE_INFO_LISTS:
+        p = d / f"{name}.txt"
+        if p.exists():
+            vals = [x for x in p.read_text().split(";") if x.strip()]
+            out[name] = np.array(vals, dtype=np.int64 if name == "neighborCount" else np.float64)
+    p = d / "data.csv"
+    if p.exists():
+        lines = p.read_text().strip().splitlines()
+        head = tuple(h.strip() for h in lines[0].split(","))
+        if head != PARTICLE_INFO_COLUMNS:
+            raise ValueError(f"{p}: unexpected columns {head}")
+        rows = np.array([[float(x) for x in ln.split(",")] for ln in lines[1:]], np.float64).reshape(-1, len(head))
+        out["data"] = {h: rows[:, k] for k, h in enumerate(head)}
+    return out
+
+
+def state_from_particle_info(folder) -> dict:
+    """A particle state for Context.upload from a save_particle_info data.csv (in its row
+    order): positions, radii, target radii, inverse masses, kernel widths and boundary
+    distances as written (six significant digits), velocities zero, the backup
+    position equal to the position, no transfers, boundariness zero."""
+    cols = load_particle_info(folder)["data"]
+    n = cols["x"].shape[0]
+    pos = np.zeros((n, 4), np.int32)
+    for k, a in enumerate(("x", "y", "z")):
+        pos[:, k] = np.rint(cols[a] * 262144.0).astype(np.int32)
+    f32 = lambda a: np.ascontiguousarray(cols[a], dtype=np.float32)  # noqa: E731
+    return {
+        "position": pos,
+        "velocity": np.zeros((n, 4), np.float32),
+        "inverse_mass": f32("inverse mass"),
+        "radius": f32("radius"),
+        "pos_backup": pos.copy(),
+        "transferring": np.zeros(n, np.uint32),
+        "target_radius": f32("target radius"),
+        "kernel_width": f32("kernel width"),
+        "boundariness": np.zeros(n, np.float32),
+        "boundary_distance": np.rint(cols["boundary distance"] * 262144.0).astype(np.uint32),
+    }
