@@ -45,7 +45,7 @@ WORKLOADS = {
     # 64 independent scenes, log-uniform 4k-200k particles, one graph launch per substep
     "batch64": ("batch", dict(scenes=64, lo=4_000, hi=200_000)),
 }
-DEFAULT_WORKLOAD = "water_drop_250k_plain"
+DEFAULT_WORKLOAD = "waterfall_1m"
 
 
 def make_spec(name: str, seed: int = 0, scale: float = 1.0):
@@ -67,13 +67,15 @@ def make_spec(name: str, seed: int = 0, scale: float = 1.0):
 
 
 def settings_dict(spec) -> dict:
-    from apbf_gb300.api import default_settings
+    """The oracle's settings for a workload: the reference's defaults (restated in the
+    oracle, so this loads nothing of the product), iterated to the error target."""
+    from oracle.oracle import DEFAULT_SETTINGS
 
-    s = default_settings()
-    s.basic_pbf = 1 if spec.basic_pbf else 0
-    s.solver_iterations = 100
-    s.density_error_target = 0.001
-    return {f: getattr(s, f) for f, _ in s._fields_ if not f.startswith("pad")}
+    s = dict(DEFAULT_SETTINGS)
+    s["basic_pbf"] = 1 if spec.basic_pbf else 0
+    s["solver_iterations"] = 100
+    s["density_error_target"] = 0.001
+    return s
 
 
 # ----------------------------------------------------------------------------- clocks
@@ -141,6 +143,19 @@ def algorithmic_bytes(kernel: str, n: int, pairs: int) -> float | None:
     if kernel == "k_build_rows":
         return 16.0 * n + 4.0 * n + 4.0 * pairs  # pos + range in, counts + rows out
     return None
+
+
+def _l2_resident(n: float, pairs: int) -> bool:
+    """Whether one Jacobi pass's working set (per particle: position and packed record,
+    solve record, self shift, widths; rows at 4 bytes per pair) fits the GPU's L2, in
+    which case an HBM roofline fraction says little about the kernel."""
+    try:
+        import torch
+
+        l2 = torch.cuda.get_device_properties(torch.cuda.current_device()).L2_cache_size
+    except (RuntimeError, AttributeError, AssertionError):
+        l2 = 126 * 1024 * 1024
+    return bool(80.0 * n + 8.0 * pairs < l2)
 
 
 def measured_peak() -> tuple[float, str]:
@@ -240,24 +255,43 @@ def cpu_baseline(workload: str, budget_s: float = 15.0) -> dict:
             "fp32": fp32}
 
 
-def _replica_loop(conn, name, scale, seed):
-    """One replica of the reference arm: builds its scene once, then advances it by the
-    requested number of substeps per command and answers with its particle count."""
+def _replica_loop(conn, name, scale, seed, presteps):
+    """One replica of the reference arm: builds its scene, brings it to the phase the
+    GPU arm times (the scene's untimed substeps, with the scene's fixed iteration
+    count, the reference's own way of running: settings.cpp:31, pool.cpp:91-95), then
+    advances it by the requested number of substeps per command (iterating to the
+    error target like the timed GPU arms) and answers with its particle count.  An
+    emitter adds particles every substep, as on the GPU."""
     sys.path.insert(0, str(ROOT))
     from oracle import oracle as orc
 
     spec = make_spec(name, seed=seed, scale=scale)
-    fs = orc.FluidState(spec.state)
+    cap = max(spec.n, int(spec.meta.get("capacity", 0) * scale)) + 4096
+    fs = orc.FluidState(spec.state, cap=cap)
     sc = orc.make_scene(orc.settings_from(settings_dict(spec)), spec.grid_min, spec.grid_max, spec.log2res,
                         spec.acceleration)
     boxes = oracle_boxes(spec)
+    em = spec.meta.get("emitter")
+    est = np.zeros(2, np.float64)
+
+    def advance():
+        if em:
+            orc.emit(fs, SimpleNamespace(**em, max_particles=0, enabled=1), est, np.float32(spec.dt),
+                     np.float32(sc.last_dt))
+        orc.substep(fs, sc, boxes, np.float32(spec.dt), int(cap * 64))
+
+    target, iters = sc.settings.density_error_target, sc.settings.solver_iterations
+    sc.settings.density_error_target, sc.settings.solver_iterations = 0.0, spec.iterations
+    for _ in range(presteps):
+        advance()
+    sc.settings.density_error_target, sc.settings.solver_iterations = target, iters
     conn.send((int(fs.n), orc.LIB.name))
     while True:
         k = conn.recv()
         if k is None:
             break
         for _ in range(k):
-            orc.substep(fs, sc, boxes, np.float32(spec.dt), int(spec.n * 64))
+            advance()
         conn.send(int(fs.n))
     conn.close()
 
@@ -276,7 +310,11 @@ def run_reference(args) -> None:
     if rank != 0:
         return
     cores = os.cpu_count() or 1
-    scale = 1.0 / 8.0 if make_spec(args.workload, scale=1.0).n <= 300_000 else 1.0 / 32.0
+    full = make_spec(args.workload, scale=1.0)
+    # a sample whose timed substep takes a few seconds per core: 1/8 of the water drops,
+    # 1/256 of the waterfall (whose reference rule runs its 100-pass cap every substep)
+    scale = 1.0 / 8.0 if full.n <= 300_000 else 1.0 / 256.0
+    presteps = args.presteps if args.presteps >= 0 else full.meta.get("presteps", 0)
     ctx = mp.get_context("spawn")
     pipes, procs = [], []
     saved = os.environ.get("APBF_ORACLE_VARIANT")
@@ -284,7 +322,7 @@ def run_reference(args) -> None:
     try:
         for s in range(cores):
             a, b = ctx.Pipe()
-            p = ctx.Process(target=_replica_loop, args=(b, args.workload, scale, s), daemon=True)
+            p = ctx.Process(target=_replica_loop, args=(b, args.workload, scale, s, presteps), daemon=True)
             p.start()
             pipes.append(a)
             procs.append(p)
@@ -321,12 +359,16 @@ def run_reference(args) -> None:
         "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.oracle_variant == "f32" else "f64",
         "data": "synthetic (seeded scene generator)",
         "config": {"workload": args.workload, "sample_particles": n_sample, "sample_scale": scale,
-                   "replicas": cores, "oracle_build": args.oracle_variant, "oracle_library": libraries},
+                   "replicas": cores, "presteps": presteps, "oracle_build": args.oracle_variant,
+                   "oracle_library": libraries,
+                   "iterations": "until mean density error <= 0.001 (max 100), reference Jacobi rule"},
         "impl": "reference",
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{cores} independent replicas of the {n_sample}-particle ({scale:g}-scale) "
-                                   f"version of the scene, each built once, one substep of every replica per "
-                                   f"step (the reference has no CPU implementation and cannot be built here; the "
+                         "sample": f"{cores} independent replicas of the {scale:g}-scale version of the scene "
+                                   f"({n_sample} particles at the start of the timed steps), each built once and "
+                                   f"brought through the GPU arm's {presteps} untimed substeps, one substep of every "
+                                   f"replica per step (the reference has no CPU implementation and cannot be built "
+                                   f"here; the "
                                    f"oracle restates its shader math, here its "
                                    f"{'FP32 build' if args.oracle_variant == 'f32' else 'FP64 checker'})"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -552,27 +594,56 @@ def run_arm(spec, args, local, mode: int, net, dist, headline: bool) -> tuple[di
     return r, ctx
 
 
+def _device_pairs(ctx, n: int) -> np.ndarray:
+    """The device's neighbour rows as sorted (i << 32 | j) keys, one per directed pair."""
+    nb = ctx.neighbors_view()
+    cnt = nb["count"][:n].cpu().numpy().view(np.uint32).astype(np.int64)
+    m = int(cnt.max()) if n else 0
+    idx = nb["index"][:m, :n].cpu().numpy().view(np.uint32).astype(np.int64)
+    live = np.arange(m)[:, None] < cnt[None, :]
+    ii = np.broadcast_to(np.arange(n, dtype=np.int64)[None, :], (m, n))[live]
+    return np.sort((ii << 32) | idx[live])
+
+
 def oracle_check(ctx, spec) -> dict:
-    """The reported density error against the FP64 oracle: on the final state, the
-    device's neighbour search and one density pass (its mean compression error, FP32
-    sums) next to the oracle's FP64 neighbour search and density error of the same
-    downloaded state."""
+    """Parity of the final state of the timed run against the FP64 oracle: the state is
+    downloaded and searched by the device and by the oracle with the substep's own
+    range scale (1 for basic PBF or kernel widths from the boundary distance, else 1.5:
+    source/pool.cpp:83) on the scene grid.  Reported: Morton keys and sort permutation
+    bit for bit, neighbour sets (every directed pair) bit for bit, and the mean
+    compression error of one density pass over those rows, FP32 on the device against
+    FP64 in the oracle."""
     from apbf_gb300.api import incompressibility, neighborhood_green
     from oracle import oracle as orc
 
-    scale = 1.0 if spec.basic_pbf else 1.5
+    s = ctx.settings
+    scale = 1.0 if (s.basic_pbf or s.base_kernel_width_on_boundary_distance) else 1.5
     st, _ = ctx.download()
+    n = int(st["position"].shape[0])
     t0 = time.perf_counter()
     neighborhood_green().set_data(ctx).set_range_scale(scale).set_position_range(
         spec.grid_min, spec.grid_max, spec.log2res).apply()
+    perm_d, keys_d = ctx.debug_sort()
+    pairs_d = _device_pairs(ctx, n)
     incompressibility().set_data(ctx).apply()
     e_dev = float(ctx.reduce_fp64()[2])
+    t1 = time.perf_counter()
     fs = orc.FluidState(st)
-    orc.neighborhood_green(fs, scale, spec.grid_min, spec.grid_max, spec.log2res, int(st["position"].shape[0] * 160))
-    e_or = float(orc.density_error(fs, orc.settings_from(ctx.settings))[0])
-    return {"particles": int(st["position"].shape[0]), "device_fp32": e_dev, "oracle_fp64": e_or,
-            "abs_diff": abs(e_dev - e_or), "seconds": round(time.perf_counter() - t0, 2),
-            "what": "mean compression error of one density pass on the final state"}
+    perm_o, keys_o, tot = orc.neighborhood_green(fs, scale, spec.grid_min, spec.grid_max, spec.log2res,
+                                                 max(n * 160, 1024))
+    off = fs.nb_off[:n + 1].astype(np.int64)
+    pairs_o = (np.repeat(np.arange(n, dtype=np.int64), np.diff(off)) << 32) | fs.nb_idx[:tot].astype(np.int64)
+    e_or = float(orc.density_error(fs, orc.settings_from(s))[0])
+    same_sets = pairs_d.shape == pairs_o.shape and bool(np.array_equal(pairs_d, np.sort(pairs_o)))
+    return {"particles": n, "range_scale": scale, "grid_log2res": spec.log2res,
+            "morton_keys_bit_exact": bool(np.array_equal(keys_d, keys_o)),
+            "sort_permutation_bit_exact": bool(np.array_equal(perm_d, perm_o)),
+            "neighbor_sets_equal": same_sets, "pairs_device": int(pairs_d.size), "pairs_oracle": int(tot),
+            "density_error_device_fp32": e_dev, "density_error_oracle_fp64": e_or, "abs_diff": abs(e_dev - e_or),
+            "device_s": round(t1 - t0, 2), "oracle_s": round(time.perf_counter() - t1, 2),
+            "what": "the final state searched again by both (keys, permutation, every directed pair) and one density "
+                    "pass over those new rows (mean compression error; rows rebuilt after the solve's last pass, so "
+                    "this is not the solve's own error, which config.density_error_last_pass reports)"}
 
 
 def reduce_over_ranks(total_ms: float, processed: float, dist, device) -> tuple[float, float]:
@@ -606,10 +677,12 @@ def run_ours(args) -> None:
 
     spec = make_spec(args.workload, seed=rank)
     n = spec.n
-    wants_learned = not args.no_warm_start
+    wants_learned = not args.no_warm_start and args.solve == "learned"
     net, train_info = train_warm_start(args, local, rank) if wants_learned else (None, None)
     learned = net is not None  # no admissible warm start: the reference rule is the headline
     head_mode = (N.WARM_LEARNED | N.WARM_PROJECTED) if learned else 0
+    if args.solve == "projected":
+        head_mode = N.WARM_PROJECTED
 
     # the plain forms first (same scene, same seed), then the headline form
     plain = {}
@@ -657,8 +730,20 @@ def run_ours(args) -> None:
 
     if rank == 0:
         solver = ("learned warm start (BF16 MLP first update) + projected Jacobi passes" if learned
+                  else "projected Jacobi rule (no network)" if args.solve == "projected"
                   else "reference Jacobi rule" + (" (no warm start within the kinetic-energy bound)"
                                                   if wants_learned else ""))
+        # the plain forms of the same scene, seed and timed window, for the learned-vs-plain comparison
+        vs_plain = {k: {"value": v["value"], "ms_per_step": round(v["ms_per_step"], 4),
+                        "density_passes_per_substep": v["density_passes_per_substep"],
+                        "converged_substeps": v["converged_substeps"],
+                        "headline_over_this": round(value / v["value"], 3) if v["value"] else None}
+                    for k, v in plain.items()} if plain else None
+        parity = None
+        if check:
+            parity = {k: check[k] for k in ("morton_keys_bit_exact", "sort_permutation_bit_exact",
+                                             "neighbor_sets_equal", "density_error_device_fp32",
+                                             "density_error_oracle_fp64")}
         fidelity = None
         if plain and head.get("state_after"):
             e = head["state_after"]["mean_v2"]
@@ -682,6 +767,9 @@ def run_ours(args) -> None:
                        "dt": spec.dt, "adaptive": not spec.basic_pbf, "pairs": head["pairs"],
                        "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas x{world}",
                        "graph_mode": args.graph_mode, "persistent_solve": bool(args.persistent),
+                       "density_error_last_pass": head["state_after"]["last_density_error"],
+                       "vs_plain": vs_plain, "parity_vs_fp64_oracle": parity,
+                       "l2_resident": _l2_resident(n, head["pairs"]),
                        "tuning": head["tuning"]},
             "state_after": head["state_after"], "fidelity": fidelity,
             "plain": plain or None,
@@ -1087,6 +1175,8 @@ def main() -> None:
     ap.add_argument("--no-oracle-check", action="store_true", help="skip the FP64 oracle check of the final state")
     ap.add_argument("--no-warm-start", action="store_true", help="headline = the reference Jacobi rule")
     ap.add_argument("--no-plain", action="store_true", help="skip the two plain-solver comparison runs")
+    ap.add_argument("--solve", choices=("learned", "reference", "projected"), default="learned",
+                    help="headline solve: the learned warm start (default), or one plain rule without a network")
     ap.add_argument("--ws-epochs", type=int, default=3)
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--oracle-variant", choices=("f32", "f64"), default="f32",

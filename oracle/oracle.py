@@ -153,6 +153,19 @@ def _p(a: np.ndarray, t):
     return a.ctypes.data_as(t)
 
 
+# pbd::settings defaults (source/settings.cpp:5-31), restated for the oracle so that
+# callers that time or check the oracle need not load the product library.
+DEFAULT_SETTINGS = {
+    "height_kernel_id": 1, "gradient_kernel_id": 1, "merge": 1, "split": 1,
+    "base_kernel_width_on_target_radius": 1, "base_kernel_width_on_boundary_distance": 1,
+    "update_target_radius": 1, "update_boundariness": 1, "boundariness_calculation_method": 2, "basic_pbf": 0,
+    "solver_iterations": 3, "boundariness_adaption_speed": 0.5, "kernel_width_adaption_speed": 0.01,
+    "boundariness_self_grad_length_factor": 2.0, "boundariness_underpressure_factor": 4.0, "merge_duration": 2.0,
+    "split_duration": 0.0, "smallest_target_radius": 1.0, "target_radius_offset": 10.0,
+    "target_radius_scale_factor": 0.3, "density_error_target": 0.0,
+}
+
+
 def settings_from(src) -> OrSettings:
     """Copies a settings struct with the same field names (apbf_gb300 Settings or dict)."""
     s = OrSettings()

@@ -49,6 +49,21 @@ def test_abi_version_and_defaults(native_lib):
     assert abs(s.target_radius_scale_factor - 0.3) < 1e-7 and s.merge_duration == 2.0
 
 
+def test_oracle_default_settings_match_library(native_lib):
+    """The oracle's restated defaults (used by the bench's CPU legs, which must not load
+    the product library) equal apbf_default_settings field for field."""
+    import ctypes as C
+
+    from apbf_gb300 import _native
+    from oracle import oracle as o
+
+    s = _native.Settings()
+    native_lib.apbf_default_settings(C.byref(s))
+    for f, _ in _native.Settings._fields_:
+        if not f.startswith("pad"):
+            assert abs(float(getattr(s, f)) - float(o.DEFAULT_SETTINGS[f])) < 1e-7, f
+
+
 def test_struct_sizes_match_oracle():
     import ctypes as C
 
