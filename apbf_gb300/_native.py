@@ -152,7 +152,7 @@ class Emitter(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("gather_lanes", C.c_uint32), ("pass_block", C.c_uint32), ("pass_blocks_per_sm", C.c_uint32),
-                ("build_tiled", C.c_uint32), ("filter_in_density", C.c_uint32), ("sort_digit_bits", C.c_uint32),
+                ("reserved0", C.c_uint32), ("filter_in_density", C.c_uint32), ("sort_digit_bits", C.c_uint32),
                 ("search_log2res", C.c_uint32), ("reserved", C.c_uint32)]
 
 
@@ -180,6 +180,7 @@ SIGNATURES = {
     "apbf_fluid_get_view": (_ST, [_P, C.POINTER(FluidView)]),
     "apbf_transfers_get_view": (_ST, [_P, C.POINTER(TransfersView)]),
     "apbf_neighbors_get_view": (_ST, [_P, C.POINTER(NeighborsView)]),
+    "apbf_neighbors_get_reverse_view": (_ST, [_P, C.POINTER(NeighborsView), C.POINTER(C.c_uint32), _P]),
     "apbf_set_lengths": (_ST, [_P, C.c_uint32, C.c_uint32, _P]),
     "apbf_get_lengths": (_ST, [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), _P]),
     "apbf_velocity_handling_apply": (_ST, [_P, C.c_float, _F3, _P]),

@@ -175,7 +175,7 @@ class Context:
         t = N.Tuning()
         N.check(self.lib.apbf_get_tuning(self.handle, C.byref(t)), "apbf_get_tuning")
         return {"gather_lanes": t.gather_lanes, "pass_block": t.pass_block,
-                "pass_blocks_per_sm": t.pass_blocks_per_sm, "build_tiled": t.build_tiled,
+                "pass_blocks_per_sm": t.pass_blocks_per_sm,
                 "filter_in_density": t.filter_in_density, "sort_digit_bits": t.sort_digit_bits,
                 "search_log2res": t.search_log2res}
 
@@ -203,7 +203,7 @@ class Context:
         return out[:, :n].t().contiguous()
 
     def set_tuning(self, gather_lanes: int | None = None, pass_block: int | None = None,
-                   pass_blocks_per_sm: int | None = None, build_tiled: int | None = None,
+                   pass_blocks_per_sm: int | None = None,
                    filter_in_density: int | None = None, sort_digit_bits: int | None = None,
                    search_log2res: int | None = None) -> None:
         t = N.Tuning()
@@ -214,8 +214,6 @@ class Context:
             t.pass_block = pass_block
         if pass_blocks_per_sm is not None:
             t.pass_blocks_per_sm = pass_blocks_per_sm
-        if build_tiled is not None:
-            t.build_tiled = build_tiled
         if filter_in_density is not None:
             t.filter_in_density = filter_in_density
         if sort_digit_bits is not None:
@@ -232,7 +230,7 @@ class Context:
         N.check(self.lib.apbf_autotune(self.handle, _stream_handle(stream), C.byref(t), ms), "apbf_autotune")
         keys = [f"L{l}/B{b}/S{p}" for l in (1, 2, 4, 8) for b in (128, 256) for p in (2, 4, 8)]
         return {"gather_lanes": t.gather_lanes, "pass_block": t.pass_block,
-                "pass_blocks_per_sm": t.pass_blocks_per_sm, "build_tiled": t.build_tiled,
+                "pass_blocks_per_sm": t.pass_blocks_per_sm,
                 "filter_in_density": t.filter_in_density, "sort_digit_bits": t.sort_digit_bits,
                 "search_log2res": t.search_log2res,
                 "pass_ms": {k: round(float(v), 5) for k, v in zip(keys, ms)}}
@@ -286,6 +284,19 @@ class Context:
             "count": device_tensor(v.count, (self.capacity,), torch.int32, self.device),
             "index": device_tensor(v.index, (v.max_per_row, v.row_stride), torch.int32, self.device),
             "row_stride": v.row_stride,
+        }
+
+    def reverse_neighbors_view(self, stream=None) -> dict:
+        """The rows the position update gathers over (apbf_neighbors_get_reverse_view):
+        kind 2 symmetric (the forward rows serve), 1 union rows, 0 transposed rows."""
+        v = N.NeighborsView()
+        kind = C.c_uint32()
+        N.check(self.lib.apbf_neighbors_get_reverse_view(self.handle, C.byref(v), C.byref(kind),
+                                                         _stream_handle(stream)), "apbf_neighbors_get_reverse_view")
+        return {
+            "count": device_tensor(v.count, (self.capacity,), torch.int32, self.device),
+            "index": device_tensor(v.index, (v.max_per_row, v.row_stride), torch.int32, self.device),
+            "row_stride": v.row_stride, "kind": int(kind.value),
         }
 
     def set_lengths(self, n_particles: int, n_transfers: int = 0, stream=None) -> None:

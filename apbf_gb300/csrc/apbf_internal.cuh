@@ -27,6 +27,10 @@
 namespace apbf {
 
 constexpr int kBlock = 256;
+// Correction-row entry flag (neighborhood.cu): the entry is in the row owner's own
+// neighbour row but the entry's radius does not reach the owner, so the position
+// update subtracts its term again; the entry's index is the low 31 bits.
+constexpr uint32_t kNoDelta = 0x80000000u;
 constexpr uint32_t kSpinLimit = 1u << 22;  // bounded device-side waits
 
 struct FluidBufs {
@@ -66,10 +70,10 @@ struct Status {
     uint32_t pass_index;           // solve loop graph: index of the first pass of the current body run
     uint32_t loop_iters;           // solve loop graph: body runs since the context was created
     uint32_t filter_tag;           // 1: this pass's density kernel left the boundariness filter to k_delta
+    uint32_t union_rows;           // 1: the reverse-row arrays hold correction rows (see neighborhood.cu)
     uint32_t kw_uniform;           // 1: every kernel width of this density pass had the same bits
     uint32_t bar_arrive;           // persistent solve: blocks arrived at the current grid barrier
     uint32_t bar_gen;              // persistent solve: grid barriers released so far
-    uint32_t pad3;
     unsigned long long loop_e1;    // persistent solve: error sums of the current pass (2^-24 fixed point)
     unsigned long long loop_e2;
 };
@@ -177,6 +181,7 @@ struct apbf_ctx {
     uint32_t *cell_start = nullptr;
     uint32_t *cell_end = nullptr;
     ulonglong2 *pos_code = nullptr;        // per particle: 96-bit position code {bits 0-63, bits 64-95}
+    int4 *srec = nullptr;                  // per particle: search record (position xyz, fixed-point radius)
     int search_method = APBF_NEIGHBORHOOD_GREEN;  // the substep's neighbour search
 
     float *lambda = nullptr;
@@ -327,7 +332,8 @@ inline int32_t f2i_host(float x) {
 
 // ---- host-side stage launchers (defined in the .cu files) ----
 apbf_status emit(apbf_ctx *ctx, float dt, cudaStream_t s);  // glue.cu
-apbf_status reorder_particles(apbf_ctx *ctx, cudaStream_t s);  // neighborhood.cu: gather by ctx->perm
+// neighborhood.cu: gather by ctx->perm; with `search` also the search records for range scale `scale`
+apbf_status reorder_particles(apbf_ctx *ctx, cudaStream_t s, bool search = false, float scale = 0.0f);
 apbf_status glue_remap(apbf_ctx *ctx, cudaStream_t s);      // constraints.cu: glue ids follow a reorder
 apbf_status sort_pairs_device(apbf_ctx *ctx, const uint32_t *keys_in, const uint32_t *vals_in, const uint32_t *d_count,
                               uint32_t max_count, uint32_t key_bits, uint32_t *keys_out, uint32_t *vals_out,

@@ -267,6 +267,7 @@ apbf_status apbf_create(const apbf_config *cfg, apbf_ctx **out) {
     A(ctx->cell_start, ncells);
     A(ctx->cell_end, ncells);
     A(ctx->pos_code, cap);
+    A(ctx->srec, cap);
     ctx->n_cells_log2_alloc = cfg->max_log2res;
     A(ctx->lambda, cap);
     A(ctx->shift, cap);
@@ -480,6 +481,24 @@ apbf_status apbf_neighbors_get_view(apbf_ctx *ctx, apbf_neighbors_view *o) {
     o->count = ctx->nb_count;
     o->index = ctx->nb_idx;
     o->d_total = ctx->d_pairs;
+    return APBF_OK;
+}
+
+apbf_status apbf_neighbors_get_reverse_view(apbf_ctx *ctx, apbf_neighbors_view *o, uint32_t *union_rows,
+                                            void *stream) {
+    if (!ctx || !o) return APBF_ERR_INVALID_ARG;
+    o->row_stride = ctx->row_stride;
+    o->max_per_row = ctx->cfg.max_neighbors;
+    o->count = ctx->rev_count;
+    o->index = ctx->rev_idx;
+    o->d_total = ctx->d_pairs;
+    if (union_rows) {
+        Status hs;
+        cudaStream_t s = (cudaStream_t)stream;
+        APBF_CUDA(cudaMemcpyAsync(&hs, ctx->status, sizeof(Status), cudaMemcpyDeviceToHost, s));
+        APBF_CUDA(cudaStreamSynchronize(s));
+        *union_rows = hs.range_min == hs.range_max ? 2u : hs.union_rows;
+    }
     return APBF_OK;
 }
 

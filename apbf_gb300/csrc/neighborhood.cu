@@ -10,8 +10,11 @@
 //  5. k_build_rows: per particle, walk the cells overlapping [X - R, X + R] and keep
 //     every other particle within R (neighborhood_green.comp:49-87), written
 //     column-major so that consecutive particles' k-th entries are contiguous.
-//  6. k_reverse_rows (only when search radii differ): transpose the rows, so the
-//     position-update pass can gather instead of scattering with atomics.
+//     When the search radii differ it also writes correction rows into the
+//     reverse-row arrays (the rare one-sided pairs), so that the position-update
+//     pass gathers over the particle's own row plus its corrections instead of
+//     scattering with atomics, and no transpose is needed.
+//  6. k_reverse_rows (binary-search rows and pruned rows): the transpose.
 #include <algorithm>
 
 #include "apbf_internal.cuh"
@@ -48,9 +51,15 @@ __global__ void k_position_keys(const int4 *__restrict__ pos, const uint32_t *d_
 }
 
 // Gather of every attribute by the sort permutation (copy_scattered_read.comp).
+// With srec non-null it also writes each particle's search record (position xyz,
+// fixed-point search radius R = range_fixed(kw, scale) in w, -1 for a NaN or
+// negative width) and reduces the radii's range into the status block, so that the
+// row build knows before it starts whether every radius is equal.
 __global__ void k_reorder(FluidBufs src, FluidBufs dst, const uint32_t *__restrict__ perm,
-                          uint32_t *__restrict__ inv_perm, const uint32_t *d_len) {
+                          uint32_t *__restrict__ inv_perm, const uint32_t *d_len, int4 *__restrict__ srec,
+                          float scale, Status *st) {
     uint32_t n = d_len[kLenParticles];
+    long long rmin = 0x7fffffffffffffffll, rmax = -1;
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         uint32_t o = perm[k];
         int4 p = src.pos[o];
@@ -67,6 +76,25 @@ __global__ void k_reorder(FluidBufs src, FluidBufs dst, const uint32_t *__restri
         dst.lambda_prev[k] = src.lambda_prev[o];
         dst.boundary_distance[k] = src.boundary_distance[o];
         inv_perm[o] = k;
+        if (srec) {
+            const long long R = range_fixed(src.kernel_width[o], scale);
+            srec[k] = make_int4(p.x, p.y, p.z, (int)R);
+            if (R >= 0) {
+                rmin = R < rmin ? R : rmin;
+                rmax = R > rmax ? R : rmax;
+            }
+        }
+    }
+    if (!srec) return;  // uniform over the grid
+    for (int off = 16; off > 0; off >>= 1) {
+        const long long a2 = __shfl_down_sync(0xffffffffu, rmin, off);
+        const long long c2 = __shfl_down_sync(0xffffffffu, rmax, off);
+        rmin = a2 < rmin ? a2 : rmin;
+        rmax = c2 > rmax ? c2 : rmax;
+    }
+    if ((threadIdx.x & 31) == 0 && rmax >= 0) {
+        atomicMin(&st->range_min, (unsigned long long)rmin);
+        atomicMax(&st->range_max, (unsigned long long)rmax);
     }
 }
 
@@ -107,53 +135,6 @@ __device__ __forceinline__ bool within32(int4 a, int4 b, uint32_t R, unsigned lo
     return s <= R2;
 }
 
-// Walks the cells [x0, x1] x [y0, y1] x [z0, z1] and appends every neighbour of
-// particle i.  The walk is a chain of dependent loads (cell range -> candidates),
-// so the ranges of up to four cells of one (z, y) row are loaded together and
-// candidates four at a time.
-template <bool FAST>
-__device__ __forceinline__ uint32_t walk_cells(uint32_t i, int4 p, long long R, uint32_t x0, uint32_t x1, uint32_t y0,
-                                               uint32_t y1, uint32_t z0, uint32_t z1,
-                                               const int4 *__restrict__ pos, const uint32_t *__restrict__ cstart,
-                                               const uint32_t *__restrict__ cend, uint32_t stride, uint32_t maxn,
-                                               uint32_t *__restrict__ idx) {
-    const uint32_t R32 = (uint32_t)R;
-    const unsigned long long R2 = (unsigned long long)R32 * R32;
-    uint32_t c = 0;
-    for (uint32_t cz = z0; cz <= z1; ++cz)
-        for (uint32_t cy = y0; cy <= y1; ++cy) {
-            const uint32_t yz = (spread3(cy) << 1) | (spread3(cz) << 2);
-            for (uint32_t cx0 = x0; cx0 <= x1; cx0 += 4) {
-                uint32_t cs[4], ce[4];
-#pragma unroll
-                for (int v = 0; v < 4; ++v) {
-                    const bool in = cx0 + v <= x1;
-                    const uint32_t key = yz | spread3(cx0 + v);
-                    cs[v] = in ? cstart[key] : 0u;
-                    ce[v] = in ? cend[key] : 0u;
-                }
-#pragma unroll
-                for (int v = 0; v < 4; ++v) {
-                    const uint32_t s = cs[v], e = ce[v];
-                    for (uint32_t j0 = s; j0 < e; j0 += 4) {
-                        int4 q[4];
-#pragma unroll
-                        for (int u = 0; u < 4; ++u) q[u] = j0 + u < e ? pos[j0 + u] : p;
-#pragma unroll
-                        for (int u = 0; u < 4; ++u) {
-                            const uint32_t j = j0 + u;
-                            if (j >= e || j == i) continue;
-                            if (FAST ? !within32(p, q[u], R32, R2) : !within(p, q[u], R)) continue;
-                            if (c < maxn) idx[(size_t)c * stride + i] = j;
-                            ++c;
-                        }
-                    }
-                }
-            }
-        }
-    return c;
-}
-
 struct BuildArgs {
     const int4 *pos;
     int4 *pos_box;  // when non-null: receives box_collision(pos) (the first Jacobi iteration's box pass)
@@ -171,26 +152,152 @@ struct BuildArgs {
     uint32_t *count, *idx;
     unsigned long long *total;
     Status *st;
+    const int4 *srec;         // per particle: position xyz and fixed-point search radius R (w)
+    uint32_t *ucount, *uidx;  // correction rows (the reverse-row arrays), when the radii differ
+    uint32_t *one_sided;      // per particle: one-sided pairs of its row (radii that differ)
 };
 
+// Appends an entry to a correction row (the reverse-row arrays; their counts were
+// zeroed before the walk, and any walk may append, so the slot is an atomic).
+__device__ __forceinline__ void push_correction(const BuildArgs &a, uint32_t row, uint32_t entry) {
+    const uint32_t slot = atomicAdd(&a.ucount[row], 1u);
+    if (slot < a.maxn) {
+        a.uidx[(size_t)slot * a.stride + row] = entry;
+    } else {
+        set_flag(a.st, APBF_FLAG_NEIGHBOR_OVERFLOW);
+        atomicMax(&a.st->required_neighbors, slot + 1u);
+    }
+}
+
+// Squared distance of two fixed-point positions when no axis differs by more than R
+// (else ~0: the pair is beyond R whatever the other axes).  FAST: both lie inside
+// the grid, so the 32-bit differences cannot wrap.
+template <bool FAST>
+__device__ __forceinline__ unsigned long long dist2_within(int4 a, int4 b, uint32_t R) {
+    uint32_t ax, ay, az;
+    if (FAST) {
+        ax = (uint32_t)abs(b.x - a.x);
+        ay = (uint32_t)abs(b.y - a.y);
+        az = (uint32_t)abs(b.z - a.z);
+    } else {
+        long long dx = (long long)b.x - a.x, dy = (long long)b.y - a.y, dz = (long long)b.z - a.z;
+        dx = dx < 0 ? -dx : dx;
+        dy = dy < 0 ? -dy : dy;
+        dz = dz < 0 ? -dz : dz;
+        if (dx > (long long)R || dy > (long long)R || dz > (long long)R) return ~0ull;
+        ax = (uint32_t)dx;
+        ay = (uint32_t)dy;
+        az = (uint32_t)dz;
+    }
+    if (max(ax, max(ay, az)) > R) return ~0ull;
+    return (unsigned long long)ax * ax + (unsigned long long)ay * ay + (unsigned long long)az * az;
+}
+
+// Walks the cells [x0, x1] x [y0, y1] x [z0, z1] and appends every neighbour of
+// particle i: j != i with |x_j - x_i| <= R_i (the neighbour predicate, C2).  The
+// walk is a chain of dependent loads (cell range -> candidates), so the ranges of
+// up to four cells of one (z, y) row are loaded together and candidates four at a
+// time.
+//
+// Correction rows (UNI, when the search radii differ): the position update of
+// particle i sums over the particles k whose rows hold i (|x_i - x_k| <= R_k),
+// and its deferred boundariness filter tests i's own row.  It sums over i's own
+// row and then over i's correction row: entries j of i's row whose radius does not
+// reach i (flagged kNoDelta, their terms subtracted), and particles k whose rows
+// hold i although i's radius does not reach them (added).  Both kinds are one-sided
+// pairs, found here (one_sided counts them) and appended after the walk.
+template <bool FAST>
+__device__ __forceinline__ uint32_t walk_cells(const BuildArgs &a, uint32_t i, int4 p, long long R, uint32_t x0,
+                                               uint32_t x1, uint32_t y0, uint32_t y1, uint32_t z0, uint32_t z1,
+                                               bool uni, uint32_t &one_sided) {
+    const uint32_t R32 = (uint32_t)R;
+    const unsigned long long R2 = (unsigned long long)R32 * R32;
+    uint32_t c = 0;
+    for (uint32_t cz = z0; cz <= z1; ++cz)
+        for (uint32_t cy = y0; cy <= y1; ++cy) {
+            const uint32_t yz = (spread3(cy) << 1) | (spread3(cz) << 2);
+            for (uint32_t cx0 = x0; cx0 <= x1; cx0 += 4) {
+                uint32_t cs[4], ce[4];
+#pragma unroll
+                for (int v = 0; v < 4; ++v) {
+                    const bool in = cx0 + v <= x1;
+                    const uint32_t key = yz | spread3(cx0 + v);
+                    cs[v] = in ? a.cstart[key] : 0u;
+                    ce[v] = in ? a.cend[key] : 0u;
+                }
+#pragma unroll 1  // one copy of the candidate loop: the kernel is bound by its instruction cache
+                for (int v = 0; v < 4; ++v) {
+                    const uint32_t s = cs[v], e = ce[v];
+                    for (uint32_t j0 = s; j0 < e; j0 += 4) {
+                        int4 q[4];
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) q[u] = j0 + u < e ? a.srec[j0 + u] : p;
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            const uint32_t j = j0 + u;
+                            if (j >= e || j == i) continue;
+                            const unsigned long long d2 = dist2_within<FAST>(p, q[u], R32);
+                            if (d2 > R2) continue;
+                            if (uni) {
+                                const unsigned long long Rj = (unsigned long long)(uint32_t)max(q[u].w, 0);
+                                one_sided += (q[u].w >= 0 && d2 <= Rj * Rj) ? 0u : 1u;
+                            }
+                            if (c < a.maxn) a.idx[(size_t)c * a.stride + i] = j;
+                            ++c;
+                        }
+                    }
+                }
+            }
+        }
+    return c;
+}
+
+// box_push as a call: the walk's kernel is bound by its instruction cache, and the
+// box pass runs once per particle.
+__device__ __noinline__ int4 box_push_call(int4 ip, float r, uint32_t id, const float4 *__restrict__ bmin,
+                                           const float4 *__restrict__ bmax, const float4 *__restrict__ rot,
+                                           uint32_t nb) {
+    return box_push(ip, r, id, bmin, bmax, rot, nb);
+}
+
+// The one-sided pairs of the rows just built (radii that differ; particles whose
+// walk counted some): found again on the particle's row, i's correction row
+// subtracts j, j's adds i.  A kernel of its own, so that the walk holds no atomics.
+__global__ void k_corrections(BuildArgs a) {
+    if (a.st->range_min == a.st->range_max) return;  // symmetric rows: nothing one-sided
+    const uint32_t n = a.d_len[kLenParticles];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (!a.one_sided[i]) continue;
+        const int4 p = a.srec[i];
+        const uint32_t m = a.count[i];
+        for (uint32_t k = 0; k < m; ++k) {
+            const uint32_t j = a.idx[(size_t)k * a.stride + i];
+            const int4 q = a.srec[j];
+            const unsigned long long Rj = (unsigned long long)(uint32_t)max(q.w, 0);
+            if (q.w >= 0 && dist2_within<false>(p, q, (uint32_t)Rj) <= Rj * Rj) continue;
+            push_correction(a, i, j | kNoDelta);
+            push_correction(a, j, i);
+        }
+    }
+}
+
 // neighborhood_green.comp:49-87 with the canonical predicate (C2), one thread per
-// particle.  A box that touches no edge cell of the grid only meets particles
-// inside the grid (edge cells also hold the clamped outsiders), so it uses the
-// 32-bit predicate.
+// particle, candidates read from the search records.  A box that touches no edge
+// cell of the grid only meets particles inside the grid (edge cells also hold the
+// clamped outsiders), so it uses the 32-bit differences.
 __global__ void __launch_bounds__(256, 4) k_build_rows(BuildArgs a) {
     const uint32_t n = a.d_len[kLenParticles];
     const uint32_t last = (1u << a.L) - 1u;
+    const bool uni = a.st->range_min != a.st->range_max;  // the radii differ: union rows
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.st->union_rows = uni ? 1u : 0u;
     unsigned long long local = 0;
-    long long rmin = 0x7fffffffffffffffll, rmax = -1;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const int4 p = a.pos[i];
-        const long long R = range_fixed(a.range[i], a.scale);
+        const int4 p = a.srec[i];
+        const long long R = p.w;
         uint32_t c = 0;
         if (R < 0) {
             set_flag(a.st, APBF_FLAG_NONFINITE);  // NaN or negative kernel width: no neighbours
         } else {
-            rmin = R < rmin ? R : rmin;
-            rmax = R > rmax ? R : rmax;
             const Bounds &b = a.b;
             const uint32_t x0 = cell_coord((long long)p.x - R, b.lo[0], b.hi[0], a.L);
             const uint32_t x1 = cell_coord((long long)p.x + R, b.lo[0], b.hi[0], a.L);
@@ -199,11 +306,10 @@ __global__ void __launch_bounds__(256, 4) k_build_rows(BuildArgs a) {
             const uint32_t z0 = cell_coord((long long)p.z - R, b.lo[2], b.hi[2], a.L);
             const uint32_t z1 = cell_coord((long long)p.z + R, b.lo[2], b.hi[2], a.L);
             const bool fast = a.fast_ok && x0 > 0 && y0 > 0 && z0 > 0 && x1 < last && y1 < last && z1 < last;
-            if (fast)
-                c = walk_cells<true>(i, p, R, x0, x1, y0, y1, z0, z1, a.pos, a.cstart, a.cend, a.stride, a.maxn, a.idx);
-            else
-                c = walk_cells<false>(i, p, R, x0, x1, y0, y1, z0, z1, a.pos, a.cstart, a.cend, a.stride, a.maxn,
-                                      a.idx);
+            uint32_t one_sided = 0;
+            c = fast ? walk_cells<true>(a, i, p, R, x0, x1, y0, y1, z0, z1, uni, one_sided)
+                     : walk_cells<false>(a, i, p, R, x0, x1, y0, y1, z0, z1, uni, one_sided);
+            if (uni) a.one_sided[i] = one_sided;  // k_corrections appends them
         }
         if (c > a.maxn) {
             set_flag(a.st, APBF_FLAG_NEIGHBOR_OVERFLOW);
@@ -211,310 +317,16 @@ __global__ void __launch_bounds__(256, 4) k_build_rows(BuildArgs a) {
         }
         a.count[i] = c < a.maxn ? c : a.maxn;
         local += c < a.maxn ? c : a.maxn;
-        if (a.pos_box) a.pos_box[i] = box_push(p, a.radius[i], i, a.bmin, a.bmax, a.rot, a.nboxes);
+        if (a.pos_box) a.pos_box[i] = box_push_call(a.pos[i], a.radius[i], i, a.bmin, a.bmax, a.rot, a.nboxes);
     }
-    // block reduction of the pair count and of the radius range
-    for (int off = 16; off > 0; off >>= 1) {
-        local += __shfl_down_sync(0xffffffffu, local, off);
-        long long a2 = __shfl_down_sync(0xffffffffu, rmin, off);
-        long long c2 = __shfl_down_sync(0xffffffffu, rmax, off);
-        rmin = a2 < rmin ? a2 : rmin;
-        rmax = c2 > rmax ? c2 : rmax;
-    }
-    if ((threadIdx.x & 31) == 0) {
-        if (local) atomicAdd(a.total, local);
-        if (rmax >= 0) {
-            atomicMin(&a.st->range_min, (unsigned long long)rmin);
-            atomicMax(&a.st->range_max, (unsigned long long)rmax);
-        }
-    }
-}
-
-// The same rows as k_build_rows, built by blocks of kTileP consecutive (Morton-
-// sorted) particles that stage their candidates in shared memory: the block takes
-// the union of its particles' cell boxes (at most kTileCells cells), loads the
-// particles of those cells kTileBuf at a time with coalesced reads, and every
-// thread tests its particle against each staged candidate whose cell lies in the
-// particle's own box.  Candidates come in (z, y, x) cell order and index order
-// within a cell, the order of walk_cells, so the rows are identical.  A block whose
-// union is larger (a jump of the Morton curve inside the block) walks per thread.
-constexpr int kTileP = 64;
-constexpr int kTileCells = 216;
-constexpr int kTileBuf = 512;
-
-__global__ void __launch_bounds__(kTileP) k_build_rows_tiled(BuildArgs a) {
-    __shared__ int4 s_pos[kTileBuf];
-    __shared__ uint32_t s_idx[kTileBuf];
-    __shared__ uint16_t s_cell[kTileBuf];        // region-relative cell of the candidate: x | y << 5 | z << 10
-    __shared__ uint32_t s_start[kTileCells];
-    __shared__ uint32_t s_pre[kTileCells + 1];  // exclusive prefix of the cells' particle counts
-    __shared__ int s_box[6];
-    const uint32_t n = a.d_len[kLenParticles];
-    const uint32_t last = (1u << a.L) - 1u;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    unsigned long long local = 0;
-    long long rmin = 0x7fffffffffffffffll, rmax = -1;
-    for (uint32_t base = blockIdx.x * kTileP; base < n; base += gridDim.x * kTileP) {
-        const uint32_t i = base + threadIdx.x;
-        const bool valid = i < n;
-        int4 p = make_int4(0, 0, 0, 0);
-        long long R = -1;
-        uint32_t x0 = 1, x1 = 0, y0 = 1, y1 = 0, z0 = 1, z1 = 0;
-        if (valid) {
-            p = a.pos[i];
-            R = range_fixed(a.range[i], a.scale);
-            if (R < 0) {
-                set_flag(a.st, APBF_FLAG_NONFINITE);
-            } else {
-                rmin = R < rmin ? R : rmin;
-                rmax = R > rmax ? R : rmax;
-                const Bounds &b = a.b;
-                x0 = cell_coord((long long)p.x - R, b.lo[0], b.hi[0], a.L);
-                x1 = cell_coord((long long)p.x + R, b.lo[0], b.hi[0], a.L);
-                y0 = cell_coord((long long)p.y - R, b.lo[1], b.hi[1], a.L);
-                y1 = cell_coord((long long)p.y + R, b.lo[1], b.hi[1], a.L);
-                z0 = cell_coord((long long)p.z - R, b.lo[2], b.hi[2], a.L);
-                z1 = cell_coord((long long)p.z + R, b.lo[2], b.hi[2], a.L);
-            }
-        }
-        const bool has = valid && R >= 0;
-        if (threadIdx.x == 0) {
-            s_box[0] = s_box[2] = s_box[4] = 0x7fffffff;
-            s_box[1] = s_box[3] = s_box[5] = -1;
-        }
-        __syncthreads();
-        if (has) {
-            atomicMin(&s_box[0], (int)x0);
-            atomicMax(&s_box[1], (int)x1);
-            atomicMin(&s_box[2], (int)y0);
-            atomicMax(&s_box[3], (int)y1);
-            atomicMin(&s_box[4], (int)z0);
-            atomicMax(&s_box[5], (int)z1);
-        }
-        __syncthreads();
-        const int bx0 = s_box[0], by0 = s_box[2], bz0 = s_box[4];
-        const int nx = s_box[1] - bx0 + 1, ny = s_box[3] - by0 + 1, nz = s_box[5] - bz0 + 1;
-        const bool fast = has && a.fast_ok && x0 > 0 && y0 > 0 && z0 > 0 && x1 < last && y1 < last && z1 < last;
-        uint32_t c = 0;
-        if (s_box[1] < 0) {
-            // no particle of the block searches
-        } else if ((long long)nx * ny * nz > kTileCells || nx > 31 || ny > 31 || nz > 31) {
-            if (has) {
-                c = fast ? walk_cells<true>(i, p, R, x0, x1, y0, y1, z0, z1, a.pos, a.cstart, a.cend, a.stride,
-                                            a.maxn, a.idx)
-                         : walk_cells<false>(i, p, R, x0, x1, y0, y1, z0, z1, a.pos, a.cstart, a.cend, a.stride,
-                                             a.maxn, a.idx);
-            }
-        } else {
-            const int cells = nx * ny * nz;
-            // cell ranges of the region in (z, y, x) order
-            for (int k = threadIdx.x; k < cells; k += kTileP) {
-                const uint32_t cx = bx0 + k % nx, cy = by0 + (k / nx) % ny, cz = bz0 + k / (nx * ny);
-                const uint32_t key = spread3(cx) | (spread3(cy) << 1) | (spread3(cz) << 2);
-                const uint32_t cs = a.cstart[key], ce = a.cend[key];
-                s_start[k] = cs;
-                s_pre[k + 1] = ce - cs;
-            }
-            __syncthreads();
-            if (warp == 0) {  // exclusive prefix over the cells: 7 per lane, then a warp scan
-                uint32_t v[7], sum = 0;
-#pragma unroll
-                for (int t = 0; t < 7; ++t) {
-                    const int k = lane * 7 + t;
-                    v[t] = k < cells ? s_pre[k + 1] : 0u;
-                    sum += v[t];
-                }
-                uint32_t incl = sum;
-#pragma unroll
-                for (int off = 1; off < 32; off <<= 1) {
-                    const uint32_t o = __shfl_up_sync(0xffffffffu, incl, off);
-                    if (lane >= off) incl += o;
-                }
-                uint32_t run = incl - sum;
-#pragma unroll
-                for (int t = 0; t < 7; ++t) {
-                    const int k = lane * 7 + t;
-                    if (k < cells) s_pre[k] = run;
-                    run += v[t];
-                }
-                if (lane == 31) s_pre[cells] = incl;
-            }
-            __syncthreads();
-            const uint32_t total = s_pre[cells];
-            // this particle's own box relative to the region
-            const int ox0 = (int)x0 - bx0, ox1 = (int)x1 - bx0, oy0 = (int)y0 - by0, oy1 = (int)y1 - by0,
-                      oz0 = (int)z0 - bz0, oz1 = (int)z1 - bz0;
-            const uint32_t R32 = (uint32_t)R;
-            const unsigned long long R2 = (unsigned long long)R32 * R32;
-            for (uint32_t b0 = 0; b0 < total; b0 += kTileBuf) {
-                const uint32_t m = total - b0 < (uint32_t)kTileBuf ? total - b0 : (uint32_t)kTileBuf;
-                for (uint32_t k = threadIdx.x; k < m; k += kTileP) {
-                    const uint32_t g = b0 + k;
-                    int lo = 0, hi = cells;  // largest cell with s_pre[cell] <= g
-                    while (hi - lo > 1) {
-                        const int mid = (lo + hi) >> 1;
-                        if (s_pre[mid] <= g) lo = mid;
-                        else hi = mid;
-                    }
-                    const uint32_t j = s_start[lo] + (g - s_pre[lo]);
-                    s_pos[k] = a.pos[j];
-                    s_idx[k] = j;
-                    s_cell[k] = (uint16_t)((lo % nx) | (((lo / nx) % ny) << 5) | ((lo / (nx * ny)) << 10));
-                }
-                __syncthreads();
-                if (has) {
-                    for (uint32_t k = 0; k < m; ++k) {
-                        const uint32_t rc = s_cell[k];
-                        const int rx = rc & 31, ry = (rc >> 5) & 31, rz = rc >> 10;
-                        if (rx < ox0 || rx > ox1 || ry < oy0 || ry > oy1 || rz < oz0 || rz > oz1) continue;
-                        const uint32_t j = s_idx[k];
-                        if (j == i) continue;
-                        const int4 q = s_pos[k];
-                        if (fast ? !within32(p, q, R32, R2) : !within(p, q, R)) continue;
-                        if (c < a.maxn) a.idx[(size_t)c * a.stride + i] = j;
-                        ++c;
-                    }
-                }
-                __syncthreads();
-            }
-        }
-        if (valid) {
-            if (c > a.maxn) {
-                set_flag(a.st, APBF_FLAG_NEIGHBOR_OVERFLOW);
-                atomicMax(&a.st->required_neighbors, c);
-            }
-            a.count[i] = c < a.maxn ? c : a.maxn;
-            local += c < a.maxn ? c : a.maxn;
-            if (a.pos_box) a.pos_box[i] = box_push(p, a.radius[i], i, a.bmin, a.bmax, a.rot, a.nboxes);
-        }
-        __syncthreads();  // s_box is reused by the next chunk
-    }
-    for (int off = 16; off > 0; off >>= 1) {
-        local += __shfl_down_sync(0xffffffffu, local, off);
-        long long a2 = __shfl_down_sync(0xffffffffu, rmin, off);
-        long long c2 = __shfl_down_sync(0xffffffffu, rmax, off);
-        rmin = a2 < rmin ? a2 : rmin;
-        rmax = c2 > rmax ? c2 : rmax;
-    }
-    if (lane == 0) {
-        if (local) atomicAdd(a.total, local);
-        if (rmax >= 0) {
-            atomicMin(&a.st->range_min, (unsigned long long)rmin);
-            atomicMax(&a.st->range_max, (unsigned long long)rmax);
-        }
-    }
-}
-
-// The same rows again, one warp per particle: lanes take 32 of the particle's
-// cells at a time, a warp scan turns their particle counts into offsets, and each
-// round the 32 lanes test 32 consecutive candidates (of whichever cells they fall
-// in) and append the hits with a ballot, so the row keeps the walk's order (cells
-// in (z, y, x) order, indices ascending within a cell) and the lanes stay busy
-// whatever the particles' cell counts.
-__global__ void __launch_bounds__(256) k_build_rows_warp(BuildArgs a) {
-    const uint32_t n = a.d_len[kLenParticles];
-    const uint32_t last = (1u << a.L) - 1u;
-    const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
-    unsigned long long local = 0;
-    long long rmin = 0x7fffffffffffffffll, rmax = -1;
-    for (uint32_t i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps) {  // warp-uniform
-        const int4 p = a.pos[i];
-        const long long R = range_fixed(a.range[i], a.scale);
-        uint32_t c = 0;
-        if (R < 0) {
-            if (lane == 0) set_flag(a.st, APBF_FLAG_NONFINITE);
-        } else {
-            rmin = R < rmin ? R : rmin;
-            rmax = R > rmax ? R : rmax;
-            const Bounds &b = a.b;
-            const uint32_t x0 = cell_coord((long long)p.x - R, b.lo[0], b.hi[0], a.L);
-            const uint32_t x1 = cell_coord((long long)p.x + R, b.lo[0], b.hi[0], a.L);
-            const uint32_t y0 = cell_coord((long long)p.y - R, b.lo[1], b.hi[1], a.L);
-            const uint32_t y1 = cell_coord((long long)p.y + R, b.lo[1], b.hi[1], a.L);
-            const uint32_t z0 = cell_coord((long long)p.z - R, b.lo[2], b.hi[2], a.L);
-            const uint32_t z1 = cell_coord((long long)p.z + R, b.lo[2], b.hi[2], a.L);
-            const bool fast = a.fast_ok && x0 > 0 && y0 > 0 && z0 > 0 && x1 < last && y1 < last && z1 < last;
-            const uint32_t nx = x1 - x0 + 1, ny = y1 - y0 + 1, nz = z1 - z0 + 1;
-            const uint32_t ncells = nx * ny * nz;
-            const uint32_t R32 = (uint32_t)R;
-            const unsigned long long R2 = (unsigned long long)R32 * R32;
-            for (uint32_t cb = 0; cb < ncells; cb += 32) {
-                // this lane's cell and its particle range
-                const uint32_t k = cb + lane;
-                uint32_t cs = 0, cnt = 0;
-                if (k < ncells) {
-                    const uint32_t cx = x0 + k % nx, cy = y0 + (k / nx) % ny, cz = z0 + k / (nx * ny);
-                    const uint32_t key = spread3(cx) | (spread3(cy) << 1) | (spread3(cz) << 2);
-                    cs = a.cstart[key];
-                    cnt = a.cend[key] - cs;
-                }
-                uint32_t incl = cnt;  // inclusive scan of the counts over the lanes
-#pragma unroll
-                for (int off = 1; off < 32; off <<= 1) {
-                    const uint32_t o = __shfl_up_sync(0xffffffffu, incl, off);
-                    if (lane >= (uint32_t)off) incl += o;
-                }
-                const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-                const uint32_t excl = incl - cnt;
-                for (uint32_t t0 = 0; t0 < total; t0 += 32) {
-                    const uint32_t g = t0 + lane;
-                    // the lane whose cell holds candidate g: the last lane with excl <= g
-                    uint32_t lo = 0;
-#pragma unroll
-                    for (int step = 16; step > 0; step >>= 1) {
-                        const uint32_t e = __shfl_sync(0xffffffffu, excl, lo + step);
-                        if (e <= g) lo += step;
-                    }
-                    const uint32_t owner_cs = __shfl_sync(0xffffffffu, cs, lo);
-                    const uint32_t owner_ex = __shfl_sync(0xffffffffu, excl, lo);
-                    bool hit = false;
-                    uint32_t j = 0;
-                    if (g < total) {
-                        j = owner_cs + (g - owner_ex);
-                        if (j != i) {
-                            const int4 q = a.pos[j];
-                            hit = fast ? within32(p, q, R32, R2) : within(p, q, R);
-                        }
-                    }
-                    const uint32_t mask = __ballot_sync(0xffffffffu, hit);
-                    if (hit) {
-                        const uint32_t slot = c + __popc(mask & ((1u << lane) - 1u));
-                        if (slot < a.maxn) a.idx[(size_t)slot * a.stride + i] = j;
-                    }
-                    c += __popc(mask);
-                }
-            }
-        }
-        if (lane == 0) {
-            if (c > a.maxn) {
-                set_flag(a.st, APBF_FLAG_NEIGHBOR_OVERFLOW);
-                atomicMax(&a.st->required_neighbors, c);
-            }
-            a.count[i] = c < a.maxn ? c : a.maxn;
-            local += c < a.maxn ? c : a.maxn;
-            if (a.pos_box) a.pos_box[i] = box_push(p, a.radius[i], i, a.bmin, a.bmax, a.rot, a.nboxes);
-        }
-    }
-    for (int off = 16; off > 0; off >>= 1) {
-        local += __shfl_down_sync(0xffffffffu, local, off);
-        long long a2 = __shfl_down_sync(0xffffffffu, rmin, off);
-        long long c2 = __shfl_down_sync(0xffffffffu, rmax, off);
-        rmin = a2 < rmin ? a2 : rmin;
-        rmax = c2 > rmax ? c2 : rmax;
-    }
-    if (lane == 0) {
-        if (local) atomicAdd(a.total, local);
-        if (rmax >= 0) {
-            atomicMin(&a.st->range_min, (unsigned long long)rmin);
-            atomicMax(&a.st->range_max, (unsigned long long)rmax);
-        }
-    }
+    for (int off = 16; off > 0; off >>= 1) local += __shfl_down_sync(0xffffffffu, local, off);
+    if ((threadIdx.x & 31) == 0 && local) atomicAdd(a.total, local);
 }
 
 __global__ void k_reverse_rows(const uint32_t *d_len, uint32_t stride, uint32_t maxn, const uint32_t *__restrict__ count,
                                const uint32_t *__restrict__ idx, uint32_t *__restrict__ rcount,
                                uint32_t *__restrict__ ridx, Status *st) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->union_rows = 0u;
     if (st->range_min == st->range_max) return;  // symmetric rows: reverse = forward
     uint32_t n = d_len[kLenParticles];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -569,12 +381,15 @@ void swap_all(apbf_ctx *ctx) { ctx->fcur ^= 1; }
 
 // Gathers every particle attribute in the order ctx->perm gives (new id -> old id),
 // remaps the transfer and glue lists, and makes the gathered set current.
-apbf_status reorder_particles(apbf_ctx *ctx, cudaStream_t s) {
+// With `search` the gather also writes the search records (srec) for range scale
+// `scale` and reduces the search radii's range into the status block.
+apbf_status reorder_particles(apbf_ctx *ctx, cudaStream_t s, bool search, float scale) {
     const uint32_t cap = ctx->cfg.particle_capacity;
     FluidBufs &cur = ctx->fl[ctx->fcur];
     FluidBufs &alt = ctx->fl[ctx->fcur ^ 1];
     APBF_BEFORE_LAUNCH(ctx, s, "k_reorder");
-    k_reorder<<<grid_for(ctx, cap), kBlock, 0, s>>>(cur, alt, ctx->perm, ctx->inv_perm, ctx->d_len);
+    k_reorder<<<grid_for(ctx, cap), kBlock, 0, s>>>(cur, alt, ctx->perm, ctx->inv_perm, ctx->d_len,
+                                                    search ? ctx->srec : nullptr, scale, ctx->status);
     APBF_AFTER_LAUNCH(ctx, s, "k_reorder");
     APBF_BEFORE_LAUNCH(ctx, s, "k_remap_transfers");
     k_remap_transfers<<<grid_for(ctx, ctx->cfg.transfer_capacity), kBlock, 0, s>>>(ctx->tr[ctx->tcur], ctx->inv_perm,
@@ -595,7 +410,6 @@ apbf_status neighborhood_green(apbf_ctx *ctx, float range_scale, const float min
     const uint32_t cap = ctx->cfg.particle_capacity;
     Bounds b = fixed_bounds(minp, maxp);
     FluidBufs &cur = ctx->fl[ctx->fcur];
-    FluidBufs &alt = ctx->fl[ctx->fcur ^ 1];
     const int g = grid_for(ctx, cap);
 
     APBF_BEFORE_LAUNCH(ctx, s, "k_position_keys");
@@ -604,7 +418,11 @@ apbf_status neighborhood_green(apbf_ctx *ctx, float range_scale, const float min
     apbf_status r = sort_pairs_device(ctx, ctx->keys[0], ctx->vals[0], ctx->d_len + kLenParticles, cap, 3u * L,
                                       ctx->sorted_keys, ctx->perm, s);
     if (r != APBF_OK) return r;
-    r = reorder_particles(ctx, s);
+    // the reorder reduces the search radii's range: reset it first
+    APBF_BEFORE_LAUNCH(ctx, s, "k_reset_search");
+    k_reset_search<<<1, 1, 0, s>>>(ctx->status, ctx->d_pairs);
+    APBF_AFTER_LAUNCH(ctx, s, "k_reset_search");
+    r = reorder_particles(ctx, s, true, range_scale);
     if (r != APBF_OK) return r;
     FluidBufs &f = ctx->fl[ctx->fcur];
 
@@ -614,9 +432,6 @@ apbf_status neighborhood_green(apbf_ctx *ctx, float range_scale, const float min
     APBF_BEFORE_LAUNCH(ctx, s, "k_cell_ranges");
     k_cell_ranges<<<g, kBlock, 0, s>>>(ctx->sorted_keys, ctx->d_len, ctx->cell_start, ctx->cell_end);
     APBF_AFTER_LAUNCH(ctx, s, "k_cell_ranges");
-    APBF_BEFORE_LAUNCH(ctx, s, "k_reset_search");
-    k_reset_search<<<1, 1, 0, s>>>(ctx->status, ctx->d_pairs);
-    APBF_AFTER_LAUNCH(ctx, s, "k_reset_search");
     APBF_BEFORE_LAUNCH(ctx, s, "k_build_rows");
     BuildArgs ba;
     ba.pos = f.pos;
@@ -643,22 +458,31 @@ apbf_status neighborhood_green(apbf_ctx *ctx, float range_scale, const float min
     ba.idx = ctx->nb_idx;
     ba.total = ctx->d_pairs;
     ba.st = ctx->status;
-    if (ctx->tuning.build_tiled == 1)
-        k_build_rows_tiled<<<grid_for(ctx, cap, kTileP, 24), kTileP, 0, s>>>(ba);
-    else if (ctx->tuning.build_tiled == 2)
-        k_build_rows_warp<<<grid_for(ctx, (uint32_t)std::min<uint64_t>((uint64_t)cap * 32u, 0xffffffffu), kBlock, 8),
-                            kBlock, 0, s>>>(ba);
-    else
-        k_build_rows<<<grid_for(ctx, cap, kBlock, 8), kBlock, 0, s>>>(ba);
+    ba.srec = ctx->srec;
+    ba.ucount = ctx->rev_count;
+    ba.uidx = ctx->rev_idx;
+    ba.one_sided = ctx->flag_scan;  // scratch: not in use during the search
+    APBF_CUDA(cudaMemsetAsync(ctx->rev_count, 0, (size_t)cap * sizeof(uint32_t), s));  // correction rows
+    k_build_rows<<<grid_for(ctx, cap, kBlock, 8), kBlock, 0, s>>>(ba);
     APBF_AFTER_LAUNCH(ctx, s, "k_build_rows");
+    APBF_BEFORE_LAUNCH(ctx, s, "k_corrections");
+    k_corrections<<<grid_for(ctx, cap), kBlock, 0, s>>>(ba);
+    APBF_AFTER_LAUNCH(ctx, s, "k_corrections");
     if (fuse_box) {  // the box-collided positions are the current ones now
         int4 *t = f.pos;
         f.pos = spare.pos;
         spare.pos = t;
     }
-    return build_reverse_rows(ctx, s);
+    APBF_BEFORE_LAUNCH(ctx, s, "k_clamp_rev");
+    k_clamp_rev<<<grid_for(ctx, cap), kBlock, 0, s>>>(ctx->d_len, ctx->cfg.max_neighbors, ctx->rev_count, ctx->status);
+    APBF_AFTER_LAUNCH(ctx, s, "k_clamp_rev");
+    return APBF_OK;
 }
 
+// Reverse rows by transposing the forward rows (the binary-search neighbourhood and
+// the rows spread_kernel_width prunes): row j lists every i whose row holds j, with
+// no forward prefix, so the boundariness filter stays in the density pass
+// (status union_rows = 0).
 apbf_status build_reverse_rows(apbf_ctx *ctx, cudaStream_t s) {
     const uint32_t cap = ctx->cfg.particle_capacity;
     APBF_CUDA(cudaMemsetAsync(ctx->rev_count, 0, (size_t)cap * sizeof(uint32_t), s));

@@ -63,7 +63,6 @@ struct PassA {
     int4 *shift;
     float4 *rec;  // per particle: lambda, Gauss ivd, Gauss norm, kernel width (read by k_delta)
     int4 *pk;     // per particle: position xyz and the applied lambda (read by k_delta when widths are uniform)
-    int rec_if_mixed;  // 1 (passes after the first): rec only when the widths are not all equal
     uint32_t *dbg_dens;
     int4 *dbg_grad;
     uint32_t *dbg_sq;
@@ -447,15 +446,18 @@ template <bool GAUSS, int L, bool XTRA>
 __global__ void __launch_bounds__(256, GAUSS ? 4 : 3) k_density_lambda(PassA a) {
     const bool skip = (a.early_exit && *(volatile uint32_t *)&a.st->converged) ||
                       (a.loop_offset >= 0 && a.st->pass_index + (uint32_t)a.loop_offset >= a.max_passes);
-    // With symmetric rows the Gauss filter runs in this pass's position update, which
-    // gathers over the same neighbours anyway; filter_tag tells it whether to.
-    const bool defer = GAUSS && a.filt && a.method == 2 && a.st->range_min == a.st->range_max;
+    // With symmetric rows or union rows the Gauss filter runs in this pass's position
+    // update, which gathers over the same neighbours anyway; filter_tag tells it whether to.
+    const bool defer = GAUSS && a.filt && a.method == 2 &&
+                       (a.st->range_min == a.st->range_max || a.st->union_rows != 0u);
     if (blockIdx.x == 0 && threadIdx.x == 0) a.st->filter_tag = (!skip && defer) ? 1u : 0u;
     if (skip) return;  // uniform over the grid
     const uint32_t n = a.d_len[kLenParticles];
     const uint32_t sub = threadIdx.x % L;
     // passes after the first: the widths' uniformity of the first pass still holds
-    const bool write_rec = !(a.rec_if_mixed && a.st->kw_uniform != 0u);
+    // the position update of the Gauss kernel gathers the packed records and widths;
+    // the other kernels gather the solve records, written every pass
+    const bool write_rec = !GAUSS;
     PassSums ps;
     // the block iterates as a whole (uniform trip count: the group shuffles need every lane)
     const uint32_t gpb = blockDim.x / L;
@@ -520,19 +522,52 @@ __device__ __forceinline__ void accumulate(float *dst, int mode, uint32_t j, flo
     else if (mode == 2) dst[j] += v;
 }
 
-// Sum over particle j's (reverse) row of int(gradW_ij * lambda_i * 2^18)
-// (incompressibility_3.comp:62-66 as a gather) and the deferred boundariness
-// filter.  PACKED: the neighbours' packed records (position, applied lambda) with
-// j's own Gauss constants cj; else the solve records and the positions.
+// One neighbour's term of a position update: int(gradW_ij * lambda_i * 2^18) per
+// axis (incompressibility_3.comp:62-66) for the neighbour's record q (position,
+// and for the Gauss kernel the applied lambda in w), its width kwi or solve record
+// rr.  Constants: cj (j's own) when PACKED or the widths are equal bit for bit, else
+// the neighbour's.  The main row and the correction rows use this one function, so
+// a term subtracted again cancels exactly.
+template <bool GAUSS, bool PACKED>
+__device__ __forceinline__ int3 pair_delta(const PassB &a, int4 q, float lam, float kwi, float4 rr, int4 p, float kwj,
+                                           KConst cj) {
+    KConst c;
+    if (PACKED) {
+        c = cj;
+    } else if (GAUSS) {
+        c = __float_as_uint(kwi) == __float_as_uint(kwj) ? cj : gauss_consts(kwi);
+    } else {
+        c.ivd = rr.y;
+        c.norm = rr.z;
+    }
+    const float3 d = fdiff(q, p);
+    const float r2 = dot3x(d, d);
+    float3 g;
+    if (GAUSS) {
+        g = kernel_gradient(1, d, r2, 0.0f, c, gauss_height(r2, c));
+    } else {
+        g = kernel_gradient(a.gk, d, r2, rr.w, c, a.gk == 1 ? gauss_height(r2, c) : 0.0f);
+    }
+    const float sc = lam * APBF_FIX;
+    return make_int3(f2i(g.x * sc), f2i(g.y * sc), f2i(g.z * sc));
+}
+
+// Sum over particle j's row of the neighbours' terms (incompressibility_3.comp:62-66
+// as a gather) and the deferred boundariness filter over the row's first fcnt
+// entries.  PACKED: the neighbours' packed records (position, applied lambda) with
+// j's own Gauss constants cj (every width equal); GAUSS otherwise: the packed
+// records and the neighbours' widths; other kernels: the solve records and the
+// positions.
 template <bool GAUSS, int L, bool PACKED>
 __device__ __forceinline__ int3 delta_row(const PassB &a, const int4 *__restrict__ pos, const uint32_t *row, uint32_t cnt,
-                                          uint32_t j, uint32_t sub,
-                                          int4 p, KConst cj, bool fil, float3 ed, bool &hit, int4 start) {
+                                          uint32_t fcnt, uint32_t j, uint32_t sub, int4 p, float kwj, KConst cj,
+                                          bool fil, float3 ed, bool &hit, int4 start) {
     int32_t ax = start.x, ay = start.y, az = start.z;
     for (uint32_t k0 = sub; k0 < cnt; k0 += L * kUnroll) {
         uint32_t ii[kUnroll];
         float4 rr[kUnroll];
         int4 qq[kUnroll];
+        float kk[kUnroll];
 #pragma unroll
         for (int u = 0; u < kUnroll; ++u) {
             const uint32_t k = k0 + u * L;
@@ -542,6 +577,9 @@ __device__ __forceinline__ int3 delta_row(const PassB &a, const int4 *__restrict
         for (int u = 0; u < kUnroll; ++u) {
             if (PACKED) {
                 qq[u] = a.pk[ii[u]];
+            } else if (GAUSS) {
+                qq[u] = a.pk[ii[u]];
+                kk[u] = a.kw[ii[u]];
             } else {
                 rr[u] = a.rec[ii[u]];
                 qq[u] = pos[ii[u]];
@@ -549,34 +587,55 @@ __device__ __forceinline__ int3 delta_row(const PassB &a, const int4 *__restrict
         }
 #pragma unroll
         for (int u = 0; u < kUnroll; ++u) {
-            if (fil && !hit && k0 + u * L < cnt) {
+            if (fil && !hit && k0 + u * L < fcnt) {
                 const float3 dn = fdiff(qq[u], p);  // x_i - x_j ...
                 hit = gauss_filter_hit(ed, make_float3(-dn.x, -dn.y, -dn.z));  // ... as the offset x_j - x_i
             }
-            const float lam = k0 + u * L < cnt ? (PACKED ? __int_as_float(qq[u].w) : rr[u].x) : 0.0f;
+            const float lam = k0 + u * L < cnt ? (PACKED || GAUSS ? __int_as_float(qq[u].w) : rr[u].x) : 0.0f;
             if (lam == 0.0f) continue;  // the applied lambda (incompressibility_3.comp:63); padding lanes
-            KConst c;
-            if (PACKED) {
-                c = cj;
-            } else {
-                c.ivd = rr[u].y;
-                c.norm = rr[u].z;
-            }
-            const float3 d = fdiff(qq[u], p);
-            const float r2 = dot3x(d, d);
-            float3 g;
-            if (GAUSS) {
-                g = kernel_gradient(1, d, r2, 0.0f, c, gauss_height(r2, c));
-            } else {
-                g = kernel_gradient(a.gk, d, r2, rr[u].w, c, a.gk == 1 ? gauss_height(r2, c) : 0.0f);
-            }
-            const float sc = lam * APBF_FIX;
-            ax = wadd(ax, f2i(g.x * sc));
-            ay = wadd(ay, f2i(g.y * sc));
-            az = wadd(az, f2i(g.z * sc));
+            const int3 t = pair_delta<GAUSS, PACKED>(a, qq[u], lam, kk[u], rr[u], p, kwj, cj);
+            ax = wadd(ax, t.x);
+            ay = wadd(ay, t.y);
+            az = wadd(az, t.z);
         }
     }
     return make_int3(ax, ay, az);
+}
+
+// Particle j's correction row (radii that differ, neighborhood.cu): terms of
+// entries flagged kNoDelta subtracted (j holds them, their radius does not reach
+// j), the others added (they hold j, j's radius does not reach them).  Lane sub of
+// the group of L takes entries sub, sub + L, ...
+template <bool GAUSS, int L, bool PACKED>
+__device__ __forceinline__ int3 delta_corrections(const PassB &a, const int4 *__restrict__ pos, uint32_t m, uint32_t j,
+                                                  uint32_t sub, int4 p, float kwj, KConst cj, int3 acc) {
+    for (uint32_t k = sub; k < m; k += L) {
+        const uint32_t e = a.ridx[(size_t)k * a.stride + j];
+        const uint32_t i = e & ~kNoDelta;
+        float4 rr = make_float4(0.f, 0.f, 0.f, 0.f);
+        int4 q;
+        float kwi = 0.0f;
+        if (PACKED || GAUSS) {
+            q = a.pk[i];
+            if (!PACKED) kwi = a.kw[i];
+        } else {
+            rr = a.rec[i];
+            q = pos[i];
+        }
+        const float lam = PACKED || GAUSS ? __int_as_float(q.w) : rr.x;
+        if (lam == 0.0f) continue;
+        const int3 t = pair_delta<GAUSS, PACKED>(a, q, lam, kwi, rr, p, kwj, cj);
+        if (e & kNoDelta) {
+            acc.x = wadd(acc.x, -t.x);
+            acc.y = wadd(acc.y, -t.y);
+            acc.z = wadd(acc.z, -t.z);
+        } else {
+            acc.x = wadd(acc.x, t.x);
+            acc.y = wadd(acc.y, t.y);
+            acc.z = wadd(acc.z, t.z);
+        }
+    }
+    return acc;
 }
 
 // One particle (row j_raw, lane sub of its group of L) of a position update:
@@ -586,12 +645,13 @@ __device__ __forceinline__ int3 delta_row(const PassB &a, const int4 *__restrict
 template <bool GAUSS, int L>
 __device__ __forceinline__ void delta_one(const PassB &a, const int4 *__restrict__ pos, int4 *pos_out, uint32_t j_raw,
                                           uint32_t n, uint32_t sub, bool packed, bool filter, const uint32_t *cnt_arr,
-                                          const uint32_t *idx_arr, uint32_t nboxes) {
+                                          const uint32_t *idx_arr, bool corr, uint32_t nboxes) {
     {
         const bool valid = j_raw < n;
         const uint32_t j = valid ? j_raw : 0u;
         const int4 p = pos[j];
-        const KConst cj = gauss_consts(packed ? a.kw[j] : 1.0f);
+        const float kwj = GAUSS ? a.kw[j] : 1.0f;
+        const KConst cj = gauss_consts(kwj);
         int32_t ax, ay, az;
         const uint32_t cnt = valid ? cnt_arr[j] : 0u;
         const uint32_t *row = idx_arr + j;
@@ -599,16 +659,23 @@ __device__ __forceinline__ void delta_one(const PassB &a, const int4 *__restrict
         const int4 shj = valid ? a.shift[j] : make_int4(0, 0, 0, 0);
         float3 ed = make_float3(0.f, 0.f, 0.f);
         bool fil = false, hit = false;  // this particle's deferred filter, and whether a neighbour cleared it
+        uint32_t fcnt = 0;              // the filter's entries: j's own neighbours, the row's prefix
         if (filter && shj.w != 0) {
             const int4 fj = a.filt[j];
             fil = filter_dir(fj.x, fj.y, fj.z, ed);
+            fcnt = a.count[j];
         }
         // the sums start from the self shift on the first lane: wrapping integer sums
         // are order-free, and the load is in flight with the particle's other data
         const int4 sh = sub == 0 ? shj : make_int4(0, 0, 0, 0);
         const float rj = a.radius[j];
-        int3 acc = packed ? delta_row<GAUSS, L, true>(a, pos, row, cnt, j, sub, p, cj, fil, ed, hit, sh)
-                          : delta_row<GAUSS, L, false>(a, pos, row, cnt, j, sub, p, cj, fil, ed, hit, sh);
+        int3 acc = packed ? delta_row<GAUSS, L, true>(a, pos, row, cnt, fcnt, j, sub, p, kwj, cj, fil, ed, hit, sh)
+                          : delta_row<GAUSS, L, false>(a, pos, row, cnt, fcnt, j, sub, p, kwj, cj, fil, ed, hit, sh);
+        if (corr) {  // the correction row (radii that differ): usually empty
+            const uint32_t m = valid ? a.rcount[j] : 0u;
+            if (m) acc = packed ? delta_corrections<GAUSS, L, true>(a, pos, m, j, sub, p, kwj, cj, acc)
+                                : delta_corrections<GAUSS, L, false>(a, pos, m, j, sub, p, kwj, cj, acc);
+        }
         ax = acc.x;
         ay = acc.y;
         az = acc.z;
@@ -676,18 +743,21 @@ __global__ void __launch_bounds__(256, 4) k_delta(PassB a) {
             delta_skip_copy(a, j);
         return;
     }
+    // Rows: symmetric (equal radii) or with correction rows (the green search with
+    // radii that differ): the particle's own row; transposed rows otherwise.
     const bool sym = a.st->range_min == a.st->range_max;
+    const bool corr = !sym && a.st->union_rows != 0u;
     // Equal kernel widths (same bits): every neighbour's Gauss constants are this
     // particle's, so one 16-byte record (position, applied lambda) per neighbour is
     // gathered instead of the solve record and the position.
     const bool packed = GAUSS && a.st->kw_uniform != 0u;
-    const uint32_t *cnt_arr = sym ? a.count : a.rcount;
-    const uint32_t *idx_arr = sym ? a.idx : a.ridx;
+    const uint32_t *cnt_arr = sym || corr ? a.count : a.rcount;
+    const uint32_t *idx_arr = sym || corr ? a.idx : a.ridx;
     const uint32_t sub = threadIdx.x % L;
     const uint32_t gpb = blockDim.x / L;
     for (uint32_t base = blockIdx.x * gpb; base < n; base += gridDim.x * gpb)
         delta_one<GAUSS, L>(a, a.pos, a.pos_out, base + threadIdx.x / L, n, sub, packed, filter, cnt_arr, idx_arr,
-                            nboxes);
+                            corr, nboxes);
 }
 
 // ---- the solve loop as one persistent cooperative kernel ----
@@ -761,16 +831,18 @@ __global__ void __launch_bounds__(256, 4) k_solve_loop(PassA a, PassB b, LoopArg
     uint32_t gen = *(volatile uint32_t *)&st->bar_gen;  // read before this block's first arrival
     const uint32_t n = a.d_len[kLenParticles];
     const bool sym = st->range_min == st->range_max;
-    // with symmetric rows the Gauss filter runs in the position phase (as k_density_lambda decides)
-    const bool defer = l.defer != 0 && sym;
+    const bool corr = !sym && st->union_rows != 0u;
+    // with symmetric rows or correction rows the Gauss filter runs in the position phase
+    // (as k_density_lambda decides)
+    const bool defer = l.defer != 0 && (sym || corr);
     const bool packed = GAUSS && st->kw_uniform != 0u;
-    const uint32_t *cnt_arr = sym ? b.count : b.rcount;
-    const uint32_t *idx_arr = sym ? b.idx : b.ridx;
+    const uint32_t *cnt_arr = sym || corr ? b.count : b.rcount;
+    const uint32_t *idx_arr = sym || corr ? b.idx : b.ridx;
     const uint32_t T = gridDim.x * blockDim.x, t0 = blockIdx.x * blockDim.x + threadIdx.x;
     int4 *cur = l.pos_a, *nxt = l.pos_b;
     for (uint32_t pass = l.first; pass < l.max_passes; ++pass) {
         PassSums ps;
-        for (uint32_t i = t0; i < n; i += T) density_one<GAUSS, 1, false>(a, cur, i, n, 0u, defer, !packed, ps);
+        for (uint32_t i = t0; i < n; i += T) density_one<GAUSS, 1, false>(a, cur, i, n, 0u, defer, !GAUSS, ps);
         const PassSums bs = block_pass_sums(ps);
         if (threadIdx.x == 0) {
             atomicAdd(&st->loop_e1, (unsigned long long)bs.e1);
@@ -788,7 +860,7 @@ __global__ void __launch_bounds__(256, 4) k_solve_loop(PassA a, PassB b, LoopArg
         }
         const uint32_t nb = pass + 1u < l.max_passes ? l.nboxes : 0u;
         for (uint32_t j = t0; j < n; j += T)
-            delta_one<GAUSS, 1>(b, cur, nxt, j, n, 0u, packed, defer, cnt_arr, idx_arr, nb);
+            delta_one<GAUSS, 1>(b, cur, nxt, j, n, 0u, packed, defer, cnt_arr, idx_arr, corr, nb);
         if (!grid_barrier(st, gen, nullptr, n)) return;
         int4 *t = cur;
         cur = nxt;
@@ -883,8 +955,9 @@ __global__ void __launch_bounds__(256, 4) k_solve_batch(const BatchScene *__rest
         const Status *st = b.a.st;
         s_n[sc] = b.a.d_len[kLenParticles];
         s_max[sc] = b.l.max_passes;
-        s_sym[sc] = st->range_min == st->range_max ? 1 : 0;
-        s_defer[sc] = (b.l.defer != 0 && s_sym[sc]) ? 1 : 0;
+        // rows: 1 symmetric, 2 own rows with correction rows, 0 transposed
+        s_sym[sc] = st->range_min == st->range_max ? 1 : (st->union_rows != 0u ? 2 : 0);
+        s_defer[sc] = (b.l.defer != 0 && s_sym[sc] != 0) ? 1 : 0;
         s_packed[sc] = st->kw_uniform != 0u ? 1 : 0;
         s_done[sc] = (b.a.early_exit && *(volatile const uint32_t *)&st->converged) ? 1 : 0;  // pass 0 met the target
         s_upd[sc] = 0;
@@ -924,7 +997,7 @@ __global__ void __launch_bounds__(256, 4) k_solve_batch(const BatchScene *__rest
             const int4 *cur = (s_upd[sc] & 1u) ? bs.l.pos_b : bs.l.pos_a;
             const uint32_t i = (u - s_unit[sc]) * blockDim.x + threadIdx.x;
             PassSums ps;
-            density_one<true, 1, false>(bs.a, cur, i, s_n[sc], 0u, s_defer[sc] != 0, !s_packed[sc], ps);
+            density_one<true, 1, false>(bs.a, cur, i, s_n[sc], 0u, s_defer[sc] != 0, false, ps);
             long long e1 = ps.e1, e2 = ps.e2;
             for (int off = 16; off > 0; off >>= 1) {
                 e1 += __shfl_down_sync(0xffffffffu, e1, off);
@@ -964,7 +1037,8 @@ __global__ void __launch_bounds__(256, 4) k_solve_batch(const BatchScene *__rest
             const uint32_t nb = pass + 1u < s_max[sc] ? bs.l.nboxes : 0u;
             const uint32_t *cnt_arr = s_sym[sc] ? b.count : b.rcount;
             const uint32_t *idx_arr = s_sym[sc] ? b.idx : b.ridx;
-            delta_one<true, 1>(b, cur, nxt, j, s_n[sc], 0u, s_packed[sc] != 0, s_defer[sc] != 0, cnt_arr, idx_arr, nb);
+            delta_one<true, 1>(b, cur, nxt, j, s_n[sc], 0u, s_packed[sc] != 0, s_defer[sc] != 0, cnt_arr, idx_arr,
+                               s_sym[sc] == 2, nb);
         }
         if (!batch_barrier(sy, gen, tab, S, acc, s_n, s_run, false)) return;
         for (uint32_t sc = threadIdx.x; sc < S; sc += blockDim.x) {
@@ -1060,7 +1134,6 @@ static PassA make_pass_a(apbf_ctx *ctx, const SolveOpts &o) {
     a.shift = ctx->shift;
     a.rec = ctx->solve_rec;
     a.pk = ctx->solve_pk;
-    a.rec_if_mixed = o.later_pass ? 1 : 0;
     a.dbg_dens = ctx->debug ? ctx->dbg_density : nullptr;
     a.dbg_grad = ctx->dbg_grad;
     a.dbg_sq = ctx->dbg_sq;

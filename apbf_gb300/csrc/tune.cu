@@ -44,10 +44,10 @@ extern "C" apbf_status apbf_set_tuning(apbf_ctx *ctx, const apbf_tuning *t) {
     const uint32_t l = t->gather_lanes;
     const uint32_t db = t->sort_digit_bits;
     if ((l != 1 && l != 2 && l != 4 && l != 8) || (t->pass_block != 128 && t->pass_block != 256) ||
-        t->pass_blocks_per_sm < 1 || t->pass_blocks_per_sm > 8 || t->build_tiled > 2 ||
+        t->pass_blocks_per_sm < 1 || t->pass_blocks_per_sm > 8 || t->reserved0 != 0 ||
         (db != 0 && (db < 6 || db > 8)) || t->search_log2res > ctx->cfg.max_log2res) {
         set_error("apbf_set_tuning: gather_lanes 1, 2, 4 or 8; pass_block 128 or 256; pass_blocks_per_sm 1..8; "
-                  "build_tiled 0, 1 or 2; sort_digit_bits 0, 6, 7 or 8; search_log2res 0..max_log2res");
+                  "reserved0 0; sort_digit_bits 0, 6, 7 or 8; search_log2res 0..max_log2res");
         return APBF_ERR_INVALID_ARG;
     }
     ctx->tuning = *t;

@@ -185,8 +185,7 @@ typedef struct apbf_tuning {
     uint32_t gather_lanes;        /* threads per particle in the density and position passes: 1, 2, 4 or 8 */
     uint32_t pass_block;          /* threads per block of those passes: 128 or 256 */
     uint32_t pass_blocks_per_sm;  /* their grid: up to this many blocks per SM (1..8) */
-    uint32_t build_tiled;         /* neighbour-row build: 0 one thread per particle, 1 blocks that stage
-                                     candidates in shared memory, 2 one warp per particle (same rows) */
+    uint32_t reserved0;           /* must be 0 */
     uint32_t filter_in_density;   /* 1: the boundariness filter always runs in the density pass (else, with
                                      symmetric rows and the Gauss kernel, in the position pass) */
     uint32_t sort_digit_bits;     /* radix sort digit width: 6, 7 or 8 bits per pass (0: 8); same order */
@@ -249,6 +248,19 @@ apbf_status apbf_set_boxes(apbf_ctx *ctx, const float *box_min4, const float *bo
 apbf_status apbf_fluid_get_view(apbf_ctx *ctx, apbf_fluid_view *out);
 apbf_status apbf_transfers_get_view(apbf_ctx *ctx, apbf_transfers_view *out);
 apbf_status apbf_neighbors_get_view(apbf_ctx *ctx, apbf_neighbors_view *out);
+/* The rows the position update gathers over besides the forward rows (no
+ * reference counterpart: the reference scatters with atomics,
+ * incompressibility_3.comp:62-66).  *union_rows (may be NULL; synchronises the
+ * stream) receives 2 when every search radius was equal (the forward rows are
+ * symmetric and serve alone; this view is unused), 1 for correction rows (the green
+ * search with radii that differ: particle i's update sums over its forward row and
+ * then over this row, whose entries with bit 31 set are entries j of i's forward
+ * row whose own radius does not reach i, subtracted again, and whose other entries
+ * are particles k whose forward rows hold i although i's radius does not reach k,
+ * added), 0 for transposed rows (row j lists every i whose forward row holds j; the
+ * forward rows are not used by the update). */
+apbf_status apbf_neighbors_get_reverse_view(apbf_ctx *ctx, apbf_neighbors_view *out, uint32_t *union_rows,
+                                            void *stream);
 /* gpu_list::set_length with a host value (source/gpu_list.h:85-90). */
 apbf_status apbf_set_lengths(apbf_ctx *ctx, uint32_t n_particles, uint32_t n_transfers, void *stream);
 /* Reads the device lengths (synchronises the stream). */

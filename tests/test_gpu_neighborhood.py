@@ -114,3 +114,55 @@ def test_neighbor_overflow_reports_required(orc):
     orc.neighborhood_green(fs, 1.0, spec.grid_min, spec.grid_max, spec.log2res, 1 << 22)
     assert info.required_neighbors == max(len(r) for r in fs.rows())
     ctx.close()
+
+
+def _pairs_sorted(count: np.ndarray, index: np.ndarray, mask: int = 0xFFFFFFFF) -> np.ndarray:
+    """(i << 32 | entry) keys of column-major rows, sorted."""
+    n = count.shape[0]
+    m = int(count.max()) if n else 0
+    idx = index[:m, :n].astype(np.int64) & mask
+    live = np.arange(m)[:, None] < count[None, :].astype(np.int64)
+    ii = np.broadcast_to(np.arange(n, dtype=np.int64)[None, :], (m, n))[live]
+    return np.sort((ii << 32) | idx[live])
+
+
+@pytest.mark.parametrize("seed,scale,L", [(4, 1.0, 4), (5, 1.5, 5), (6, 1.0, 3)])
+def test_correction_rows(seed, scale, L):
+    """With differing search radii the position update of particle i sums over i's own
+    row and then over i's correction row: entries flagged (bit 31) are the j of i's row
+    whose radius does not reach i (their terms are subtracted again), the others the k
+    whose rows hold i although i's radius does not reach k (added).  So own row minus
+    flagged plus added is exactly the transpose of the rows, the set the reference's
+    atomic scatter (incompressibility_3.comp:62-66) adds to i."""
+    from apbf_gb300.api import neighborhood_green
+
+    st = _random_scene(6000, seed, 2.0, 4.5)
+    n = st["position"].shape[0]
+    ctx = _ctx(n, maxn=512, L=max(L, 3))
+    ctx.upload(st)
+    neighborhood_green().set_data(ctx).set_range_scale(scale).set_position_range(GRID[0], GRID[1], L).apply()
+    ctx.check_status()
+    g, _ = ctx.download()
+    fw = ctx.neighbors_view()
+    rv = ctx.reverse_neighbors_view()
+    assert rv["kind"] == 1
+    fc = fw["count"][:n].cpu().numpy().astype(np.int64)
+    fi = fw["index"][:, :n].cpu().numpy().view(np.uint32).astype(np.int64)
+    cc = rv["count"][:n].cpu().numpy().astype(np.int64)
+    ci = rv["index"][:, :n].cpu().numpy().view(np.uint32).astype(np.int64)
+    fwd = _pairs_sorted(fc, fi)  # (i << 32 | j): j in i's row
+    flagged = _pairs_sorted(cc, ci) if n else fwd[:0]
+    sub_ = flagged[(flagged & 0x80000000) != 0] & ~np.int64(0x80000000)
+    add = flagged[(flagged & 0x80000000) == 0]
+    # the flagged entries are exactly the one-sided pairs of the rows
+    R = np.floor(g["kernel_width"].astype(np.float64) * np.float64(np.float32(scale)) * 262144.0).astype(np.int64)
+    pos = g["position"][:, :3].astype(np.int64)
+    i_, j_ = fwd >> 32, fwd & 0xFFFFFFFF
+    one_sided = np.sum((pos[j_] - pos[i_]) ** 2, axis=1) > R[j_] * R[j_]
+    assert np.array_equal(np.sort(sub_), np.sort(fwd[one_sided]))
+    assert one_sided.any(), "the scene should have one-sided pairs"
+    # own row - subtracted + added == transpose of the rows, as multisets
+    transpose = np.sort(((fwd & 0xFFFFFFFF) << 32) | (fwd >> 32))
+    delta = np.sort(np.concatenate([np.setdiff1d(fwd, sub_, assume_unique=True), add]))
+    assert np.array_equal(delta, transpose)
+    ctx.close()

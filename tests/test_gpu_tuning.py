@@ -31,7 +31,7 @@ def test_gather_lanes_bit_identical(name):
         ctx = _ctx(spec, 5, maxn=maxn)
         ctx.set_tuning(gather_lanes=lanes, pass_block=block, pass_blocks_per_sm=per_sm)
         assert ctx.tuning() == {"gather_lanes": lanes, "pass_block": block, "pass_blocks_per_sm": per_sm,
-                                "build_tiled": 0, "filter_in_density": 0, "sort_digit_bits": 0, "search_log2res": 0}
+                                "filter_in_density": 0, "sort_digit_bits": 0, "search_log2res": 0}
         for _ in range(8):
             ctx.substep(spec.dt)
         ctx.check_status()
@@ -78,53 +78,10 @@ def test_set_tuning_rejects_bad_shapes():
 
     spec = scenes.dam_break(n_side=8)
     ctx = _ctx(spec, 2)
-    for bad in (dict(gather_lanes=3), dict(pass_block=192), dict(pass_blocks_per_sm=0), dict(pass_blocks_per_sm=9),
-                dict(build_tiled=3)):
+    for bad in (dict(gather_lanes=3), dict(pass_block=192), dict(pass_blocks_per_sm=0), dict(pass_blocks_per_sm=9)):
         with pytest.raises(ApbfError):
             ctx.set_tuning(**bad)
     ctx.close()
-
-
-@pytest.mark.parametrize("name", ["dam_break", "water_drop_adaptive", "outside_grid"])
-def test_tiled_build_identical_rows(name):
-    """Neighbour rows built by shared-memory tiles and by a warp per particle equal
-    the per-thread walk's, entry for entry, and so do whole substeps."""
-    if name == "dam_break":
-        spec, maxn = scenes.dam_break(n_side=18), 128
-    elif name == "water_drop_adaptive":
-        spec, maxn = scenes.water_drop(total=20_000, seed=6, basic_pbf=False), 256
-    else:  # a block partly outside the search grid: clamped cells, the 64-bit predicate
-        from dataclasses import replace
-
-        spec = scenes.dam_break(n_side=14, seed=3)
-        st = {k: v.copy() for k, v in spec.state.items()}
-        st["position"][:, 0] -= np.int32(20 * 262144)
-        spec = replace(spec, state=st, box_min=np.zeros((0, 4), np.float32), box_max=np.zeros((0, 4), np.float32))
-        maxn = 160
-    out = []
-    for tiled in (0, 1, 2):
-        ctx = _ctx(spec, 4, maxn=maxn)
-        ctx.set_tuning(build_tiled=tiled)
-        rows = []
-        for _ in range(5):
-            ctx.substep(spec.dt)
-            n, _ = ctx.lengths()
-            nb = ctx.neighbors_view()
-            cnt = nb["count"][:n].cpu().numpy().copy()
-            idx = nb["index"][:, :n].cpu().numpy().copy()
-            rows.append((cnt, idx))
-        ctx.check_status()
-        out.append((rows, ctx.download()[0]))
-        ctx.close()
-    ra, sa = out[0]
-    for rb, sb in out[1:]:
-        for (ca, ia), (cb, ib) in zip(ra, rb):
-            assert np.array_equal(ca, cb)
-            for k in range(int(ca.max())):
-                live = ca > k
-                assert np.array_equal(ia[k][live], ib[k][live]), k
-        for k in sa:
-            assert np.array_equal(sa[k], sb[k]), k
 
 
 @pytest.mark.parametrize("lanes", [1, 4])
