@@ -226,18 +226,25 @@ __device__ __forceinline__ void density_one(const PassA &a, const int4 *__restri
         const float4 vi = feat ? a.vel[i] : make_float4(0.f, 0.f, 0.f, 0.f);
         float div = 0.0f;  // sum_j m_j (v_j - v_i) . gradW_ij  (velocity divergence x density)
         float nprev = 0.0f;  // sum_j lambda_prev_j (the neighbours' previous-substep lambda sums)
-        // Batches of kUnroll pairs per lane: all row entries, then all neighbour
-        // gathers, then the arithmetic, so each lane keeps kUnroll loads in flight.
-        for (uint32_t k0 = sub; k0 < cnt; k0 += L * kUnroll) {
-            uint32_t jj[kUnroll];
-            int4 qq[kUnroll];
+        // Batches of kUnroll pairs per lane, software-pipelined: the neighbour gathers
+        // of a batch go out with the row entries of the next, then the arithmetic, so
+        // a batch costs one memory latency instead of two.
+        uint32_t jj[kUnroll];
 #pragma unroll
-            for (int u = 0; u < kUnroll; ++u) {
-                const uint32_t k = k0 + u * L;
-                jj[u] = k < cnt ? row[(size_t)k * a.stride] : i;
-            }
+        for (int u = 0; u < kUnroll; ++u) {
+            const uint32_t k = sub + u * L;
+            jj[u] = k < cnt ? row[(size_t)k * a.stride] : i;
+        }
+        for (uint32_t k0 = sub; k0 < cnt; k0 += L * kUnroll) {
+            int4 qq[kUnroll];
+            uint32_t jn[kUnroll];
 #pragma unroll
             for (int u = 0; u < kUnroll; ++u) qq[u] = pos[jj[u]];
+#pragma unroll
+            for (int u = 0; u < kUnroll; ++u) {
+                const uint32_t k = k0 + (L * kUnroll) + u * L;
+                jn[u] = k < cnt ? row[(size_t)k * a.stride] : i;
+            }
 #pragma unroll
             for (int u = 0; u < kUnroll; ++u) {
                 if (k0 + u * L >= cnt) break;
@@ -266,6 +273,8 @@ __device__ __forceinline__ void density_one(const PassA &a, const int4 *__restri
                     cw = wadd(cw, f2i(mjf));
                 }
             }
+#pragma unroll
+            for (int u = 0; u < kUnroll; ++u) jj[u] = jn[u];
         }
         if (L > 1) {
             dens = group_sum<L>(dens);
@@ -563,16 +572,19 @@ __device__ __forceinline__ int3 delta_row(const PassB &a, const int4 *__restrict
                                           uint32_t fcnt, uint32_t j, uint32_t sub, int4 p, float kwj, KConst cj,
                                           bool fil, float3 ed, bool &hit, int4 start) {
     int32_t ax = start.x, ay = start.y, az = start.z;
+    // software-pipelined as in density_one: the gathers of a batch go out with the
+    // row entries of the next
+    uint32_t ii[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) {
+        const uint32_t k = sub + u * L;
+        ii[u] = k < cnt ? row[(size_t)k * a.stride] : j;
+    }
     for (uint32_t k0 = sub; k0 < cnt; k0 += L * kUnroll) {
-        uint32_t ii[kUnroll];
         float4 rr[kUnroll];
         int4 qq[kUnroll];
         float kk[kUnroll];
-#pragma unroll
-        for (int u = 0; u < kUnroll; ++u) {
-            const uint32_t k = k0 + u * L;
-            ii[u] = k < cnt ? row[(size_t)k * a.stride] : j;
-        }
+        uint32_t in_[kUnroll];
 #pragma unroll
         for (int u = 0; u < kUnroll; ++u) {
             if (PACKED) {
@@ -587,6 +599,11 @@ __device__ __forceinline__ int3 delta_row(const PassB &a, const int4 *__restrict
         }
 #pragma unroll
         for (int u = 0; u < kUnroll; ++u) {
+            const uint32_t k = k0 + (L * kUnroll) + u * L;
+            in_[u] = k < cnt ? row[(size_t)k * a.stride] : j;
+        }
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) {
             if (fil && !hit && k0 + u * L < fcnt) {
                 const float3 dn = fdiff(qq[u], p);  // x_i - x_j ...
                 hit = gauss_filter_hit(ed, make_float3(-dn.x, -dn.y, -dn.z));  // ... as the offset x_j - x_i
@@ -598,6 +615,8 @@ __device__ __forceinline__ int3 delta_row(const PassB &a, const int4 *__restrict
             ay = wadd(ay, t.y);
             az = wadd(az, t.z);
         }
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) ii[u] = in_[u];
     }
     return make_int3(ax, ay, az);
 }
