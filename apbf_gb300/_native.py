@@ -141,6 +141,8 @@ class StatusInfo(C.Structure):
         ("pairs", C.c_ulonglong),
         ("density_passes", C.c_uint32),
         ("converged_substeps", C.c_uint32),
+        ("spin_where", C.c_uint32),
+        ("reserved", C.c_uint32),
     ]
 
 
@@ -180,6 +182,7 @@ SIGNATURES = {
     "apbf_fluid_get_view": (_ST, [_P, C.POINTER(FluidView)]),
     "apbf_transfers_get_view": (_ST, [_P, C.POINTER(TransfersView)]),
     "apbf_neighbors_get_view": (_ST, [_P, C.POINTER(NeighborsView)]),
+    "apbf_set_wait_limit": (_ST, [_P, C.c_uint32, C.c_int]),
     "apbf_neighbors_get_reverse_view": (_ST, [_P, C.POINTER(NeighborsView), C.POINTER(C.c_uint32), _P]),
     "apbf_set_lengths": (_ST, [_P, C.c_uint32, C.c_uint32, _P]),
     "apbf_get_lengths": (_ST, [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), _P]),

@@ -168,6 +168,11 @@ class Context:
         N.check(self.lib.apbf_save_particle_info(self.handle, str(folder).encode(), (C.c_float * 3)(*center),
                                                  _stream_handle(stream)), "apbf_save_particle_info")
 
+    def set_wait_limit(self, limit: int = 0, inject: bool = False) -> None:
+        """apbf_set_wait_limit: spins of the device-side waits before they give up (0:
+        defaults); inject makes every wait run out (failure-path tests)."""
+        N.check(self.lib.apbf_set_wait_limit(self.handle, limit, 1 if inject else 0), "apbf_set_wait_limit")
+
     def set_debug(self, enable: bool) -> None:
         N.check(self.lib.apbf_set_debug(self.handle, 1 if enable else 0), "apbf_set_debug")
 

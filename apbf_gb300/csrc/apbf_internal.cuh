@@ -71,6 +71,8 @@ struct Status {
     uint32_t loop_iters;           // solve loop graph: body runs since the context was created
     uint32_t filter_tag;           // 1: this pass's density kernel left the boundariness filter to k_delta
     uint32_t union_rows;           // 1: the reverse-row arrays hold correction rows (see neighborhood.cu)
+    uint32_t wait_limit;           // spins of a bounded device wait before it gives up (0: the wait's default);
+                                   // bit 31: the waits treat their awaited flag as never set (failure tests)
     uint32_t kw_uniform;           // 1: every kernel width of this density pass had the same bits
     uint32_t bar_arrive;           // persistent solve: blocks arrived at the current grid barrier
     uint32_t bar_gen;              // persistent solve: grid barriers released so far
@@ -428,6 +430,16 @@ __device__ __forceinline__ uint32_t f2u(float x) { return __float2uint_rz(x); }
 __device__ __forceinline__ int32_t wadd(int32_t a, int32_t b) { return (int32_t)((uint32_t)a + (uint32_t)b); }
 
 __device__ __forceinline__ void set_flag(Status *st, uint32_t f) { atomicOr(&st->flags, f); }
+
+// Spin bound of a bounded wait and whether the wait ignores its flag (set by
+// apbf_set_wait_limit to test the failure path without a fault or a hang).
+constexpr uint32_t kWaitInject = 0x80000000u;
+__device__ __forceinline__ uint32_t wait_limit(const Status *st, uint32_t dflt, bool &inject) {
+    const uint32_t v = *(volatile const uint32_t *)&st->wait_limit;
+    inject = (v & kWaitInject) != 0u;
+    const uint32_t l = v & ~kWaitInject;
+    return l ? l : dflt;
+}
 
 // Bits of a 10-bit value spread to every third bit (Morton interleave).
 __device__ __host__ __forceinline__ uint32_t spread3(uint32_t x) {

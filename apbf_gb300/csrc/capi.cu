@@ -747,6 +747,17 @@ apbf_status apbf_reduce_fp64(apbf_ctx *ctx, double out[4], void *stream) {
     return reduce_fp64(ctx, out, (cudaStream_t)stream);
 }
 
+apbf_status apbf_set_wait_limit(apbf_ctx *ctx, uint32_t limit, int inject) {
+    if (!ctx || (limit & kWaitInject)) {
+        set_error("apbf_set_wait_limit: limit must be below 2^31");
+        return APBF_ERR_INVALID_ARG;
+    }
+    const uint32_t v = limit | (inject ? kWaitInject : 0u);
+    APBF_CUDA(cudaSetDevice(ctx->device));
+    APBF_CUDA(cudaMemcpy(&ctx->status->wait_limit, &v, sizeof(v), cudaMemcpyHostToDevice));
+    return APBF_OK;
+}
+
 apbf_status apbf_get_status(apbf_ctx *ctx, apbf_status_info *out, int clear, void *stream) {
     if (!ctx || !out) return APBF_ERR_INVALID_ARG;
     cudaStream_t s = (cudaStream_t)stream;
@@ -762,6 +773,8 @@ apbf_status apbf_get_status(apbf_ctx *ctx, apbf_status_info *out, int clear, voi
     out->pairs = pairs;
     out->density_passes = hs.density_passes;
     out->converged_substeps = hs.converged_substeps;
+    out->spin_where = hs.spin_where;
+    out->reserved = 0;
     if (clear) {
         Status z = hs;
         z.flags = 0;

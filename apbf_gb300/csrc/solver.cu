@@ -817,8 +817,10 @@ __device__ __forceinline__ bool grid_barrier(Status *st, uint32_t &gen, const Pa
             atomicAdd(&st->bar_gen, 1u);  // release
         } else {
             uint32_t spins = 0;
-            while (*(volatile uint32_t *)&st->bar_gen == gen) {
-                if (++spins > kBarrierSpins) {
+            bool inject;
+            const uint32_t limit = wait_limit(st, kBarrierSpins, inject);
+            while (inject || *(volatile uint32_t *)&st->bar_gen == gen) {
+                if (++spins > limit) {
                     set_flag(st, APBF_FLAG_SPIN_LIMIT);
                     st->spin_where = 3u;
                     ok = 0u;
@@ -939,9 +941,14 @@ __device__ __forceinline__ bool batch_barrier(BatchSync *sy, uint32_t &gen, cons
         }
     } else if (threadIdx.x == 0) {
         uint32_t spins = 0;
-        while (*(volatile uint32_t *)&sy->bar_gen == gen) {
-            if (++spins > kBarrierSpins) {
-                for (uint32_t sc = 0; sc < S; ++sc) set_flag(tab[sc].a.st, APBF_FLAG_SPIN_LIMIT);
+        bool inject;
+        const uint32_t limit = wait_limit(tab[0].a.st, kBarrierSpins, inject);
+        while (inject || *(volatile uint32_t *)&sy->bar_gen == gen) {
+            if (++spins > limit) {
+                for (uint32_t sc = 0; sc < S; ++sc) {
+                    set_flag(tab[sc].a.st, APBF_FLAG_SPIN_LIMIT);
+                    tab[sc].a.st->spin_where = 4u;
+                }
                 s_ok = 0u;
                 break;
             }

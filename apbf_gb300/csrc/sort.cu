@@ -131,11 +131,13 @@ __global__ void __launch_bounds__(256) k_onesweep(const uint32_t *__restrict__ k
         st_volatile(my, kFlagAgg | run);
         int j = (int)tile - 1;
         uint32_t spins = 0;
+        bool inject;
+        const uint32_t limit = wait_limit(st, kSpinLimit, inject);
         while (j >= 0) {
             uint32_t v = ld_volatile(tile_status + (size_t)j * NB + t);
-            uint32_t f = v & ~kValMask;
+            uint32_t f = inject ? 0u : (v & ~kValMask);
             if (f == 0u) {
-                if (++spins > kSpinLimit) {
+                if (++spins > limit) {
                     set_flag(st, APBF_FLAG_SPIN_LIMIT);
                     st->spin_where = 1u;
                     break;
@@ -218,11 +220,13 @@ __global__ void __launch_bounds__(256) k_scan(uint32_t *data, const uint32_t *d_
                 st_volatile(my, kFlagAgg | (total & kValMask));
                 int j = (int)tile - 1;
                 uint32_t spins = 0;
+                bool inject;
+                const uint32_t limit = wait_limit(st, kSpinLimit, inject);
                 while (j >= 0) {
                     uint32_t s = ld_volatile(tile_status + j);
-                    uint32_t f = s & ~kValMask;
+                    uint32_t f = inject ? 0u : (s & ~kValMask);
                     if (f == 0u) {
-                        if (++spins > kSpinLimit) {
+                        if (++spins > limit) {
                             set_flag(st, APBF_FLAG_SPIN_LIMIT);
                             st->spin_where = 2u;
                             break;
@@ -410,9 +414,17 @@ extern "C" apbf_status apbf_sort_pairs_noalloc(const uint32_t *d_keys, const uin
         set_error("apbf_sort_pairs_noalloc: max_count above the fixed scratch size of 1048576 elements");
         return APBF_ERR_INVALID_ARG;
     }
-    if (d_keys == d_out_keys || d_keys == d_out_values || d_values == d_out_keys || d_values == d_out_values) {
-        set_error("apbf_sort_pairs_noalloc: inputs must not alias outputs");
-        return APBF_ERR_INVALID_ARG;
+    {  // each output range [p, p + 4 max_count) must overlap no other buffer's range
+        const uintptr_t bytes = (uintptr_t)max_count * 4u;
+        auto overlap = [bytes](const void *x, const void *y) {
+            const uintptr_t a = (uintptr_t)x, b = (uintptr_t)y;
+            return bytes != 0 && a < b + bytes && b < a + bytes;
+        };
+        if (overlap(d_out_keys, d_out_values) || overlap(d_out_keys, d_keys) || overlap(d_out_keys, d_values) ||
+            overlap(d_out_values, d_keys) || overlap(d_out_values, d_values)) {
+            set_error("apbf_sort_pairs_noalloc: an output overlaps an input or the other output");
+            return APBF_ERR_INVALID_ARG;
+        }
     }
     if (max_count == 0) return APBF_OK;
     int dev = 0;

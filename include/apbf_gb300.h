@@ -176,6 +176,9 @@ typedef struct apbf_status_info {
     unsigned long long pairs;    /* pairs of the last neighbourhood search */
     uint32_t density_passes;     /* density passes executed since the status was last cleared */
     uint32_t converged_substeps; /* substeps whose density error met density_error_target, same period */
+    uint32_t spin_where;         /* with APBF_ERR_SPIN_LIMIT: the wait that gave up: 1 sort look-back, 2 scan
+                                    look-back, 3 persistent-solve grid barrier, 4 batched-solve grid barrier */
+    uint32_t reserved;
 } apbf_status_info;
 
 /* Launch shapes of the context's kernels (no reference counterpart: the
@@ -336,6 +339,16 @@ apbf_status apbf_export_pairs(apbf_ctx *ctx, uint32_t *d_pairs, uint32_t capacit
  * intermediates read by apbf_debug_incompressibility (costs 24 bytes per particle
  * of extra writes per iteration). */
 apbf_status apbf_set_debug(apbf_ctx *ctx, int enable);
+/* Bound of the context's device-side waits (no reference counterpart: the reference
+ * has no cross-block waits): the decoupled look-backs of its sorts and scans and the
+ * grid barriers of its persistent solves spin at most `limit` times (0: their
+ * defaults, about 2^22) before giving up, setting APBF_FLAG_SPIN_LIMIT and returning,
+ * so that apbf_get_status reports APBF_ERR_SPIN_LIMIT and the context stays usable.
+ * inject != 0 makes every such wait treat the flag it waits for as never set, so each
+ * wait runs out: a way to test the failure path without a fault or a hang.  Results
+ * computed while a wait gave up are wrong (every index stays in bounds).  Synchronous;
+ * not during stream capture. */
+apbf_status apbf_set_wait_limit(apbf_ctx *ctx, uint32_t limit, int inject);
 /* Graph use of apbf_substep (no counterpart in the reference):
  *   0  one launch per kernel, one launch pair per possible Jacobi pass;
  *   1  (default) Jacobi passes 1.. as one CUDA graph launch whose while loop ends
@@ -538,12 +551,16 @@ apbf_status apbf_sort_pairs(apbf_ctx *ctx, const uint32_t *d_keys, const uint32_
  * and per-frame code on which cudaMalloc / cudaFree would synchronise the device.
  * Its scratch is one fixed array in the library's device memory, held on every
  * device that loads the library until the process exits; max_count above
- * 1048576 (1 << 20) is rejected with APBF_ERR_INVALID_ARG, as are inputs that
- * alias outputs.  The first call on a device looks up that array's address on the
- * current device; make that first call before any stream capture.  All calls
- * share the array: calls whose work overlaps on the GPU (other streams, other
- * threads) race and must be serialised by the caller.  A bounded look-back wait
- * that gives up (which does not happen in normal operation) is not reported. */
+ * 1048576 (1 << 20) is rejected with APBF_ERR_INVALID_ARG, as are outputs that
+ * overlap an input or each other (each buffer taken as max_count words).  The
+ * first call on a device looks up that array's address on the current device and
+ * keeps it for the life of the process; make that first call before any stream
+ * capture, and do not use the entry point after cudaDeviceReset in the same
+ * process (the module may then be loaded at another address).  All calls share
+ * the array: calls whose work overlaps on the GPU (other streams, other threads)
+ * race and must be serialised by the caller.  A bounded look-back wait that gives
+ * up (which does not happen in normal operation) leaves the output out of order
+ * and cannot be detected by the caller. */
 apbf_status apbf_sort_pairs_noalloc(const uint32_t *d_keys, const uint32_t *d_values, const uint32_t *d_count,
                                     uint32_t max_count, uint32_t value_upper_bound, uint32_t *d_out_keys,
                                     uint32_t *d_out_values, void *stream);

@@ -7,7 +7,7 @@ and expected outputs of each known-answer test, and writes
 tests/golden/reference_known_answers.json.  The tests only read the JSON (the
 reference checkout is not available where the GPU tests run).
 
-Usage: python tests/golden/make_golden.py [path/to/reference]
+Usage: python tests/golden/make_golden.py path/to/reference
 """
 from __future__ import annotations
 
@@ -73,4 +73,6 @@ def main(ref: Path) -> None:
 
 
 if __name__ == "__main__":
-    main(Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference"))
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path of the APBF reference checkout>")
+    main(Path(sys.argv[1]))

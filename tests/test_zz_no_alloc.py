@@ -64,3 +64,22 @@ def test_noalloc_sort_rejects_oversize(native_lib, cuda):
                                             C.c_void_p(r.data_ptr()), None)
     assert st == 1
     assert b"1048576" in native_lib.apbf_last_error()
+
+
+def test_noalloc_sort_rejects_overlapping_outputs(native_lib, cuda):
+    """Outputs that are the same buffer, or overlap an input or each other by part of
+    their length, are rejected before any work is queued."""
+    buf = torch.zeros(64, dtype=torch.int32, device="cuda")
+    base = buf.data_ptr()
+    cnt = torch.tensor([16], dtype=torch.int32, device="cuda")
+    keys = torch.zeros(16, dtype=torch.int32, device="cuda")
+    vals = torch.zeros(16, dtype=torch.int32, device="cuda")
+
+    def call(out_k, out_v, k=keys.data_ptr(), v=vals.data_ptr()):
+        return native_lib.apbf_sort_pairs_noalloc(C.c_void_p(k), C.c_void_p(v), C.c_void_p(cnt.data_ptr()), 16,
+                                                  255, C.c_void_p(out_k), C.c_void_p(out_v), None)
+
+    assert call(base, base) == 1                       # the two outputs are one buffer
+    assert call(base, base + 8 * 4) == 1               # they overlap by half
+    assert call(base, base + 32 * 4, k=base + 4) == 1  # the keys overlap the key output
+    assert b"overlaps" in native_lib.apbf_last_error()
