@@ -183,6 +183,8 @@ SIGNATURES = {
     "apbf_transfers_get_view": (_ST, [_P, C.POINTER(TransfersView)]),
     "apbf_neighbors_get_view": (_ST, [_P, C.POINTER(NeighborsView)]),
     "apbf_set_wait_limit": (_ST, [_P, C.c_uint32, C.c_int]),
+    "apbf_bind_lists": (_ST, [_P, C.POINTER(FluidView), C.POINTER(TransfersView), C.POINTER(NeighborsView)]),
+    "apbf_unbind_lists": (_ST, [_P]),
     "apbf_neighbors_get_reverse_view": (_ST, [_P, C.POINTER(NeighborsView), C.POINTER(C.c_uint32), _P]),
     "apbf_set_lengths": (_ST, [_P, C.c_uint32, C.c_uint32, _P]),
     "apbf_get_lengths": (_ST, [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), _P]),

@@ -73,6 +73,37 @@ FLUID_FIELDS = {
 }
 
 
+@dataclass
+class CallerLists:
+    """Device lists owned by the caller (torch tensors), for Context.bind_lists: two
+    buffer sets of the particle lists and of the transfer list, one length word per
+    list, and the neighbour rows (column-major, row_stride as the context reports)."""
+
+    capacity: int
+    transfer_capacity: int
+    row_stride: int
+    max_neighbors: int
+    device: int = 0
+
+    def __post_init__(self):
+        dev = f"cuda:{self.device}"
+        self.fluid = [{name: torch.zeros((self.capacity, comps) if comps > 1 else (self.capacity,), dtype=dt,
+                                         device=dev) for name, (dt, comps) in FLUID_FIELDS.items()} for _ in range(2)]
+        self.transfers = [{"source": torch.zeros(self.transfer_capacity, dtype=torch.int32, device=dev),
+                           "target": torch.zeros(self.transfer_capacity, dtype=torch.int32, device=dev),
+                           "time_left": torch.zeros(self.transfer_capacity, dtype=torch.float32, device=dev)}
+                          for _ in range(2)]
+        self.len_particles = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.len_transfers = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.count = torch.zeros(self.capacity, dtype=torch.int32, device=dev)
+        self.index = torch.zeros((self.max_neighbors, self.row_stride), dtype=torch.int32, device=dev)
+
+    @classmethod
+    def for_context(cls, ctx: "Context") -> "CallerLists":
+        return cls(ctx.capacity, ctx.transfer_capacity, ctx.neighbors_view()["row_stride"], ctx.max_neighbors,
+                   ctx.device)
+
+
 class Context:
     """One apbf_ctx: the device lists of one scene plus the solver's scratch memory."""
 
@@ -167,6 +198,25 @@ class Context:
         """save_particle_info::apply: the reference's particle-info text files in `folder`."""
         N.check(self.lib.apbf_save_particle_info(self.handle, str(folder).encode(), (C.c_float * 3)(*center),
                                                  _stream_handle(stream)), "apbf_save_particle_info")
+
+    def bind_lists(self, lists: "CallerLists") -> None:
+        """apbf_bind_lists: the stages run on the caller's device lists from now on."""
+        fv = (N.FluidView * 2)()
+        tv = (N.TransfersView * 2)()
+        for k in range(2):
+            f, t = lists.fluid[k], lists.transfers[k]
+            fv[k] = N.FluidView(lists.capacity, lists.len_particles.data_ptr(),
+                                *[f[name].data_ptr() for name in FLUID_FIELDS])
+            tv[k] = N.TransfersView(lists.transfer_capacity, lists.len_transfers.data_ptr(), t["source"].data_ptr(),
+                                    t["target"].data_ptr(), t["time_left"].data_ptr())
+        nv = N.NeighborsView(lists.row_stride, lists.max_neighbors, lists.count.data_ptr(), lists.index.data_ptr(),
+                             None)
+        N.check(self.lib.apbf_bind_lists(self.handle, fv, tv, C.byref(nv)), "apbf_bind_lists")
+        self.bound = lists
+
+    def unbind_lists(self) -> None:
+        N.check(self.lib.apbf_unbind_lists(self.handle), "apbf_unbind_lists")
+        self.bound = None
 
     def set_wait_limit(self, limit: int = 0, inject: bool = False) -> None:
         """apbf_set_wait_limit: spins of the device-side waits before they give up (0:

@@ -271,6 +271,14 @@ struct apbf_ctx {
     unsigned long long loop_launches_per_iter = 0;  // kernel nodes per body run
     apbf::SubstepGraph substep_graphs[apbf::kSubstepGraphs];
     int substep_graph_next = 0;
+
+    // caller-owned lists (apbf_bind_lists): the context's own buffers while bound, and
+    // the caller's length words
+    bool bound = false;
+    apbf::FluidBufs own_fl[2];
+    apbf::TransferBufs own_tr[2];
+    uint32_t *own_nb_count = nullptr, *own_nb_idx = nullptr;
+    uint32_t *ext_len_particles = nullptr, *ext_len_transfers = nullptr;
 };
 
 namespace apbf {
@@ -316,6 +324,32 @@ inline void after_launch(apbf_ctx *c, cudaStream_t s) {
         cudaError_t _e = cudaGetLastError();                         \
         if (_e != cudaSuccess) return apbf::cuda_check(_e, what);    \
     } while (0)
+
+// While the caller's lists are bound (apbf_bind_lists), a stage call copies the
+// caller's length words into the context's length block before its work and back
+// after it, stream-ordered: the kernels read every length from that one block.
+struct BoundLengths {
+    apbf_ctx *c;
+    cudaStream_t s;
+    apbf_status status = APBF_OK;
+    BoundLengths(apbf_ctx *ctx, cudaStream_t stream) : c(ctx), s(stream) {
+        if (!c || !c->bound) return;
+        cudaError_t e = cudaMemcpyAsync(c->d_len + kLenParticles, c->ext_len_particles, sizeof(uint32_t),
+                                        cudaMemcpyDeviceToDevice, s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(c->d_len + kLenTransfers, c->ext_len_transfers, sizeof(uint32_t),
+                                cudaMemcpyDeviceToDevice, s);
+        if (e != cudaSuccess) status = cuda_check(e, "copy of the bound lists' lengths");
+    }
+    ~BoundLengths() {
+        if (!c || !c->bound || status != APBF_OK) return;
+        cudaMemcpyAsync(c->ext_len_particles, c->d_len + kLenParticles, sizeof(uint32_t), cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(c->ext_len_transfers, c->d_len + kLenTransfers, sizeof(uint32_t), cudaMemcpyDeviceToDevice, s);
+    }
+};
+#define APBF_BOUND_LENGTHS(ctx, stream)                          \
+    apbf::BoundLengths _bound_lengths((ctx), (stream));          \
+    if (_bound_lengths.status != APBF_OK) return _bound_lengths.status
 
 inline int grid_for(const apbf_ctx *ctx, uint32_t n, int block = kBlock, int per_sm = 8) {
     uint64_t need = ((uint64_t)n + block - 1) / block;

@@ -449,7 +449,7 @@ apbf_status apbf_fluid_get_view(apbf_ctx *ctx, apbf_fluid_view *o) {
     if (!ctx || !o) return APBF_ERR_INVALID_ARG;
     const FluidBufs &f = ctx->fl[ctx->fcur];
     o->capacity = ctx->cfg.particle_capacity;
-    o->d_length = ctx->d_len + kLenParticles;
+    o->d_length = ctx->bound ? ctx->ext_len_particles : ctx->d_len + kLenParticles;
     o->position = (int32_t *)f.pos;
     o->velocity = (float *)f.vel;
     o->inverse_mass = f.inv_mass;
@@ -467,7 +467,7 @@ apbf_status apbf_transfers_get_view(apbf_ctx *ctx, apbf_transfers_view *o) {
     if (!ctx || !o) return APBF_ERR_INVALID_ARG;
     const TransferBufs &t = ctx->tr[ctx->tcur];
     o->capacity = ctx->cfg.transfer_capacity;
-    o->d_length = ctx->d_len + kLenTransfers;
+    o->d_length = ctx->bound ? ctx->ext_len_transfers : ctx->d_len + kLenTransfers;
     o->source = t.source;
     o->target = t.target;
     o->time_left = t.time_left;
@@ -510,6 +510,10 @@ apbf_status apbf_set_lengths(apbf_ctx *ctx, uint32_t np, uint32_t nt, void *stre
     uint32_t v[2] = {np, nt};
     cudaStream_t s = (cudaStream_t)stream;
     APBF_CUDA(cudaMemcpyAsync(ctx->d_len, v, sizeof(v), cudaMemcpyHostToDevice, s));
+    if (ctx->bound) {
+        APBF_CUDA(cudaMemcpyAsync(ctx->ext_len_particles, ctx->d_len + kLenParticles, 4, cudaMemcpyDeviceToDevice, s));
+        APBF_CUDA(cudaMemcpyAsync(ctx->ext_len_transfers, ctx->d_len + kLenTransfers, 4, cudaMemcpyDeviceToDevice, s));
+    }
     // a new state has no lambda history (the warm start's previous-substep feature)
     APBF_CUDA(cudaMemsetAsync(ctx->fl[ctx->fcur].lambda_prev, 0, (size_t)ctx->cfg.particle_capacity * sizeof(float), s));
     APBF_CUDA(cudaStreamSynchronize(s));
@@ -560,7 +564,12 @@ apbf_status apbf_get_lengths(apbf_ctx *ctx, uint32_t *np, uint32_t *nt, void *st
     if (!ctx) return APBF_ERR_INVALID_ARG;
     uint32_t v[2];
     cudaStream_t s = (cudaStream_t)stream;
-    APBF_CUDA(cudaMemcpyAsync(v, ctx->d_len, sizeof(v), cudaMemcpyDeviceToHost, s));
+    if (ctx->bound) {
+        APBF_CUDA(cudaMemcpyAsync(v, ctx->ext_len_particles, 4, cudaMemcpyDeviceToHost, s));
+        APBF_CUDA(cudaMemcpyAsync(v + 1, ctx->ext_len_transfers, 4, cudaMemcpyDeviceToHost, s));
+    } else {
+        APBF_CUDA(cudaMemcpyAsync(v, ctx->d_len, sizeof(v), cudaMemcpyDeviceToHost, s));
+    }
     APBF_CUDA(cudaStreamSynchronize(s));
     if (np) *np = v[0];
     if (nt) *nt = v[1];
@@ -569,42 +578,50 @@ apbf_status apbf_get_lengths(apbf_ctx *ctx, uint32_t *np, uint32_t *nt, void *st
 
 apbf_status apbf_velocity_handling_apply(apbf_ctx *ctx, float dt, const float acc[3], void *stream) {
     if (!ctx || !acc) return APBF_ERR_INVALID_ARG;
+    APBF_BOUND_LENGTHS(ctx, (cudaStream_t)stream);
     return velocity_handling(ctx, dt, acc, (cudaStream_t)stream);
 }
 
 apbf_status apbf_neighborhood_green_apply(apbf_ctx *ctx, float range_scale, const float minp[3], const float maxp[3],
                                           uint32_t log2res, void *stream) {
     if (!ctx || !minp || !maxp) return APBF_ERR_INVALID_ARG;
+    APBF_BOUND_LENGTHS(ctx, (cudaStream_t)stream);
     return neighborhood_green(ctx, range_scale, minp, maxp, log2res, (cudaStream_t)stream);
 }
 
 apbf_status apbf_box_collision_apply(apbf_ctx *ctx, void *stream) {
     if (!ctx) return APBF_ERR_INVALID_ARG;
+    APBF_BOUND_LENGTHS(ctx, (cudaStream_t)stream);
     return box_collision(ctx, (cudaStream_t)stream);
 }
 
 apbf_status apbf_incompressibility_apply(apbf_ctx *ctx, void *stream) {
     if (!ctx) return APBF_ERR_INVALID_ARG;
+    APBF_BOUND_LENGTHS(ctx, (cudaStream_t)stream);
     return incompressibility(ctx, (cudaStream_t)stream);
 }
 
 apbf_status apbf_kernel_width_from_boundary_distance_apply(apbf_ctx *ctx, void *stream) {
     if (!ctx) return APBF_ERR_INVALID_ARG;
+    APBF_BOUND_LENGTHS(ctx, (cudaStream_t)stream);
     return kw_from_boundary_distance(ctx, (cudaStream_t)stream);
 }
 
 apbf_status apbf_spread_kernel_width_apply(apbf_ctx *ctx, void *stream) {
     if (!ctx) return APBF_ERR_INVALID_ARG;
+    APBF_BOUND_LENGTHS(ctx, (cudaStream_t)stream);
     return spread_kernel_width(ctx, (cudaStream_t)stream);
 }
 
 apbf_status apbf_update_transfers_apply(apbf_ctx *ctx, void *stream) {
     if (!ctx) return APBF_ERR_INVALID_ARG;
+    APBF_BOUND_LENGTHS(ctx, (cudaStream_t)stream);
     return update_transfers(ctx, (cudaStream_t)stream);
 }
 
 apbf_status apbf_particle_transfer_apply(apbf_ctx *ctx, float dt, void *stream) {
     if (!ctx) return APBF_ERR_INVALID_ARG;
+    APBF_BOUND_LENGTHS(ctx, (cudaStream_t)stream);
     return particle_transfer(ctx, dt, (cudaStream_t)stream);
 }
 
@@ -738,13 +755,102 @@ apbf_status apbf_substep(apbf_ctx *ctx, float dt, void *stream) {
         return APBF_ERR_INVALID_ARG;
     }
     cudaStream_t s = (cudaStream_t)stream;
+    APBF_BOUND_LENGTHS(ctx, s);
     if (substep_graph_eligible(ctx)) return substep_graph(ctx, dt, s);
     return substep_body(ctx, dt, s, false);
 }
 
 apbf_status apbf_reduce_fp64(apbf_ctx *ctx, double out[4], void *stream) {
     if (!ctx || !out) return APBF_ERR_INVALID_ARG;
+    APBF_BOUND_LENGTHS(ctx, (cudaStream_t)stream);
     return reduce_fp64(ctx, out, (cudaStream_t)stream);
+}
+
+namespace {
+bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0u; }
+}  // namespace
+
+apbf_status apbf_bind_lists(apbf_ctx *ctx, const apbf_fluid_view fluid[2], const apbf_transfers_view transfers[2],
+                            const apbf_neighbors_view *nb) {
+    if (!ctx || !fluid || !transfers || !nb) return APBF_ERR_INVALID_ARG;
+    if (ctx->bound) {
+        set_error("apbf_bind_lists: lists already bound (apbf_unbind_lists first)");
+        return APBF_ERR_INVALID_ARG;
+    }
+    for (int k = 0; k < 2; ++k) {
+        const apbf_fluid_view &f = fluid[k];
+        const apbf_transfers_view &t = transfers[k];
+        const bool ok_f = f.capacity >= ctx->cfg.particle_capacity && f.d_length && f.d_length == fluid[0].d_length &&
+                          f.position && f.velocity && f.inverse_mass && f.radius && f.pos_backup && f.transferring &&
+                          f.target_radius && f.kernel_width && f.boundariness && f.boundary_distance &&
+                          aligned16(f.position) && aligned16(f.velocity) && aligned16(f.pos_backup);
+        const bool ok_t = t.capacity >= ctx->cfg.transfer_capacity && t.d_length &&
+                          t.d_length == transfers[0].d_length && t.source && t.target && t.time_left;
+        if (!ok_f || !ok_t) {
+            set_error("apbf_bind_lists: two list sets with every attribute, capacities of at least the context's, one "
+                      "length word per list, 16-byte aligned int4/float4 arrays");
+            return APBF_ERR_INVALID_ARG;
+        }
+    }
+    if (nb->row_stride != ctx->row_stride || nb->max_per_row < ctx->cfg.max_neighbors || !nb->count || !nb->index) {
+        set_error("apbf_bind_lists: neighbour rows need the context's row_stride (apbf_neighbors_get_view) and at "
+                  "least its max_neighbors entries per row");
+        return APBF_ERR_INVALID_ARG;
+    }
+    APBF_CUDA(cudaSetDevice(ctx->device));
+    APBF_CUDA(cudaDeviceSynchronize());  // no work of the context may still use its own lists
+    for (int k = 0; k < 2; ++k) {
+        ctx->own_fl[k] = ctx->fl[k];
+        ctx->own_tr[k] = ctx->tr[k];
+        FluidBufs &d = ctx->fl[k];
+        const apbf_fluid_view &f = fluid[k];
+        d.pos = (int4 *)f.position;
+        d.vel = (float4 *)f.velocity;
+        d.inv_mass = f.inverse_mass;
+        d.radius = f.radius;
+        d.pos_backup = (int4 *)f.pos_backup;
+        d.transferring = f.transferring;
+        d.target_radius = f.target_radius;
+        d.kernel_width = f.kernel_width;
+        d.boundariness = f.boundariness;
+        d.boundary_distance = f.boundary_distance;  // lambda_prev stays the context's (warm-start history)
+        ctx->tr[k].source = transfers[k].source;
+        ctx->tr[k].target = transfers[k].target;
+        ctx->tr[k].time_left = transfers[k].time_left;
+    }
+    ctx->fcur = 0;
+    ctx->tcur = 0;
+    ctx->own_nb_count = ctx->nb_count;
+    ctx->own_nb_idx = ctx->nb_idx;
+    ctx->nb_count = nb->count;
+    ctx->nb_idx = nb->index;
+    ctx->ext_len_particles = fluid[0].d_length;
+    ctx->ext_len_transfers = transfers[0].d_length;
+    destroy_substep_graphs(ctx);  // captured with the context's own buffers
+    destroy_solve_graphs(ctx);
+    ctx->graph_version++;
+    ctx->bound = true;
+    return APBF_OK;
+}
+
+apbf_status apbf_unbind_lists(apbf_ctx *ctx) {
+    if (!ctx) return APBF_ERR_INVALID_ARG;
+    if (!ctx->bound) return APBF_OK;
+    APBF_CUDA(cudaSetDevice(ctx->device));
+    APBF_CUDA(cudaDeviceSynchronize());
+    for (int k = 0; k < 2; ++k) {
+        ctx->fl[k] = ctx->own_fl[k];
+        ctx->tr[k] = ctx->own_tr[k];
+    }
+    ctx->fcur = 0;
+    ctx->tcur = 0;
+    ctx->nb_count = ctx->own_nb_count;
+    ctx->nb_idx = ctx->own_nb_idx;
+    destroy_substep_graphs(ctx);
+    destroy_solve_graphs(ctx);
+    ctx->graph_version++;
+    ctx->bound = false;
+    return APBF_OK;
 }
 
 apbf_status apbf_set_wait_limit(apbf_ctx *ctx, uint32_t limit, int inject) {

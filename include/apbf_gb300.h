@@ -249,6 +249,28 @@ apbf_status apbf_set_boxes(apbf_ctx *ctx, const float *box_min4, const float *bo
 
 /* ---- list access (gpu_list::buffer / length, source/gpu_list.h) ---- */
 apbf_status apbf_fluid_get_view(apbf_ctx *ctx, apbf_fluid_view *out);
+/* Caller-owned lists, the reference's ownership model: its stages keep pointers to
+ * lists the scene owns (neighborhood_green::set_data, neighborhood_green.h:11;
+ * incompressibility::set_data, incompressibility.h:11; update_transfers::set_data,
+ * update_transfers.h:11; particle_transfer::set_data, particle_transfer.h:11), and a
+ * list edit moves a list to another of its pooled buffers (gpu_list.h:238-261).
+ * apbf_bind_lists makes the context run every stage, apbf_substep and the host-list
+ * copies on the caller's device memory: two buffer sets of the particle lists and
+ * of the transfer list (a reorder, a compaction or a Jacobi pass writes one set from
+ * the other), one length word per list (shared by its two sets), and the neighbour
+ * rows (row_stride as apbf_neighbors_get_view reports it, at least max_neighbors
+ * entries per row).  The context keeps only scratch (and the warm start's lambda
+ * history); it allocates nothing in this call and never frees the caller's memory.
+ * fluid[0] and transfers[0] are current at the bind; after any call
+ * apbf_fluid_get_view / apbf_transfers_get_view name the caller's set that is
+ * current, and the length words hold the lists' lengths (each stage call copies them
+ * in before its work and out after it, stream-ordered).  int4 / float4 arrays must
+ * be 16-byte aligned.  Synchronises the device; invalidates captured graphs. */
+apbf_status apbf_bind_lists(apbf_ctx *ctx, const apbf_fluid_view fluid[2], const apbf_transfers_view transfers[2],
+                            const apbf_neighbors_view *neighbors);
+/* Back to the context's own lists, with the contents they had before the bind (set
+ * their lengths, or upload, before the next stage call).  Synchronises the device. */
+apbf_status apbf_unbind_lists(apbf_ctx *ctx);
 apbf_status apbf_transfers_get_view(apbf_ctx *ctx, apbf_transfers_view *out);
 apbf_status apbf_neighbors_get_view(apbf_ctx *ctx, apbf_neighbors_view *out);
 /* The rows the position update gathers over besides the forward rows (no
