@@ -376,8 +376,10 @@ apbf_status sort_pairs_device(apbf_ctx *ctx, const uint32_t *keys_in, const uint
                               cudaStream_t s);
 apbf_status prefix_sum_device(apbf_ctx *ctx, uint32_t *d_values, const uint32_t *d_count, uint32_t max_count,
                               cudaStream_t s);
+// corrections = false: no correction rows (the substep prunes and transposes the rows
+// next, spread_kernel_width)
 apbf_status neighborhood_green(apbf_ctx *ctx, float range_scale, const float minp[3], const float maxp[3],
-                               uint32_t log2res, cudaStream_t s, bool fuse_box = false);
+                               uint32_t log2res, cudaStream_t s, bool fuse_box = false, bool corrections = true);
 apbf_status neighborhood_binary_search(apbf_ctx *ctx, float range_scale, cudaStream_t s,
                                        bool fuse_box = false);  // neighborhood_bs.cu
 apbf_status velocity_handling(apbf_ctx *ctx, float dt, const float accel[3], cudaStream_t s);

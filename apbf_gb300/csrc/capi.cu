@@ -661,7 +661,7 @@ apbf_status substep_body(apbf_ctx *ctx, float dt, cudaStream_t s, bool capture, 
     else
         r = neighborhood_green(ctx, scale, ctx->scene.min_pos, ctx->scene.max_pos,
                                ctx->tuning.search_log2res ? ctx->tuning.search_log2res : ctx->scene.log2res, s,
-                               fuse_first);
+                               fuse_first, !spread);
     if (r != APBF_OK) return r;
     if (spread) {
         r = spread_kernel_width(ctx, s);

@@ -155,6 +155,7 @@ struct BuildArgs {
     const int4 *srec;         // per particle: position xyz and fixed-point search radius R (w)
     uint32_t *ucount, *uidx;  // correction rows (the reverse-row arrays), when the radii differ
     uint32_t *one_sided;      // per particle: one-sided pairs of its row (radii that differ)
+    int corrections;          // 0: no correction rows (the caller transposes pruned rows next)
 };
 
 // Appends an entry to a correction row (the reverse-row arrays; their counts were
@@ -264,7 +265,7 @@ __device__ __noinline__ int4 box_push_call(int4 ip, float r, uint32_t id, const 
 // walk counted some): found again on the particle's row, i's correction row
 // subtracts j, j's adds i.  A kernel of its own, so that the walk holds no atomics.
 __global__ void k_corrections(BuildArgs a) {
-    if (a.st->range_min == a.st->range_max) return;  // symmetric rows: nothing one-sided
+    if (!a.corrections || a.st->range_min == a.st->range_max) return;  // none wanted, or nothing one-sided
     const uint32_t n = a.d_len[kLenParticles];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         if (!a.one_sided[i]) continue;
@@ -288,7 +289,7 @@ __global__ void k_corrections(BuildArgs a) {
 __global__ void __launch_bounds__(256, 4) k_build_rows(BuildArgs a) {
     const uint32_t n = a.d_len[kLenParticles];
     const uint32_t last = (1u << a.L) - 1u;
-    const bool uni = a.st->range_min != a.st->range_max;  // the radii differ: union rows
+    const bool uni = a.corrections && a.st->range_min != a.st->range_max;  // the radii differ: correction rows
     if (blockIdx.x == 0 && threadIdx.x == 0) a.st->union_rows = uni ? 1u : 0u;
     unsigned long long local = 0;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -402,7 +403,7 @@ apbf_status reorder_particles(apbf_ctx *ctx, cudaStream_t s, bool search, float 
 }
 
 apbf_status neighborhood_green(apbf_ctx *ctx, float range_scale, const float minp[3], const float maxp[3],
-                               uint32_t L, cudaStream_t s, bool fuse_box) {
+                               uint32_t L, cudaStream_t s, bool fuse_box, bool corrections) {
     if (L < 1 || L > ctx->cfg.max_log2res || L > 10) {
         set_error("neighborhood_green: log2res must be in [1, max_log2res of apbf_create]");
         return APBF_ERR_INVALID_ARG;
@@ -462,6 +463,7 @@ apbf_status neighborhood_green(apbf_ctx *ctx, float range_scale, const float min
     ba.ucount = ctx->rev_count;
     ba.uidx = ctx->rev_idx;
     ba.one_sided = ctx->flag_scan;  // scratch: not in use during the search
+    ba.corrections = corrections ? 1 : 0;
     APBF_CUDA(cudaMemsetAsync(ctx->rev_count, 0, (size_t)cap * sizeof(uint32_t), s));  // correction rows
     k_build_rows<<<grid_for(ctx, cap, kBlock, 8), kBlock, 0, s>>>(ba);
     APBF_AFTER_LAUNCH(ctx, s, "k_build_rows");

@@ -574,11 +574,14 @@ __device__ __forceinline__ int3 delta_row(const PassB &a, const int4 *__restrict
     int32_t ax = start.x, ay = start.y, az = start.z;
     // software-pipelined as in density_one: the gathers of a batch go out with the
     // row entries of the next
+    // Entries are masked to their index bits: rows the search tuner leaves behind may be
+    // correction rows read as transposed ones (flag bit 31), and no entry may address
+    // beyond the lists (the index bits of every valid entry are the entry itself).
     uint32_t ii[kUnroll];
 #pragma unroll
     for (int u = 0; u < kUnroll; ++u) {
         const uint32_t k = sub + u * L;
-        ii[u] = k < cnt ? row[(size_t)k * a.stride] : j;
+        ii[u] = k < cnt ? row[(size_t)k * a.stride] & ~kNoDelta : j;
     }
     for (uint32_t k0 = sub; k0 < cnt; k0 += L * kUnroll) {
         float4 rr[kUnroll];
@@ -600,7 +603,7 @@ __device__ __forceinline__ int3 delta_row(const PassB &a, const int4 *__restrict
 #pragma unroll
         for (int u = 0; u < kUnroll; ++u) {
             const uint32_t k = k0 + (L * kUnroll) + u * L;
-            in_[u] = k < cnt ? row[(size_t)k * a.stride] : j;
+            in_[u] = k < cnt ? row[(size_t)k * a.stride] & ~kNoDelta : j;
         }
 #pragma unroll
         for (int u = 0; u < kUnroll; ++u) {

@@ -212,6 +212,7 @@ extern "C" apbf_status apbf_autotune_search(apbf_ctx *ctx, void *stream, apbf_tu
     // (2) search grid
     const apbf_settings &st = ctx->settings;
     const float scale = (st.basic_pbf || st.base_kernel_width_on_boundary_distance) ? 1.0f : 1.5f;
+    const bool spread = !st.basic_pbf && !st.base_kernel_width_on_boundary_distance;  // as apbf_substep searches
     uint32_t best_L = L0;
     float best_t = 0.0f;
     ctx->tuning.sort_digit_bits = best_bits;
@@ -221,7 +222,7 @@ extern "C" apbf_status apbf_autotune_search(apbf_ctx *ctx, void *stream, apbf_tu
         float tot = 0.0f;
         for (int k = 0; k < 3 && r == APBF_OK; ++k) {  // one warm-up, two timed
             cudaEventRecord(ev.a, s);
-            r = neighborhood_green(ctx, scale, ctx->scene.min_pos, ctx->scene.max_pos, (uint32_t)L, s, false);
+            r = neighborhood_green(ctx, scale, ctx->scene.min_pos, ctx->scene.max_pos, (uint32_t)L, s, false, !spread);
             cudaEventRecord(ev.b, s);
             const float t = ev.ms(s);
             if (k > 0) tot += t;

@@ -37,7 +37,13 @@ UNIT = "particle-substeps/s"
 
 WORKLOADS = {
     # name: (scene factory, description)
-    "water_drop_250k": ("water_drop", dict(total=250_000, basic_pbf=False)),
+    # config 1: split/merge with kernel widths spread across neighbours (the
+    # spread_kernel_width path, pool.cpp:87-89, taken when the widths do not come from
+    # the boundary distance); target radii from 1 at the surface to 2 at the pool's
+    # floor (volume ratios 1x-8x): scale factor 1/40 per radius of boundary distance
+    "water_drop_250k": ("water_drop", dict(total=250_000, basic_pbf=False, max_neighbors=1024,
+                                           settings={"base_kernel_width_on_boundary_distance": 0,
+                                                     "target_radius_scale_factor": 0.025})),
     "water_drop_250k_plain": ("water_drop", dict(total=250_000, basic_pbf=True)),
     "dam_break_32k": ("dam_break", dict(n_side=32)),
     # 384k particles pre-filled + 2000/substep from the emitter: ~1M after 300 substeps
@@ -63,7 +69,14 @@ def make_spec(name: str, seed: int = 0, scale: float = 1.0):
         spec.meta["presteps"] = 300  # the emitter has brought the count to ~1M
         return spec
     basic = kw.pop("basic_pbf")
-    return scenes.water_drop(seed=seed, basic_pbf=basic, **kw)
+    settings = kw.pop("settings", None)
+    maxn = kw.pop("max_neighbors", None)
+    spec = scenes.water_drop(seed=seed, basic_pbf=basic, **kw)
+    if settings:
+        spec.meta["settings"] = dict(settings)
+    if maxn:
+        spec.meta["max_neighbors"] = maxn
+    return spec
 
 
 def settings_dict(spec) -> dict:
@@ -72,6 +85,7 @@ def settings_dict(spec) -> dict:
     from oracle.oracle import DEFAULT_SETTINGS
 
     s = dict(DEFAULT_SETTINGS)
+    s.update(spec.meta.get("settings", {}))
     s["basic_pbf"] = 1 if spec.basic_pbf else 0
     s["solver_iterations"] = 100
     s["density_error_target"] = 0.001
@@ -382,12 +396,13 @@ def _make_ctx(spec, args, local, mode: int = 0, net=None):
 
     cap = max(int(spec.n * 1.25) + 1024, int(spec.meta.get("capacity", 0) * 1.15))
     maxn = args.max_neighbors if spec.basic_pbf else max(args.max_neighbors, 256)
+    maxn = max(maxn, spec.meta.get("max_neighbors", 0))
     # the search tuner may try grids up to search_levels finer than the scene's
     levels = min(9, max(spec.log2res, 3) + max(0, getattr(args, "search_levels", 0)))
     ctx = Context(particle_capacity=cap, max_neighbors=maxn, max_log2res=levels, device=local)
     # iterate every substep until the mean density error is at most the target
     ctx.set_settings(basic_pbf=1 if spec.basic_pbf else 0, solver_iterations=args.max_iterations,
-                     density_error_target=args.error_target)
+                     density_error_target=args.error_target, **spec.meta.get("settings", {}))
     ctx.load_scene(spec)
     ctx.set_solve_graph(args.graph_mode)
     if getattr(args, "persistent", False):

@@ -137,3 +137,24 @@ def test_search_tuning_restores_the_state_and_keeps_results():
     assert ctx.check_status().pairs == ref.check_status().pairs, choice
     ctx.close()
     ref.close()
+
+
+def test_tuners_on_spread_kernel_width_scene():
+    """Kernel widths spread across neighbours (the rows the substep leaves are
+    transposed rows) and the search tuner (whose searches leave correction rows while
+    the status it restores names the transposed kind): the pass tuner and the next
+    substeps run on those rows without error and the state stays finite."""
+    spec = scenes.water_drop(total=20_000, seed=9, basic_pbf=False)
+    ctx = _ctx(spec, spec.iterations, maxn=256)
+    ctx.set_settings(base_kernel_width_on_boundary_distance=0)
+    for _ in range(15):
+        ctx.substep(spec.dt)
+    ctx.check_status()
+    ctx.autotune_search()
+    ctx.autotune()
+    for _ in range(5):
+        ctx.substep(spec.dt)
+    ctx.check_status()
+    g, _ = ctx.download()
+    assert np.all(np.isfinite(g["velocity"]))
+    ctx.close()
