@@ -190,6 +190,7 @@ struct apbf_ctx {
     int4 *shift = nullptr;
     float4 *solve_rec = nullptr;   // per particle: lambda, Gauss constants (ivd, norm), kernel width
     int4 *solve_pk = nullptr;      // per particle: position (xyz) and applied lambda (w, float bits)
+    float2 *solve_kc = nullptr;    // per particle: Gauss constants (ivd, norm) of its kernel width
     int4 *filt = nullptr;          // per particle: gradient sum and boundariness > 0, for the deferred filter
     // learned warm start
     float *mlp_params = nullptr;   // FP32 parameter vector (mlp.cu)
@@ -713,8 +714,9 @@ __device__ __forceinline__ int4 box_push(int4 ip, float r, uint32_t id, const fl
                                          const float4 *__restrict__ bmax, const float4 *__restrict__ rot,
                                          uint32_t nb) {
     if (nb == 0) return ip;
-    float px = __fdiv_rn((float)ip.x, 262144.0f), py = __fdiv_rn((float)ip.y, 262144.0f),
-          pz = __fdiv_rn((float)ip.z, 262144.0f);
+    // vec3(position) / POS_RESOLUTION: a division by 2^18 is the exact product with 2^-18
+    float px = __fmul_rn((float)ip.x, 0x1p-18f), py = __fmul_rn((float)ip.y, 0x1p-18f),
+          pz = __fmul_rn((float)ip.z, 0x1p-18f);
     const float fid = (float)id;
     float3 h1 = make_float3(0.f, 0.f, 0.f), h2 = h1;
     bool have = false;

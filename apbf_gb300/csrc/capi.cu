@@ -273,6 +273,7 @@ apbf_status apbf_create(const apbf_config *cfg, apbf_ctx **out) {
     A(ctx->shift, cap);
     A(ctx->solve_rec, cap);
     A(ctx->solve_pk, cap);
+    A(ctx->solve_kc, cap);
     A(ctx->filt, cap);
     A(ctx->mlp_params, kMlpParams);
     A(ctx->mlp_image, mlp_image_bytes());

@@ -63,6 +63,7 @@ struct PassA {
     int4 *shift;
     float4 *rec;  // per particle: lambda, Gauss ivd, Gauss norm, kernel width (read by k_delta)
     int4 *pk;     // per particle: position xyz and the applied lambda (read by k_delta when widths are uniform)
+    float2 *kc;   // per particle: Gauss constants of its width, ivd 2^-36 and norm (read by k_delta when widths differ)
     uint32_t *dbg_dens;
     int4 *dbg_grad;
     uint32_t *dbg_sq;
@@ -84,6 +85,48 @@ struct PassA {
     int hk, gk, method, update_b;
     float b_speed, b_sgl_factor, b_up_factor;
 };
+
+// Gauss constants in the units of the unscaled fixed-point offset D (2^18 per
+// reference unit): the exponent scale ivd 2^-36 (r^2 = |D|^2 2^-36), the height
+// norm, and the gradient factor 2 ln2 ivd 2^-18 (kernels.glsl:112-123 with r = D 2^-18).
+struct GaussPair {
+    float ivd36, norm, k2;
+};
+__device__ __forceinline__ GaussPair gauss_pair(float ivd36, float norm) {
+    // k2 = round(ivd ln2) 2^-17: the factor 2 of the gradient and the 2^-18 of r = D 2^-18
+    return {ivd36, norm, ivd36 * (0.693147180559945309f * 0x1p19f)};
+}
+__device__ __forceinline__ GaussPair gauss_pair(KConst c) { return gauss_pair(c.ivd * 0x1p-36f, c.norm); }
+__device__ __forceinline__ float3 udiff(int4 from, int4 to) {
+    return make_float3((float)wadd(to.x, -from.x), (float)wadd(to.y, -from.y), (float)wadd(to.z, -from.z));
+}
+
+// The Gauss height and gradient of the offset D = to - from in fixed-point units.
+// Every product is the FP32 rounding of the reference-unit product (fdiff, r2,
+// kernel_gradient's -2 ivd W r) scaled by a power of two, which is exact in the
+// normal range: the terms equal the reference-unit evaluation bit for bit, except
+// for gradients far below one fixed-point unit of any sum (subnormal intermediates).
+__device__ __forceinline__ void gauss_terms_r2(float3 D, float r2, const GaussPair &k, float &W, float3 &g) {
+    W = exp2f(r2 * k.ivd36) * k.norm;
+    if (r2 < 1.0e-8f * 0x1p36f) {  // dist < 0.0001 reference units
+        g = make_float3(0.f, 0.f, 0.f);
+        return;
+    }
+    const float s = W * k.k2;
+    g = make_float3(s * D.x, s * D.y, s * D.z);
+}
+__device__ __forceinline__ void gauss_terms(float3 D, const GaussPair &k, float &W, float3 &g) {
+    gauss_terms_r2(D, dot3x(D, D), k, W, g);
+}
+
+// gauss_filter_hit for the offset x_j - x_i = -D, D in fixed-point units and
+// r2 = |D|^2.  Every quantity is the reference-unit one times a power of two, and
+// none is subnormal (|D| components are 0 or >= 1, those of ed 0 or >= 2^-32), so
+// the decision is gauss_filter_hit's bit for bit.
+__device__ __forceinline__ bool gauss_filter_hit_fixed(float3 ed, float3 D, float r2) {
+    if (r2 < 1.0e-8f * 0x1p36f) return false;
+    return dot3x(ed, D) > __fmul_rn(0.6f, __fsqrt_rn(r2));
+}
 
 template <bool GAUSS>
 __device__ __forceinline__ void pair_terms(int hk, int gk, float3 d, float kw, KConst c, float &W, float3 &g) {
@@ -212,6 +255,7 @@ __device__ __forceinline__ void density_one(const PassA &a, const int4 *__restri
         const int4 p = pos[i];
         const float kw = a.kw[i];
         const KConst c = gauss_consts(kw);
+        const GaussPair gp = gauss_pair(c);
         uint32_t dens = 0u;
         int32_t gx = 0, gy = 0, gz = 0;
         uint32_t sq = 0;
@@ -251,10 +295,12 @@ __device__ __forceinline__ void density_one(const PassA &a, const int4 *__restri
                 const int4 q = qq[u];
                 // the neighbour's mass rides in position.w (x / invMassN = x * mass)
                 const float mjf = __int_as_float(q.w) * APBF_FIX;  // neighbour mass x 2^18
-                const float3 d = fdiff(p, q);
                 float W;
                 float3 g;
-                pair_terms<GAUSS>(a.hk, a.gk, d, kw, c, W, g);
+                if (GAUSS)
+                    gauss_terms(udiff(p, q), gp, W, g);
+                else
+                    pair_terms<false>(a.hk, a.gk, fdiff(p, q), kw, c, W, g);
                 dens += f2u(W * mjf);
                 gx = wadd(gx, f2i(g.x * mjf));
                 gy = wadd(gy, f2i(g.y * mjf));
@@ -336,6 +382,7 @@ __device__ __forceinline__ void density_one(const PassA &a, const int4 *__restri
             else applied = 0.0f;
         }
         if (write_rec) a.rec[i] = make_float4(applied, c.ivd, c.norm, kw);
+        else if (GAUSS) a.kc[i] = make_float2(gp.ivd36, gp.norm);
         a.pk[i] = make_int4(p.x, p.y, p.z, __float_as_int(applied));
         ps.kwlo = min(ps.kwlo, __float_as_uint(kw));
         ps.kwhi = max(ps.kwhi, __float_as_uint(kw));
@@ -503,6 +550,7 @@ struct PassB {
     int4 *pos_out;
     const float4 *rec;
     const int4 *pk;   // the density pass's packed records (position, applied lambda)
+    const float2 *kc;  // the density pass's Gauss constants per particle
     const float *kw;
     const int4 *shift;
     const float *radius;
@@ -533,28 +581,33 @@ __device__ __forceinline__ void accumulate(float *dst, int mode, uint32_t j, flo
 
 // One neighbour's term of a position update: int(gradW_ij * lambda_i * 2^18) per
 // axis (incompressibility_3.comp:62-66) for the neighbour's record q (position,
-// and for the Gauss kernel the applied lambda in w), its width kwi or solve record
-// rr.  Constants: cj (j's own) when PACKED or the widths are equal bit for bit, else
-// the neighbour's.  The main row and the correction rows use this one function, so
-// a term subtracted again cancels exactly.
+// and for the Gauss kernel the applied lambda in w), its Gauss constants kci (as
+// the density pass computed them from its width) or solve record rr.  PACKED (every
+// width equal): j's own constants cj.  The main row and the correction rows use this
+// one function, so a term subtracted again cancels exactly.
+// The Gauss term of the offset D = x_j - x_i (fixed-point units) with r2 = |D|^2.
+__device__ __forceinline__ int3 gauss_delta(float3 D, float r2, float lam, const GaussPair &k) {
+    float W;
+    float3 g;
+    gauss_terms_r2(D, r2, k, W, g);
+    const float sc = lam * APBF_FIX;
+    return make_int3(f2i(g.x * sc), f2i(g.y * sc), f2i(g.z * sc));
+}
+
 template <bool GAUSS, bool PACKED>
-__device__ __forceinline__ int3 pair_delta(const PassB &a, int4 q, float lam, float kwi, float4 rr, int4 p, float kwj,
-                                           KConst cj) {
-    KConst c;
-    if (PACKED) {
-        c = cj;
-    } else if (GAUSS) {
-        c = __float_as_uint(kwi) == __float_as_uint(kwj) ? cj : gauss_consts(kwi);
-    } else {
+__device__ __forceinline__ int3 pair_delta(const PassB &a, int4 q, float lam, float2 kci, float4 rr, int4 p,
+                                           const GaussPair &gpj) {
+    if (GAUSS) {
+        const float3 D = udiff(q, p);
+        return gauss_delta(D, dot3x(D, D), lam, PACKED ? gpj : gauss_pair(kci.x, kci.y));
+    }
+    float3 g;
+    {
+        KConst c;
         c.ivd = rr.y;
         c.norm = rr.z;
-    }
-    const float3 d = fdiff(q, p);
-    const float r2 = dot3x(d, d);
-    float3 g;
-    if (GAUSS) {
-        g = kernel_gradient(1, d, r2, 0.0f, c, gauss_height(r2, c));
-    } else {
+        const float3 d = fdiff(q, p);
+        const float r2 = dot3x(d, d);
         g = kernel_gradient(a.gk, d, r2, rr.w, c, a.gk == 1 ? gauss_height(r2, c) : 0.0f);
     }
     const float sc = lam * APBF_FIX;
@@ -565,11 +618,11 @@ __device__ __forceinline__ int3 pair_delta(const PassB &a, int4 q, float lam, fl
 // as a gather) and the deferred boundariness filter over the row's first fcnt
 // entries.  PACKED: the neighbours' packed records (position, applied lambda) with
 // j's own Gauss constants cj (every width equal); GAUSS otherwise: the packed
-// records and the neighbours' widths; other kernels: the solve records and the
-// positions.
+// records and the neighbours' Gauss constants; other kernels: the solve records
+// and the positions.
 template <bool GAUSS, int L, bool PACKED>
 __device__ __forceinline__ int3 delta_row(const PassB &a, const int4 *__restrict__ pos, const uint32_t *row, uint32_t cnt,
-                                          uint32_t fcnt, uint32_t j, uint32_t sub, int4 p, float kwj, KConst cj,
+                                          uint32_t fcnt, uint32_t j, uint32_t sub, int4 p, const GaussPair &cj,
                                           bool fil, float3 ed, bool &hit, int4 start) {
     int32_t ax = start.x, ay = start.y, az = start.z;
     // software-pipelined as in density_one: the gathers of a batch go out with the
@@ -586,7 +639,7 @@ __device__ __forceinline__ int3 delta_row(const PassB &a, const int4 *__restrict
     for (uint32_t k0 = sub; k0 < cnt; k0 += L * kUnroll) {
         float4 rr[kUnroll];
         int4 qq[kUnroll];
-        float kk[kUnroll];
+        float2 kk[kUnroll];
         uint32_t in_[kUnroll];
 #pragma unroll
         for (int u = 0; u < kUnroll; ++u) {
@@ -594,7 +647,7 @@ __device__ __forceinline__ int3 delta_row(const PassB &a, const int4 *__restrict
                 qq[u] = a.pk[ii[u]];
             } else if (GAUSS) {
                 qq[u] = a.pk[ii[u]];
-                kk[u] = a.kw[ii[u]];
+                kk[u] = a.kc[ii[u]];
             } else {
                 rr[u] = a.rec[ii[u]];
                 qq[u] = pos[ii[u]];
@@ -607,13 +660,21 @@ __device__ __forceinline__ int3 delta_row(const PassB &a, const int4 *__restrict
         }
 #pragma unroll
         for (int u = 0; u < kUnroll; ++u) {
-            if (fil && !hit && k0 + u * L < fcnt) {
-                const float3 dn = fdiff(qq[u], p);  // x_i - x_j ...
-                hit = gauss_filter_hit(ed, make_float3(-dn.x, -dn.y, -dn.z));  // ... as the offset x_j - x_i
-            }
             const float lam = k0 + u * L < cnt ? (PACKED || GAUSS ? __int_as_float(qq[u].w) : rr[u].x) : 0.0f;
-            if (lam == 0.0f) continue;  // the applied lambda (incompressibility_3.comp:63); padding lanes
-            const int3 t = pair_delta<GAUSS, PACKED>(a, qq[u], lam, kk[u], rr[u], p, kwj, cj);
+            int3 t;
+            if (GAUSS) {
+                // the deferred filter (Gauss only) shares the offset and its square with the term
+                const bool ftest = fil && !hit && k0 + u * L < fcnt;
+                if (lam == 0.0f && !ftest) continue;
+                const float3 D = udiff(qq[u], p);
+                const float r2 = dot3x(D, D);
+                if (ftest) hit = gauss_filter_hit_fixed(ed, D, r2);
+                if (lam == 0.0f) continue;  // the applied lambda (incompressibility_3.comp:63); padding lanes
+                t = gauss_delta(D, r2, lam, PACKED ? cj : gauss_pair(kk[u].x, kk[u].y));
+            } else {
+                if (lam == 0.0f) continue;
+                t = pair_delta<false, false>(a, qq[u], lam, kk[u], rr[u], p, cj);
+            }
             ax = wadd(ax, t.x);
             ay = wadd(ay, t.y);
             az = wadd(az, t.z);
@@ -630,23 +691,23 @@ __device__ __forceinline__ int3 delta_row(const PassB &a, const int4 *__restrict
 // the group of L takes entries sub, sub + L, ...
 template <bool GAUSS, int L, bool PACKED>
 __device__ __forceinline__ int3 delta_corrections(const PassB &a, const int4 *__restrict__ pos, uint32_t m, uint32_t j,
-                                                  uint32_t sub, int4 p, float kwj, KConst cj, int3 acc) {
+                                                  uint32_t sub, int4 p, const GaussPair &cj, int3 acc) {
     for (uint32_t k = sub; k < m; k += L) {
         const uint32_t e = a.ridx[(size_t)k * a.stride + j];
         const uint32_t i = e & ~kNoDelta;
         float4 rr = make_float4(0.f, 0.f, 0.f, 0.f);
         int4 q;
-        float kwi = 0.0f;
+        float2 kci = make_float2(0.f, 0.f);
         if (PACKED || GAUSS) {
             q = a.pk[i];
-            if (!PACKED) kwi = a.kw[i];
+            if (!PACKED) kci = a.kc[i];
         } else {
             rr = a.rec[i];
             q = pos[i];
         }
         const float lam = PACKED || GAUSS ? __int_as_float(q.w) : rr.x;
         if (lam == 0.0f) continue;
-        const int3 t = pair_delta<GAUSS, PACKED>(a, q, lam, kwi, rr, p, kwj, cj);
+        const int3 t = pair_delta<GAUSS, PACKED>(a, q, lam, kci, rr, p, cj);
         if (e & kNoDelta) {
             acc.x = wadd(acc.x, -t.x);
             acc.y = wadd(acc.y, -t.y);
@@ -672,8 +733,9 @@ __device__ __forceinline__ void delta_one(const PassB &a, const int4 *__restrict
         const bool valid = j_raw < n;
         const uint32_t j = valid ? j_raw : 0u;
         const int4 p = pos[j];
-        const float kwj = GAUSS ? a.kw[j] : 1.0f;
-        const KConst cj = gauss_consts(kwj);
+        // j's Gauss constants as the density pass stored them
+        const float2 kcj = GAUSS ? a.kc[j] : make_float2(0.f, 0.f);
+        const GaussPair cj = gauss_pair(kcj.x, kcj.y);
         int32_t ax, ay, az;
         const uint32_t cnt = valid ? cnt_arr[j] : 0u;
         const uint32_t *row = idx_arr + j;
@@ -691,12 +753,12 @@ __device__ __forceinline__ void delta_one(const PassB &a, const int4 *__restrict
         // are order-free, and the load is in flight with the particle's other data
         const int4 sh = sub == 0 ? shj : make_int4(0, 0, 0, 0);
         const float rj = a.radius[j];
-        int3 acc = packed ? delta_row<GAUSS, L, true>(a, pos, row, cnt, fcnt, j, sub, p, kwj, cj, fil, ed, hit, sh)
-                          : delta_row<GAUSS, L, false>(a, pos, row, cnt, fcnt, j, sub, p, kwj, cj, fil, ed, hit, sh);
+        int3 acc = packed ? delta_row<GAUSS, L, true>(a, pos, row, cnt, fcnt, j, sub, p, cj, fil, ed, hit, sh)
+                          : delta_row<GAUSS, L, false>(a, pos, row, cnt, fcnt, j, sub, p, cj, fil, ed, hit, sh);
         if (corr) {  // the correction row (radii that differ): usually empty
             const uint32_t m = valid ? a.rcount[j] : 0u;
-            if (m) acc = packed ? delta_corrections<GAUSS, L, true>(a, pos, m, j, sub, p, kwj, cj, acc)
-                                : delta_corrections<GAUSS, L, false>(a, pos, m, j, sub, p, kwj, cj, acc);
+            if (m) acc = packed ? delta_corrections<GAUSS, L, true>(a, pos, m, j, sub, p, cj, acc)
+                                : delta_corrections<GAUSS, L, false>(a, pos, m, j, sub, p, cj, acc);
         }
         ax = acc.x;
         ay = acc.y;
@@ -1163,6 +1225,7 @@ static PassA make_pass_a(apbf_ctx *ctx, const SolveOpts &o) {
     a.shift = ctx->shift;
     a.rec = ctx->solve_rec;
     a.pk = ctx->solve_pk;
+    a.kc = ctx->solve_kc;
     a.dbg_dens = ctx->debug ? ctx->dbg_density : nullptr;
     a.dbg_grad = ctx->dbg_grad;
     a.dbg_sq = ctx->dbg_sq;
@@ -1201,6 +1264,7 @@ static PassB make_pass_b(apbf_ctx *ctx, const SolveOpts &o) {
     b.pos_out = alt.pos;
     b.rec = ctx->solve_rec;
     b.pk = ctx->solve_pk;
+    b.kc = ctx->solve_kc;
     b.kw = f.kernel_width;
     b.shift = ctx->shift;
     b.radius = f.radius;

@@ -223,4 +223,5 @@ def waterfall(initial: int = 384_000, seed: int = 0, substeps: int = 300, iterat
                                  "oriented_boxes": (np.array([[*centre, 0.0]], np.float32),
                                                     np.array([[*half, 0.0]], np.float32),
                                                     np.array([quat], np.float32)),
-                                 "capacity": int(initial + per_substep * substeps * 1.05) + 4096, "presteps": 0})
+                                 "capacity": int(initial + per_substep * substeps * 1.05) + 4096, "presteps": 0,
+                                 "per_substep": per_substep})

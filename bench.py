@@ -41,7 +41,7 @@ WORKLOADS = {
     # spread_kernel_width path, pool.cpp:87-89, taken when the widths do not come from
     # the boundary distance); target radii from 1 at the surface to 2 at the pool's
     # floor (volume ratios 1x-8x): scale factor 1/40 per radius of boundary distance
-    "water_drop_250k": ("water_drop", dict(total=250_000, basic_pbf=False, max_neighbors=1024,
+    "water_drop_250k": ("water_drop", dict(total=250_000, basic_pbf=False, max_neighbors=2048,
                                            settings={"base_kernel_width_on_boundary_distance": 0,
                                                      "target_radius_scale_factor": 0.025})),
     "water_drop_250k_plain": ("water_drop", dict(total=250_000, basic_pbf=True)),
@@ -452,51 +452,95 @@ def _selection_info(choice, table, seeds, args) -> dict:
                        "plain": table["plain"], "candidates": table["candidates"]})}
 
 
-def train_warm_start(args, local: int, rank: int) -> tuple[object, dict]:
-    """Untimed: samples from projected-rule rollouts of two scenes with seeds that the
-    timed scene does not use; minibatch Adam with the project's kernels, one network
-    per overshoot weight of the loss; then the network and over-relaxation bound
-    chosen on one or two further seeds (fewest passes within the plain solve's kinetic
-    energy).  Returns (None, info) when no candidate passes: the headline then runs
-    the reference Jacobi rule."""
+# The warm start's training mixture: rollouts of the dam break (32 k), the adaptive
+# water drop with spread kernel widths (250 k) and the adaptive waterfall (to ~1 M),
+# two seeds each, that neither a timed scene (seed = rank), a validation scene
+# (1000 + ...) nor an evaluation scene of the per-workload report (3000 + ...) uses.
+MIXTURE = ("dam_break_32k", "water_drop_250k", "waterfall_1m")
+MIXTURE_SAMPLES = 60_000_000  # about the same share from each rollout
+
+
+def training_rollouts(rank: int) -> list[tuple]:
+    """(workload, seed, substeps, every, particles at the end) of the mixture's
+    rollouts: each runs from the scene's start through its untimed presteps plus 60
+    substeps (the timed window and more; a scene timed from its start runs its own
+    length) and records every `every`-th substep, so that each contributes about
+    MIXTURE_SAMPLES / 6 samples (a growing scene counted at its mean size)."""
+    per = MIXTURE_SAMPLES / (2 * len(MIXTURE))
+    out = []
+    for w in MIXTURE:
+        for k in (0, 1):
+            seed = 2000 + 10 * rank + k
+            sp = make_spec(w, seed=seed)
+            pre = sp.meta.get("presteps", 0)
+            steps = pre + 60 if pre else sp.substeps
+            n_end = sp.n + sp.meta.get("per_substep", 0) * steps
+            every = max(1, int(round(steps * 0.5 * (sp.n + n_end) / per)))
+            out.append((w, seed, steps, every, n_end))
+    return out
+
+
+def train_mixture(args, local: int, rank: int) -> tuple[dict, dict]:
+    """Untimed: samples from projected-rule rollouts of the mixture (the plain solve;
+    the target is the lambda sum a substep's passes apply), then minibatch Adam with
+    the project's kernels, one network per overshoot weight of the loss."""
     import torch
 
     from apbf_gb300 import _native as N
-    from apbf_gb300.warmstart import SampleBuffer, ValidationCase, record_rollout, select_warm_start
+    from apbf_gb300.warmstart import SampleBuffer, record_rollout
 
     t0 = time.perf_counter()
-    seeds = [1000 + 10 * rank + k for k in (1, 2)]
-    specs = [make_spec(args.workload, seed=s) for s in seeds]
-    per = [sp.meta.get("presteps", 0) + 60 for sp in specs]
-    large = max(sp.n for sp in specs) >= 500_000
-    every = 12 if large else 3  # bounds the sample count of growing scenes
-    grown = [max(sp.n, int(sp.meta.get("capacity", 0))) for sp in specs]
-    cap = min(sum(int(g * 1.3) * ((p + every - 1) // every + 1) for g, p in zip(grown, per)), 120_000_000)
-    buf = SampleBuffer.allocate(cap, device=local)
-    for sp, p in zip(specs, per):
+    plan = training_rollouts(rank)
+    cap = int(sum(max(n_end, make_spec(w).n) * (steps // every + 1) for w, _, steps, every, n_end in plan) * 1.1)
+    buf = SampleBuffer.allocate(min(cap, 160_000_000), device=local)
+    counts = []
+    for w, seed, steps, every, _ in plan:
+        sp = make_spec(w, seed=seed)
         ctx = _make_ctx(sp, args, local, N.WARM_PROJECTED)
-        record_rollout(ctx, sp.dt, p, buf, iterations=args.max_iterations, every=every)
-        ctx.check_status()
+        before = buf.size()
+        record_rollout(ctx, sp.dt, steps, buf, iterations=args.max_iterations, every=every)
+        try:
+            ctx.check_status()
+        except Exception as e:
+            raise RuntimeError(f"training rollout {w} seed {seed}: {e}") from e
         ctx.close()
+        print(f"rollout {w} seed {seed}: {buf.size() - before} samples", file=sys.stderr, flush=True)
+        counts.append({"workload": w, "seed": seed, "substeps": steps, "every": every,
+                       "samples": buf.size() - before})
     torch.cuda.synchronize()
     t1 = time.perf_counter()
     X, T = buf.view()
     n_samples = int(X.shape[0])
-    ows, oms = _ws_choices(args)
+    ows, _ = _ws_choices(args)
     trained = _fit_nets(X, T, args, local, ows)
     torch.cuda.synchronize()
     t2 = time.perf_counter()
     del buf, X, T
     torch.cuda.empty_cache()
+    info = {"samples": n_samples, "rollouts": counts,
+            "target": "sum of the lambdas applied over all passes of a projected-rule substep",
+            "epochs": args.ws_epochs,
+            "loss_per_epoch": {k: [round(h, 5) for h in v[1]] for k, v in trained.items()},
+            "collect_s": round(t1 - t0, 3), "train_s": round(t2 - t1, 3)}
+    return {k: v[0] for k, v in trained.items()}, info
 
-    nets = {k: v[0] for k, v in trained.items()}
+
+def select_for_workload(nets: dict, args, local: int, rank: int, workload: str) -> tuple:
+    """Chooses the network and over-relaxation bound for `workload` on one or two of
+    its seeds that training and the timed scene do not use (fewest passes within the
+    plain solve's kinetic energy).  Returns (net or None, selection info)."""
+    from apbf_gb300.warmstart import ValidationCase, select_warm_start
+
+    t0 = time.perf_counter()
+    _, oms = _ws_choices(args)
     nmin = args.ws_min_neighbors if args.ws_min_neighbors is not None else 16.0
+    large = make_spec(workload).n >= 500_000 or workload.startswith("waterfall")
     vseeds = [1000 + 10 * rank + k for k in ((3,) if large else (3, 4))]
     table = None
     if len(nets) * len(oms) > 1:
         cases = []
         for vs in vseeds:
-            vspec = make_spec(args.workload, seed=vs)
+            vspec = make_spec(workload, seed=vs)
             before = (args.presteps if args.presteps >= 0 else vspec.meta.get("presteps", 0)) + args.warmup
             cases.append(ValidationCase(
                 make=lambda mode, params, vspec=vspec: _make_ctx(vspec, args, local, mode, params),
@@ -506,14 +550,18 @@ def train_warm_start(args, local: int, rank: int) -> tuple[object, dict]:
         key = next(iter(nets))
         nets[key].omega_max, nets[key].min_neighbors = oms[0], nmin
         choice = {"net": key, "omega_max": oms[0], "min_neighbors": nmin}
-    t3 = time.perf_counter()
-    info = {"samples": n_samples, "rollout_seeds": seeds, "substeps_per_rollout": per,
-            "target": "sum of the lambdas applied over all passes of a projected-rule substep",
-            "epochs": args.ws_epochs,
-            "loss_per_epoch": {k: [round(h, 5) for h in v[1]] for k, v in trained.items()},
-            "collect_s": round(t1 - t0, 3), "train_s": round(t2 - t1, 3), "select_s": round(t3 - t2, 3),
-            **_selection_info(choice, table, vseeds, args)}
+    info = {"select_s": round(time.perf_counter() - t0, 3), **_selection_info(choice, table, vseeds, args)}
     return (nets[choice["net"]] if choice else None), info
+
+
+def train_warm_start(args, local: int, rank: int) -> tuple[object, dict]:
+    """Untimed: one network set trained on the mixture, then the network and bound for
+    the timed workload chosen on seeds of it that neither training nor the timed scene
+    uses.  Returns (None, info) when no candidate passes: the headline then runs the
+    reference Jacobi rule."""
+    nets, info = train_mixture(args, local, rank)
+    net, sel = select_for_workload(nets, args, local, rank, args.workload)
+    return net, {**info, **sel}
 
 
 def _state_summary(ctx) -> dict:
@@ -607,6 +655,49 @@ def run_arm(spec, args, local, mode: int, net, dist, headline: bool) -> tuple[di
     if headline:
         r["_prof"], r["_dropped"], r["_clocks"], r["_window"] = prof, dropped, clk, window
     return r, ctx
+
+
+def run_warm_start_report(args) -> None:
+    """Passes saved per workload by one network set trained on the mixture.  For each
+    workload of the mixture: the network and bound chosen on its validation seeds,
+    then the reference rule, the projected rule and the learned form run on an
+    evaluation seed (3000) that neither training nor validation uses, each timed like
+    the headline (presteps and warm-up untimed, `steps` substeps with CUDA events, L2
+    flushed): passes per substep and particle-substeps/s at the same error target.
+    Prints one JSON line."""
+    import torch
+
+    from apbf_gb300 import _native as N
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    nets, info = train_mixture(args, local, 0)
+    keep = ("value", "ms_per_step", "density_passes_per_substep", "converged_substeps", "particles_mean",
+            "presteps", "state_after")
+    per = {}
+    for w in MIXTURE:
+        net, sel = select_for_workload(nets, args, local, 0, w)
+        spec = make_spec(w, seed=3000)
+        arms = {}
+        forms = [("reference_rule", 0, None), ("projected_rule", N.WARM_PROJECTED, None)]
+        if net is not None:
+            forms.append(("learned", N.WARM_LEARNED | N.WARM_PROJECTED, net))
+        for name, mode, nn in forms:
+            r, c = run_arm(spec, args, local, mode, nn, None, headline=False)
+            c.close()
+            arms[name] = {k: r[k] for k in keep}
+        row = {"chosen": sel["chosen"], "select_s": sel["select_s"], "selection": sel["selection"], "arms": arms}
+        if net is not None:
+            lp = arms["learned"]["density_passes_per_substep"]
+            for k in ("reference_rule", "projected_rule"):
+                row[f"passes_saved_vs_{k}"] = round(arms[k]["density_passes_per_substep"] - lp, 2)
+                row[f"rate_over_{k}"] = round(arms["learned"]["value"] / max(arms[k]["value"], 1e-30), 3)
+        per[w] = row
+        print(json.dumps({"workload": w, **{k: v for k, v in row.items() if k != "selection"}}), flush=True)
+    print(json.dumps({"report": "warm start trained on the mixture, per workload", "metric": METRIC, "unit": UNIT,
+                      "error_target": args.error_target, "max_iterations": args.max_iterations,
+                      "evaluation_seed": 3000, "steps": args.steps, "warmup": args.warmup,
+                      "training": info, "per_workload": per}), flush=True)
 
 
 def _device_pairs(ctx, n: int) -> np.ndarray:
@@ -1217,10 +1308,14 @@ def main() -> None:
     ap.add_argument("--ws-height-slack", type=float, default=1.25,
                     help="validation admits a warm start whose final 99th-percentile particle height is at most "
                          "this times the plain rule's (<= 0: no height condition)")
+    ap.add_argument("--warm-start-report", action="store_true",
+                    help="train one warm start on the mixture and report passes saved on each of its workloads")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.warm_start_report:
+        run_warm_start_report(args)
+    elif args.impl == "reference":
         run_reference(args)
     elif WORKLOADS[args.workload][0] == "batch":
         run_batch(args)
