@@ -891,6 +891,18 @@ def run_ours(args) -> None:
         dist.destroy_process_group()
 
 
+def batch_whole_job(seq_ms: float, seq_particles: float, e2e_s: float, e2e_particles: float, scenes: int,
+                    particles: int, dist, device) -> dict:
+    """Whole-job figures of the batch's comparison runs on N ranks, as for the headline:
+    the slowest rank's time and the particle-substeps and scenes of all ranks."""
+    seq_ms, seq_particles = reduce_over_ranks(seq_ms, seq_particles, dist, device)
+    e2e_s, e2e_particles = reduce_over_ranks(e2e_s, e2e_particles, dist, device)
+    _, scenes = reduce_over_ranks(0.0, float(scenes), dist, device)
+    _, particles = reduce_over_ranks(0.0, float(particles), dist, device)
+    return {"sequential_ms": seq_ms, "sequential_value": seq_particles / (seq_ms / 1000.0),
+            "e2e_value": e2e_particles / e2e_s, "scenes": int(scenes), "particles_total": int(particles)}
+
+
 # ----------------------------------------------------------------------------- batch
 def batch_specs(n_scenes: int, lo: int, hi: int, seed: int = 7) -> list:
     """Seeded scene table: particle counts log-uniform in [lo, hi]; every other scene a
@@ -1053,6 +1065,9 @@ def run_batch(args) -> None:
     # per-scene density error: the device's FP64 value against the oracle's FP64
     # recomputation on the same (downloaded) state, for every 8th scene
     e2e = run_batch_e2e(batch, ctxs, args, dt, windows)
+    whole = batch_whole_job(seq_ms, float(n_total * args.steps), e2e.pop("_seconds"), e2e.pop("_particles"),
+                            len(specs), n_total, dist, f"cuda:{local}")
+    e2e["value"] = whole["e2e_value"]
     check = []
     if rank == 0 and not args.no_cpu_baseline:
         from apbf_gb300.api import incompressibility, neighborhood_green
@@ -1083,7 +1098,10 @@ def run_batch(args) -> None:
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 (int32 fixed-point positions and sums; bf16 MLP)",
             "data": "synthetic (seeded scene table)",
-            "config": {"workload": args.workload, "scenes": len(specs), "particles_total": int(n_total),
+            "config": {"workload": args.workload, "scenes": whole["scenes"], "particles_total": whole["particles_total"],
+                       "per_rank_fields": (None if world == 1 else
+                                           "rank 0's own scene table: particles_min/max, adaptive_scenes, passes, "
+                                           "convergence, scene errors, oracle check, warm-start selection"),
                        "particles_min": int(min(sp.n for sp in specs)), "particles_max": int(max(sp.n for sp in specs)),
                        "adaptive_scenes": int(sum(not sp.basic_pbf for sp in specs)), "dt": dt,
                        "solver": ("learned warm start + projected Jacobi passes, per-scene convergence; "
@@ -1096,8 +1114,8 @@ def run_batch(args) -> None:
                                   (" around one persistent cooperative launch of every scene's Jacobi passes 1.."
                                    if args.batch_persistent else "")),
                        "l2": "flushed between timed steps (256 MB write)"},
-            "sequential": {"ms_per_step": seq_ms / args.steps,
-                           "value": n_total * args.steps / (seq_ms / 1000.0),
+            "sequential": {"ms_per_step": whole["sequential_ms"] / args.steps,
+                           "value": whole["sequential_value"],
                            "density_passes_per_scene_substep": seq_passes,
                            "note": "the same window of the same scenes replayed, one whole-substep graph launch "
                                    "each, one after the other"},
@@ -1161,7 +1179,7 @@ def run_batch_e2e(batch, ctxs, args, dt, windows) -> dict:
         total += sum(ns)
     el = time.perf_counter() - t0
     infos = [c.check_status() for c in ctxs]
-    return {"value": total / el, "unit": UNIT, "h2d_bytes_per_step": int(h2d / steps),
+    return {"value": total / el, "_seconds": el, "_particles": float(total), "unit": UNIT, "h2d_bytes_per_step": int(h2d / steps),
             "d2h_bytes_per_step": int(d2h / steps), "steps": steps, "warmup": min(args.warmup, steps),
             "density_passes_per_scene_substep": sum(i.density_passes for i in infos) / (len(ctxs) * steps),
             "window": "the device-resident timed window replayed from its start state",

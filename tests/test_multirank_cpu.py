@@ -31,7 +31,10 @@ def _rank_main(rank, world, port, out):
     import bench
 
     t, p = bench.reduce_over_ranks(10.0 + 5.0 * rank, 100.0 * (rank + 1), dist, "cpu")
-    out.put((rank, t, p))
+    # the batch's comparison runs: each rank its own scene table and timings
+    w = bench.batch_whole_job(seq_ms=20.0 * (rank + 1), seq_particles=1000.0 * (rank + 1), e2e_s=0.5 + rank,
+                              e2e_particles=300.0, scenes=64, particles=5000 + rank, dist=dist, device="cpu")
+    out.put((rank, t, p, w))
     dist.barrier()
     dist.destroy_process_group()
 
@@ -43,11 +46,17 @@ def test_two_ranks_aggregate_slowest_time_and_all_particles():
     procs = [ctx.Process(target=_rank_main, args=(r, 2, port, q)) for r in range(2)]
     for p in procs:
         p.start()
-    res = sorted(q.get(timeout=120) for _ in procs)
+    res = sorted((q.get(timeout=120) for _ in procs), key=lambda r: r[0])
     for p in procs:
         p.join(timeout=60)
     assert [p.exitcode for p in procs] == [0, 0]
-    assert res == [(0, 15.0, 300.0), (1, 15.0, 300.0)]
+    assert [r[:3] for r in res] == [(0, 15.0, 300.0), (1, 15.0, 300.0)]
+    # batch: every whole-job field is the same on both ranks: slowest time, all ranks' work
+    for _, _, _, w in res:
+        assert w["sequential_ms"] == 40.0
+        assert w["sequential_value"] == 3000.0 / 0.040
+        assert w["e2e_value"] == 600.0 / 1.5
+        assert w["scenes"] == 128 and w["particles_total"] == 10001
 
 
 def test_one_process_is_unchanged():
