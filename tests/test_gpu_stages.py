@@ -1,8 +1,10 @@
 """The reference's operator API as a binding would use it: the stage objects
 (set_data / apply) run in pool::update order (SubstepStages.update) give the state
 that apbf_substep gives, bit for bit, over several substeps of a plain and of an
-adaptive scene.  apbf_substep fuses the box passes into the kernels before them and
-runs the passes from graphs; the stages launch every pass on its own."""
+adaptive scene, and of a small waterfall's pre-filled stream over its oriented slope
+box (the stage objects have no emitter stage, so the emitter is off).  apbf_substep
+fuses the box passes into the kernels before them and runs the passes from graphs;
+the stages launch every pass on its own."""
 import numpy as np
 import pytest
 
@@ -20,12 +22,15 @@ def _ctx(spec, maxn):
     return ctx
 
 
-@pytest.mark.parametrize("name", ["dam_break", "water_drop_adaptive"])
+@pytest.mark.parametrize("name", ["dam_break", "water_drop_adaptive", "waterfall"])
 def test_stage_objects_equal_substep(name):
     from apbf_gb300.api import SubstepStages
 
     if name == "dam_break":
         spec, maxn, steps = scenes.dam_break(n_side=14, seed=2), 128, 8
+    elif name == "waterfall":
+        spec, maxn, steps = scenes.waterfall(initial=12_000, seed=3, scale=0.35, per_substep=300), 256, 60
+        spec.meta["emitter"] = None
     else:
         spec, maxn, steps = scenes.water_drop(total=20_000, seed=4, basic_pbf=False), 256, 40
     fused, staged = _ctx(spec, maxn), _ctx(spec, maxn)
