@@ -61,7 +61,8 @@ def make_spec(name: str, seed: int = 0, scale: float = 1.0):
     kw = dict(kw)
     if "total" in kw:
         kw["total"] = int(kw["total"] * scale)
-    if factory == "dam_break":
+    if factory == "dam_break":  # a cube of n_side^3 particles: scale its side
+        kw["n_side"] = max(4, int(round(kw["n_side"] * scale ** (1.0 / 3.0))))
         return scenes.dam_break(seed=seed, **kw)
     if factory == "waterfall":
         spec = scenes.waterfall(initial=int(kw["initial"] * scale), seed=seed, basic_pbf=kw["basic_pbf"],
@@ -269,6 +270,15 @@ def cpu_baseline(workload: str, budget_s: float = 15.0) -> dict:
             "fp32": fp32}
 
 
+def _product_library_mapped() -> bool:
+    """Whether this process has mapped the library under test (Linux /proc)."""
+    try:
+        with open("/proc/self/maps") as f:
+            return any("libapbf_gb300" in line for line in f)
+    except OSError:
+        return False
+
+
 def _replica_loop(conn, name, scale, seed, presteps):
     """One replica of the reference arm: builds its scene, brings it to the phase the
     GPU arm times (the scene's untimed substeps, with the scene's fixed iteration
@@ -299,7 +309,7 @@ def _replica_loop(conn, name, scale, seed, presteps):
     for _ in range(presteps):
         advance()
     sc.settings.density_error_target, sc.settings.solver_iterations = target, iters
-    conn.send((int(fs.n), orc.LIB.name))
+    conn.send((int(fs.n), orc.LIB.name, _product_library_mapped()))
     while True:
         k = conn.recv()
         if k is None:
@@ -348,6 +358,7 @@ def run_reference(args) -> None:
     built = [c.recv() for c in pipes]  # (particles, oracle library) once the scenes are built
     counts = [b[0] for b in built]
     libraries = sorted({b[1] for b in built})
+    product_mapped = _product_library_mapped() or any(b[2] for b in built)
 
     def step():
         for c in pipes:
@@ -374,7 +385,7 @@ def run_reference(args) -> None:
         "data": "synthetic (seeded scene generator)",
         "config": {"workload": args.workload, "sample_particles": n_sample, "sample_scale": scale,
                    "replicas": cores, "presteps": presteps, "oracle_build": args.oracle_variant,
-                   "oracle_library": libraries,
+                   "oracle_library": libraries, "product_library_mapped": product_mapped,
                    "iterations": "until mean density error <= 0.001 (max 100), reference Jacobi rule"},
         "impl": "reference",
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
@@ -849,7 +860,7 @@ def run_ours(args) -> None:
         if check:
             parity = {k: check[k] for k in ("morton_keys_bit_exact", "sort_permutation_bit_exact",
                                              "neighbor_sets_equal", "density_error_device_fp32",
-                                             "density_error_oracle_fp64")}
+                                             "density_error_oracle_fp64", "what")}
         fidelity = None
         if plain and head.get("state_after"):
             e = head["state_after"]["mean_v2"]
