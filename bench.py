@@ -545,8 +545,12 @@ def select_for_workload(nets: dict, args, local: int, rank: int, workload: str) 
     t0 = time.perf_counter()
     _, oms = _ws_choices(args)
     nmin = args.ws_min_neighbors if args.ws_min_neighbors is not None else 16.0
+    # seeds of the validation: a candidate must stay within the slacks on every one, so
+    # more seeds keep a candidate at the edge of a slack from passing by chance (with
+    # two seeds, the water drop admitted splashes of 1.2x that reached 1.34-1.51x on
+    # other seeds)
     large = make_spec(workload).n >= 500_000 or workload.startswith("waterfall")
-    vseeds = [1000 + 10 * rank + k for k in ((3,) if large else (3, 4))]
+    vseeds = [1000 + 10 * rank + k for k in ((3, 4) if large else (3, 4, 5, 6))]
     table = None
     if len(nets) * len(oms) > 1:
         cases = []
@@ -634,6 +638,9 @@ def run_arm(spec, args, local, mode: int, net, dist, headline: bool) -> tuple[di
     total_ms = float(np.sum([a.elapsed_time(b) for a, b in ev]))
     info = ctx.check_status()
     n_end, _ = ctx.lengths()
+    # the end state of the timed window, before the traced substeps below: every arm
+    # (headline and plain) is compared at the same substep
+    state_after = _state_summary(ctx)
     prof, dropped = {}, 0
     if headline and args.prof_steps > 0:
         # per-kernel CUDA events on a few more substeps with the same pass count and
@@ -662,7 +669,7 @@ def run_arm(spec, args, local, mode: int, net, dist, headline: bool) -> tuple[di
          "converged_substeps": f"{info.converged_substeps}/{args.steps}", "pairs": int(info.pairs),
          "particles_after": int(n_end), "presteps": presteps, "total_ms": total_ms, "gpu_launches": int(launches),
          "tuning": tuning,
-         "state_after": _state_summary(ctx)}
+         "state_after": state_after}
     if headline:
         r["_prof"], r["_dropped"], r["_clocks"], r["_window"] = prof, dropped, clk, window
     return r, ctx

@@ -1,7 +1,7 @@
 """The warm start's training mixture (bench.training_rollouts): rollouts of the dam
 break, the adaptive water drop and the adaptive waterfall, about 60 M samples in
 all, on seeds that neither a timed scene (seed = rank), a validation scene
-(1000 + 10 rank + 3, 4) nor the per-workload evaluation scene (3000) uses."""
+(1000 + 10 rank + 3..6) nor the per-workload evaluation scene (3000) uses."""
 import sys
 from pathlib import Path
 
@@ -39,7 +39,7 @@ def test_mixture_seeds_are_held_out():
 
     for world in (1, 2, 8):
         timed = set(range(world))
-        valid = {1000 + 10 * r + k for r in range(world) for k in (3, 4)}
+        valid = {1000 + 10 * r + k for r in range(world) for k in (3, 4, 5, 6)}
         train = {p[1] for r in range(world) for p in bench.training_rollouts(r)}
         assert not train & timed
         assert not train & valid
