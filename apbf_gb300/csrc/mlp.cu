@@ -5,8 +5,10 @@
 // lambda, velocity divergence, the previous substep's applied lambda sum and its
 // neighbour mean) to an initial lambda that replaces the plain one in the first
 // position update.  Weights are BF16 on the tensor cores with FP32
-// accumulation: inference with tcgen05.mma into TMEM (k_mlp_tc), training with
-// mma.sync m16n8k16 (k_mlp_grad); the master copy is FP32.
+// accumulation: inference with tcgen05.mma into TMEM (k_mlp_tc); training
+// (k_mlp_grad) runs the per-row forward and backward on mma.sync m16n8k16 and the two
+// weight-gradient GEMMs, sums over the CTA's rows, as one tcgen05.mma into TMEM; the
+// master copy is FP32.
 //
 // Parameter vector (FP32), offsets in floats:
 //   0 mu[8]  8 inv_sigma[8]  16 W1[64][8]  528 b1[64]  592 W2[64][64]  4688 b2[64]
@@ -42,7 +44,6 @@ constexpr int kRowsWarp = 32;   // rows per warp (two m16 tiles)
 constexpr int kWarps = 4;
 constexpr int kRowsCta = kRowsWarp * kWarps;
 constexpr int kLd = 72;         // bf16 row stride of 64-wide tiles in shared memory (bank-conflict free)
-constexpr int kLdT = kRowsCta + 8;  // bf16 row stride of transposed [64][128] tiles
 
 namespace {
 
@@ -243,6 +244,13 @@ __device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t a, uint64_t b, 
         "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
         "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
         "l"(a), "l"(b), "r"(kTcIdesc), "r"(accumulate));
+}
+__device__ __forceinline__ void tc_mma_id(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate,
+                                          uint32_t idesc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
 }
 __device__ __forceinline__ void tc_commit(unsigned long long *bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
@@ -505,9 +513,24 @@ static int tc_grid(uint32_t rows) {
     return (int)std::max(1u, std::min(tiles, cap));
 }
 
-constexpr size_t kGradOffT = (sizeof(SmemW) + 15) / 16 * 16;
-constexpr size_t kGradSmem = kGradOffT + (size_t)(3 * kH + 16) * kLdT * sizeof(__nv_bfloat16) +
-                             (size_t)kWarps * (3 * kH + 2) * sizeof(float);
+// Weight gradients as one GEMM on the tensor cores: D (M 128 x N 80, FP32 in TMEM)
+// = A B^T summed over the CTA's 128 rows (K), A = [dH2^T; dH1^T] (rows 0..63: the
+// hidden-2 deltas, 64..127: the hidden-1 deltas) and B = [h1^T; x^T] (rows 0..63:
+// relu(layer 1), 64..79: the 16 feature slots, 8..15 zero), both K-major in the
+// canonical layout without swizzle.  Rows 0..63, columns 0..63 of D are dW2; rows
+// 64..127, columns 64..71 are dW1 (the off-diagonal blocks are not used).
+constexpr uint32_t kGradN = 80;
+constexpr uint32_t kGradCols = 128;  // TMEM columns: a power of two >= kGradN
+constexpr uint32_t kGradIdesc = (1u << 4)                   // D: FP32
+                                | (1u << 7) | (1u << 10)     // A, B: BF16
+                                | ((kGradN >> 3) << 17)      // N = 80
+                                | ((128u >> 4) << 24);       // M = 128; A and B K-major
+constexpr size_t kGradOffA = (sizeof(SmemW) + 1023) / 1024 * 1024;
+constexpr size_t kGradOffB = kGradOffA + (size_t)128 * kRowsCta * 2;
+constexpr size_t kGradOffR = kGradOffB + (size_t)kGradN * kRowsCta * 2;
+constexpr size_t kGradOffBar = kGradOffR + (size_t)kWarps * (3 * kH + 2) * sizeof(float);
+constexpr size_t kGradSmem = kGradOffBar + 16;
+static_assert(kRowsCta == 128, "the weight-gradient GEMM takes K = 128 rows per CTA");
 
 // Training: forward + backward of one CTA's 128 rows; the CTA's gradient (sum over
 // its rows of d loss / d param) goes to partials[blockIdx.x][param];
@@ -519,16 +542,32 @@ constexpr size_t kGradSmem = kGradOffT + (size_t)(3 * kH + 16) * kLdT * sizeof(_
 __global__ void __launch_bounds__(kRowsCta) k_mlp_grad(const float *__restrict__ P, const float *__restrict__ X,
                                                         const float *__restrict__ T, uint32_t nrows,
                                                         float over_weight, float *__restrict__ partials) {
-    extern __shared__ __align__(16) unsigned char smem[];
+    extern __shared__ __align__(1024) unsigned char smem[];
     SmemW &w = *reinterpret_cast<SmemW *>(smem);
-    __nv_bfloat16 *dh2t = reinterpret_cast<__nv_bfloat16 *>(smem + kGradOffT);   // [n][row]
-    __nv_bfloat16 *h1t = dh2t + kH * kLdT;                                        // [k][row]
-    __nv_bfloat16 *dh1t = h1t + kH * kLdT;                                        // [n][row]
-    __nv_bfloat16 *xt = dh1t + kH * kLdT;                                         // [f][row]
-    float(*red)[3 * kH + 2] = reinterpret_cast<float(*)[3 * kH + 2]>(xt + 16 * kLdT);  // per warp
+    unsigned char *ga = smem + kGradOffA;  // A of the weight-gradient GEMM (M 128 x K 128)
+    unsigned char *gb = smem + kGradOffB;  // B (N 80 x K 128)
+    float(*red)[3 * kH + 2] = reinterpret_cast<float(*)[3 * kH + 2]>(smem + kGradOffR);  // per warp
+    unsigned long long *bar = reinterpret_cast<unsigned long long *>(smem + kGradOffBar);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + kGradOffBar + 8);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, q = lane & 3;
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(kGradCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+        tc_fence_before();
+    }
     load_weights(w, P);
     __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, q = lane & 3;
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    auto put = [](unsigned char *op, int row, int k, float v) {
+        *reinterpret_cast<__nv_bfloat16 *>(op + core_off((uint32_t)row, (uint32_t)k, kRowsCta)) = __float2bfloat16_rn(v);
+    };
     const uint32_t base = blockIdx.x * kRowsCta;
     const uint32_t row0 = base + warp * kRowsWarp;
     const float inv_b = 1.0f / (float)nrows;
@@ -591,35 +630,39 @@ __global__ void __launch_bounds__(kRowsCta) k_mlp_grad(const float *__restrict__
             db1[j][0] += dh1[j][0] + dh1[j][2];
             db1[j][1] += dh1[j][1] + dh1[j][3];
         }
-        // stage transposed tiles for the weight-gradient GEMMs
-        const int lr0 = warp * kRowsWarp + 16 * t + g, lr1 = lr0 + 8;  // local rows
+        // the operands of the weight-gradient GEMM: local row = K index
+        const int lr0 = warp * kRowsWarp + 16 * t + g, lr1 = lr0 + 8;
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
             const int c0 = 8 * j + 2 * q, c1 = c0 + 1;
-            dh2t[c0 * kLdT + lr0] = __float2bfloat16_rn(dh2[j][0]);
-            dh2t[c1 * kLdT + lr0] = __float2bfloat16_rn(dh2[j][1]);
-            dh2t[c0 * kLdT + lr1] = __float2bfloat16_rn(dh2[j][2]);
-            dh2t[c1 * kLdT + lr1] = __float2bfloat16_rn(dh2[j][3]);
-            h1t[c0 * kLdT + lr0] = __float2bfloat16_rn(A.h1[t][j][0]);
-            h1t[c1 * kLdT + lr0] = __float2bfloat16_rn(A.h1[t][j][1]);
-            h1t[c0 * kLdT + lr1] = __float2bfloat16_rn(A.h1[t][j][2]);
-            h1t[c1 * kLdT + lr1] = __float2bfloat16_rn(A.h1[t][j][3]);
-            dh1t[c0 * kLdT + lr0] = __float2bfloat16_rn(dh1[j][0]);
-            dh1t[c1 * kLdT + lr0] = __float2bfloat16_rn(dh1[j][1]);
-            dh1t[c0 * kLdT + lr1] = __float2bfloat16_rn(dh1[j][2]);
-            dh1t[c1 * kLdT + lr1] = __float2bfloat16_rn(dh1[j][3]);
+            put(ga, c0, lr0, dh2[j][0]);
+            put(ga, c1, lr0, dh2[j][1]);
+            put(ga, c0, lr1, dh2[j][2]);
+            put(ga, c1, lr1, dh2[j][3]);
+            put(ga, kH + c0, lr0, dh1[j][0]);
+            put(ga, kH + c1, lr0, dh1[j][1]);
+            put(ga, kH + c0, lr1, dh1[j][2]);
+            put(ga, kH + c1, lr1, dh1[j][3]);
+            put(gb, c0, lr0, A.h1[t][j][0]);
+            put(gb, c1, lr0, A.h1[t][j][1]);
+            put(gb, c0, lr1, A.h1[t][j][2]);
+            put(gb, c1, lr1, A.h1[t][j][3]);
         }
-        // normalised features (A fragment a0/a1 hold columns 2q, 2q+1 of rows g, g+8)
+        // normalised features (A fragment a0/a1 hold columns 2q, 2q+1 of rows g, g+8),
+        // slots 8..15 zero
         const __nv_bfloat162 x0 = *reinterpret_cast<const __nv_bfloat162 *>(&A.x[t][0]);
         const __nv_bfloat162 x1 = *reinterpret_cast<const __nv_bfloat162 *>(&A.x[t][1]);
-        xt[(2 * q) * kLdT + lr0] = x0.x;
-        xt[(2 * q + 1) * kLdT + lr0] = x0.y;
-        xt[(2 * q) * kLdT + lr1] = x1.x;
-        xt[(2 * q + 1) * kLdT + lr1] = x1.y;
-        xt[(2 * q + 8) * kLdT + lr0] = __float2bfloat16_rn(0.0f);
-        xt[(2 * q + 9) * kLdT + lr0] = __float2bfloat16_rn(0.0f);
-        xt[(2 * q + 8) * kLdT + lr1] = __float2bfloat16_rn(0.0f);
-        xt[(2 * q + 9) * kLdT + lr1] = __float2bfloat16_rn(0.0f);
+        const auto putb = [&](int row, int k, __nv_bfloat16 v) {
+            *reinterpret_cast<__nv_bfloat16 *>(gb + core_off((uint32_t)(kH + row), (uint32_t)k, kRowsCta)) = v;
+        };
+        putb(2 * q, lr0, x0.x);
+        putb(2 * q + 1, lr0, x0.y);
+        putb(2 * q, lr1, x1.x);
+        putb(2 * q + 1, lr1, x1.y);
+        putb(2 * q + 8, lr0, __float2bfloat16_rn(0.0f));
+        putb(2 * q + 9, lr0, __float2bfloat16_rn(0.0f));
+        putb(2 * q + 8, lr1, __float2bfloat16_rn(0.0f));
+        putb(2 * q + 9, lr1, __float2bfloat16_rn(0.0f));
     }
     // warp reductions of the vector gradients over the 8 row groups (lanes with equal q)
 #pragma unroll
@@ -662,61 +705,50 @@ __global__ void __launch_bounds__(kRowsCta) k_mlp_grad(const float *__restrict__
         else if (t == 3 * kH) out[kP_B3] = v;
         else out[kP_N - 1] = v;
     }
-    // dW2[n][k] = sum_r dH2[r][n] h1[r][k]: warp w owns rows n of m-tile w
-    {
-        const int m0 = 16 * warp;
-        float acc[8][4];
+    // dW2 and dW1 on the tensor cores: one thread issues the 8 K-steps of 16 rows,
+    // the commit arrives on the mbarrier, and thread t reads row t of D from its lane
+    fence_async_smem();  // the operands written above, for the tensor core's proxy
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (threadIdx.x == 0) {
 #pragma unroll
-        for (int j = 0; j < 8; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.0f;
-#pragma unroll
-        for (int s = 0; s < kRowsCta / 16; ++s) {
-            uint32_t a[4];
-            a[0] = *reinterpret_cast<const uint32_t *>(&dh2t[(m0 + g) * kLdT + 16 * s + 2 * q]);
-            a[1] = *reinterpret_cast<const uint32_t *>(&dh2t[(m0 + g + 8) * kLdT + 16 * s + 2 * q]);
-            a[2] = *reinterpret_cast<const uint32_t *>(&dh2t[(m0 + g) * kLdT + 16 * s + 8 + 2 * q]);
-            a[3] = *reinterpret_cast<const uint32_t *>(&dh2t[(m0 + g + 8) * kLdT + 16 * s + 8 + 2 * q]);
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                const int k = 8 * j + g;
-                const uint32_t b0 = *reinterpret_cast<const uint32_t *>(&h1t[k * kLdT + 16 * s + 2 * q]);
-                const uint32_t b1 = *reinterpret_cast<const uint32_t *>(&h1t[k * kLdT + 16 * s + 8 + 2 * q]);
-                mma16816(acc[j], a, b0, b1);
-            }
-        }
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            const int c = 8 * j + 2 * q;
-            out[kP_W2 + (m0 + g) * kH + c] = acc[j][0];
-            out[kP_W2 + (m0 + g) * kH + c + 1] = acc[j][1];
-            out[kP_W2 + (m0 + g + 8) * kH + c] = acc[j][2];
-            out[kP_W2 + (m0 + g + 8) * kH + c + 1] = acc[j][3];
-        }
+        for (int k = 0; k < kRowsCta / 16; ++k)
+            tc_mma_id(tmem, tc_desc(ga + 256 * k, 128u, kRowsCta * 16u), tc_desc(gb + 256 * k, 128u, kRowsCta * 16u),
+                      k > 0 ? 1u : 0u, kGradIdesc);
+        tc_commit(bar);
     }
-    // dW1[n][f] = sum_r dH1[r][n] x[r][f]
-    {
-        const int m0 = 16 * warp;
-        float acc[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+    const bool ok = __syncthreads_and(mbar_wait(bar, 0u)) != 0;
+    const int tr = threadIdx.x;  // row of D (its TMEM lane)
+    const uint32_t lane_tmem = tmem + ((uint32_t)(warp * 32) << 16);
+    if (ok) {
+        tc_fence_after();
+        if (warp < 2) {  // rows 0..63: dW2[tr][0..63]
 #pragma unroll
-        for (int s = 0; s < kRowsCta / 16; ++s) {
-            uint32_t a[4];
-            a[0] = *reinterpret_cast<const uint32_t *>(&dh1t[(m0 + g) * kLdT + 16 * s + 2 * q]);
-            a[1] = *reinterpret_cast<const uint32_t *>(&dh1t[(m0 + g + 8) * kLdT + 16 * s + 2 * q]);
-            a[2] = *reinterpret_cast<const uint32_t *>(&dh1t[(m0 + g) * kLdT + 16 * s + 8 + 2 * q]);
-            a[3] = *reinterpret_cast<const uint32_t *>(&dh1t[(m0 + g + 8) * kLdT + 16 * s + 8 + 2 * q]);
+            for (int c = 0; c < 4; ++c) {
+                float v[16];
+                tmem_ld16(lane_tmem + 16u * c, v);
 #pragma unroll
-            for (int j = 0; j < 2; ++j) {
-                const int f = 8 * j + g;
-                const uint32_t b0 = *reinterpret_cast<const uint32_t *>(&xt[f * kLdT + 16 * s + 2 * q]);
-                const uint32_t b1 = *reinterpret_cast<const uint32_t *>(&xt[f * kLdT + 16 * s + 8 + 2 * q]);
-                mma16816(acc[j], a, b0, b1);
+                for (int i = 0; i < 16; ++i) out[kP_W2 + tr * kH + 16 * c + i] = v[i];
             }
+        } else {  // rows 64..127, columns 64..71: dW1[tr - 64][0..7]
+            float v[16];
+            tmem_ld16(lane_tmem + 64u, v);
+#pragma unroll
+            for (int f = 0; f < kF; ++f) out[kP_W1 + (tr - kH) * kF + f] = v[f];
         }
-        // only features 0..7 are parameters (tile j = 0)
-        const int c = 2 * q;
-        out[kP_W1 + (m0 + g) * kF + c] = acc[0][0];
-        out[kP_W1 + (m0 + g) * kF + c + 1] = acc[0][1];
-        out[kP_W1 + (m0 + g + 8) * kF + c] = acc[0][2];
-        out[kP_W1 + (m0 + g + 8) * kF + c + 1] = acc[0][3];
+    } else {
+        // the MMA did not complete in time: wait (bounded) before the TMEM is freed, and
+        // mark the weight gradients NaN (the loss and the parameters show it)
+        mbar_wait(bar, 0u);
+        for (int t = tr; t < kH * kH; t += blockDim.x) out[kP_W2 + t] = __int_as_float(0x7fc00000);
+        for (int t = tr; t < kH * kF; t += blockDim.x) out[kP_W1 + t] = __int_as_float(0x7fc00000);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kGradCols) : "memory");
     }
 }
 
