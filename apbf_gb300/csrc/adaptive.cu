@@ -52,15 +52,40 @@ __global__ void k_fsm12(const int4 *__restrict__ pos, const uint32_t *__restrict
         const int4 p = pos[i];
         uint32_t bd = 0xffffffffu, md = 0xffffffffu, nn = 0xffffffffu;
         const uint32_t c = count[i];
-        for (uint32_t k = 0; k < c; ++k) {
-            const uint32_t j = idx[(size_t)k * stride + i];
-            const uint32_t d = fixed_dist(p, pos[j]);
-            const uint32_t cand = old_bd[j] + d;  // uint wrap as in the shader
-            bd = cand < bd ? cand : bd;
-            if (d < md || (d == md && j < nn)) {
-                md = d;
-                nn = j;
+        const uint32_t *row = idx + i;
+        // batches of four neighbours, software-pipelined: a batch's gathers go out with
+        // the row entries of the next (the minima do not depend on the order)
+        constexpr uint32_t U = 4;
+        uint32_t jj[U];
+#pragma unroll
+        for (uint32_t u = 0; u < U; ++u) jj[u] = u < c ? row[(size_t)u * stride] : i;
+        for (uint32_t k0 = 0; k0 < c; k0 += U) {
+            int4 q[U];
+            uint32_t ob[U], jn[U];
+#pragma unroll
+            for (uint32_t u = 0; u < U; ++u) {
+                q[u] = pos[jj[u]];
+                ob[u] = old_bd[jj[u]];
             }
+#pragma unroll
+            for (uint32_t u = 0; u < U; ++u) {
+                const uint32_t k = k0 + U + u;
+                jn[u] = k < c ? row[(size_t)k * stride] : i;
+            }
+#pragma unroll
+            for (uint32_t u = 0; u < U; ++u) {
+                if (k0 + u >= c) break;
+                const uint32_t j = jj[u];
+                const uint32_t d = fixed_dist(p, q[u]);
+                const uint32_t cand = ob[u] + d;  // uint wrap as in the shader
+                bd = cand < bd ? cand : bd;
+                if (d < md || (d == md && j < nn)) {
+                    md = d;
+                    nn = j;
+                }
+            }
+#pragma unroll
+            for (uint32_t u = 0; u < U; ++u) jj[u] = jn[u];
         }
         new_bd[i] = bd;
         nearest[i] = nn;
