@@ -444,15 +444,41 @@ __global__ void k_kw_spread(FluidBufs f, uint32_t *ukw, uint32_t *count, uint32_
         const float cut = fmaxf(ok, f.kernel_width[i]);
         const uint32_t c = count[i];
         uint32_t w = 0;
-        for (uint32_t k = 0; k < c; ++k) {
-            const uint32_t j = idx[(size_t)k * stride + i];
-            const int4 q = f.pos[j];
-            const float dx = (float)wadd(q.x, -p.x) / 262144.0f, dy = (float)wadd(q.y, -p.y) / 262144.0f,
-                        dz = (float)wadd(q.z, -p.z) / 262144.0f;
-            const float dist = sqrtf((dx * dx + dy * dy) + dz * dz);
-            const float infl = fmaxf(0.0f, 1.0f - fmaxf(0.0f, (dist - ok) / (ok * 0.5f)));
-            atomicMax(&ukw[j], f2u((ok * infl) * 262144.0f));
-            if (dist <= cut) idx[(size_t)(w++) * stride + i] = j;
+        // batches of four neighbours, software-pipelined (the pruned row is written
+        // behind the entries read ahead); a maximum only grows, so an atomic whose value
+        // a plain read already meets or exceeds would change nothing and is left out
+        constexpr uint32_t U = 4;
+        uint32_t *row = idx + i;
+        uint32_t jj[U];
+#pragma unroll
+        for (uint32_t u = 0; u < U; ++u) jj[u] = u < c ? row[(size_t)u * stride] : i;
+        for (uint32_t k0 = 0; k0 < c; k0 += U) {
+            int4 q[U];
+            uint32_t cur[U], jn[U];
+#pragma unroll
+            for (uint32_t u = 0; u < U; ++u) {
+                q[u] = f.pos[jj[u]];
+                cur[u] = *(volatile const uint32_t *)&ukw[jj[u]];
+            }
+#pragma unroll
+            for (uint32_t u = 0; u < U; ++u) {
+                const uint32_t k = k0 + U + u;
+                jn[u] = k < c ? row[(size_t)k * stride] : i;
+            }
+#pragma unroll
+            for (uint32_t u = 0; u < U; ++u) {
+                if (k0 + u >= c) break;
+                const uint32_t j = jj[u];
+                const float dx = (float)wadd(q[u].x, -p.x) / 262144.0f, dy = (float)wadd(q[u].y, -p.y) / 262144.0f,
+                            dz = (float)wadd(q[u].z, -p.z) / 262144.0f;
+                const float dist = sqrtf((dx * dx + dy * dy) + dz * dz);
+                const float infl = fmaxf(0.0f, 1.0f - fmaxf(0.0f, (dist - ok) / (ok * 0.5f)));
+                const uint32_t v = f2u((ok * infl) * 262144.0f);
+                if (v > cur[u]) atomicMax(&ukw[j], v);
+                if (dist <= cut) row[(size_t)(w++) * stride] = j;
+            }
+#pragma unroll
+            for (uint32_t u = 0; u < U; ++u) jj[u] = jn[u];
         }
         count[i] = w;
     }

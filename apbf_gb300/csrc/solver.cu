@@ -416,16 +416,37 @@ __device__ __forceinline__ void density_one(const PassA &a, const int4 *__restri
             }
         } else if (a.method == 2 && b > 0.0f) {
             float3 ed;
-            if (filter_dir(gx, gy, gz, ed)) {
+            if (GAUSS && filter_dir(gx, gy, gz, ed)) {
+                // batches of kUnroll neighbours in row order, software-pipelined as the
+                // sums above (the first hit ends the test, as in the plain loop)
+                uint32_t fj[kUnroll];
+#pragma unroll
+                for (int u = 0; u < kUnroll; ++u) fj[u] = (uint32_t)u < cnt ? row[(size_t)u * a.stride] : i;
+                bool hit = false;
+                for (uint32_t k0 = 0; k0 < cnt && !hit; k0 += kUnroll) {
+                    int4 fq[kUnroll];
+                    uint32_t fn[kUnroll];
+#pragma unroll
+                    for (int u = 0; u < kUnroll; ++u) fq[u] = pos[fj[u]];
+#pragma unroll
+                    for (int u = 0; u < kUnroll; ++u) {
+                        const uint32_t k = k0 + kUnroll + u;
+                        fn[u] = k < cnt ? row[(size_t)k * a.stride] : i;
+                    }
+#pragma unroll
+                    for (int u = 0; u < kUnroll; ++u) {
+                        if (hit || k0 + u >= cnt) break;
+                        hit = gauss_filter_hit(ed, fdiff(p, fq[u]));
+                    }
+#pragma unroll
+                    for (int u = 0; u < kUnroll; ++u) fj[u] = fn[u];
+                }
+                if (hit) b = 0.0f;
+            } else if (!GAUSS && filter_dir(gx, gy, gz, ed)) {
                 for (uint32_t k = 0; k < cnt; ++k) {
                     const uint32_t j = a.idx[(size_t)k * a.stride + i];
                     const float3 d = fdiff(p, pos[j]);
-                    if (GAUSS) {
-                        if (gauss_filter_hit(ed, d)) {
-                            b = 0.0f;
-                            break;
-                        }
-                    } else {
+                    {
                         float W;
                         float3 g;
                         pair_terms<GAUSS>(a.hk, a.gk, d, kw, c, W, g);
