@@ -330,16 +330,27 @@ __global__ void k_reverse_rows(const uint32_t *d_len, uint32_t stride, uint32_t 
     if (blockIdx.x == 0 && threadIdx.x == 0) st->union_rows = 0u;
     if (st->range_min == st->range_max) return;  // symmetric rows: reverse = forward
     uint32_t n = d_len[kLenParticles];
+    // four entries per batch: their slot atomics are in flight together (the slots'
+    // order within a reverse row is arbitrary either way, and the position update's
+    // integer sums do not depend on it)
+    constexpr uint32_t U = 4;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        uint32_t c = count[i];
-        for (uint32_t k = 0; k < c; ++k) {
-            uint32_t j = idx[(size_t)k * stride + i];
-            uint32_t slot = atomicAdd(&rcount[j], 1u);
-            if (slot < maxn) {
-                ridx[(size_t)slot * stride + j] = i;
-            } else {
-                set_flag(st, APBF_FLAG_NEIGHBOR_OVERFLOW);
-                atomicMax(&st->required_neighbors, slot + 1u);
+        const uint32_t c = count[i];
+        for (uint32_t k0 = 0; k0 < c; k0 += U) {
+            uint32_t j[U], slot[U];
+#pragma unroll
+            for (uint32_t u = 0; u < U; ++u) j[u] = k0 + u < c ? idx[(size_t)(k0 + u) * stride + i] : 0u;
+#pragma unroll
+            for (uint32_t u = 0; u < U; ++u) slot[u] = k0 + u < c ? atomicAdd(&rcount[j[u]], 1u) : 0u;
+#pragma unroll
+            for (uint32_t u = 0; u < U; ++u) {
+                if (k0 + u >= c) break;
+                if (slot[u] < maxn) {
+                    ridx[(size_t)slot[u] * stride + j[u]] = i;
+                } else {
+                    set_flag(st, APBF_FLAG_NEIGHBOR_OVERFLOW);
+                    atomicMax(&st->required_neighbors, slot[u] + 1u);
+                }
             }
         }
     }
