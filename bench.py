@@ -37,7 +37,7 @@ UNIT = "particle-substeps/s"
 
 WORKLOADS = {
     # name: (scene factory, description)
-    # config 1: split/merge with kernel widths spread across neighbours (the
+    # the 250 k water drop with split/merge and kernel widths spread across neighbours (the
     # spread_kernel_width path, pool.cpp:87-89, taken when the widths do not come from
     # the boundary distance); target radii from 1 at the surface to 2 at the pool's
     # floor (volume ratios 1x-8x): scale factor 1/40 per radius of boundary distance
@@ -939,7 +939,7 @@ def batch_specs(n_scenes: int, lo: int, hi: int, seed: int = 7) -> list:
 
 
 def run_batch(args) -> None:
-    """Config-4 style throughput: many independent scenes of uneven sizes advanced by
+    """Batch throughput: many independent scenes of uneven sizes advanced by
     one graph launch per substep (their substeps are the graph's parallel branches),
     against the same scenes advanced one after the other."""
     import torch

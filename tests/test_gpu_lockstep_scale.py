@@ -1,6 +1,6 @@
-"""Whole substeps at the configurations' scale in stage lockstep with the FP64
-oracle: a 32 768-particle dam break (config 0), a waterfall after its emitter has
-brought it past 100 000 particles (config 2, lengths scaled by 1/2), and an
+"""Whole substeps at the benched scenes' scale in stage lockstep with the FP64
+oracle: a 32 768-particle dam break, a waterfall after its emitter has brought it
+past 100 000 particles (the 1 M waterfall with lengths scaled by 1/2), and an
 adaptive water drop whose kernel widths are spread across neighbours
 (base_kernel_width_on_boundary_distance off, the spread_kernel_width path of
 pool.cpp:87-89).  Each stage of a substep runs on the device; the oracle starts
