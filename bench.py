@@ -219,7 +219,7 @@ def oracle_boxes(spec) -> tuple:
 def cpu_sample(workload: str, budget_s: float = 15.0) -> dict:
     """The single-threaded oracle on a bounded sample: the same scene at 1/8 of the
     particle count (every length halved), substeps until the budget is spent.  The
-    oracle library is the FP64 checker, or its FP32 build when the process was
+    oracle library is the FP64 oracle, or its FP32 build when the process was
     started with APBF_ORACLE_VARIANT=f32."""
     from oracle import oracle as orc
 
@@ -247,7 +247,7 @@ def cpu_sample(workload: str, budget_s: float = 15.0) -> dict:
 
 
 def cpu_baseline(workload: str, budget_s: float = 15.0) -> dict:
-    """The oracle timed on this host: the FP64 checker in this process, then the FP32
+    """The oracle timed on this host: the FP64 oracle in this process, then the FP32
     build of the same code in a child process (same sample, same single thread)."""
     r64 = cpu_sample(workload, budget_s)
     env = dict(os.environ, APBF_ORACLE_VARIANT="f32")
@@ -326,7 +326,7 @@ def run_reference(args) -> None:
     as independent replicas of a bounded sample of the scene (1/8 of its particles).
     By default the replicas run the oracle's FP32 build (the reference's shaders
     compute in FP32, and it is the faster CPU form); --oracle-variant f64 runs the
-    FP64 checker.  Each replica builds its scene once; a step is one substep of every
+    FP64 oracle.  Each replica builds its scene once; a step is one substep of every
     replica, timed from the command to the last answer."""
     import multiprocessing as mp
 
@@ -395,7 +395,7 @@ def run_reference(args) -> None:
                                    f"replica per step (the reference has no CPU implementation and cannot be built "
                                    f"here; the "
                                    f"oracle restates its shader math, here its "
-                                   f"{'FP32 build' if args.oracle_variant == 'f32' else 'FP64 checker'})"},
+                                   f"{'FP32 build' if args.oracle_variant == 'f32' else 'FP64 oracle'})"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -1322,7 +1322,7 @@ def main() -> None:
     ap.add_argument("--ws-epochs", type=int, default=3)
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--oracle-variant", choices=("f32", "f64"), default="f32",
-                    help="reference arm: the oracle's FP32 build (default) or the FP64 checker")
+                    help="reference arm: the oracle's FP32 build (default) or the FP64 oracle")
     ap.add_argument("--search-levels", type=int, default=1,
                     help="finer search grids than the scene's that the search tuner may try")
     ap.add_argument("--graph-mode", type=int, default=2, choices=(0, 1, 2),

@@ -1,6 +1,6 @@
 """FP64 restatement of the warm-start network -- test infrastructure only.
 
-This module is the checker for the CUDA forward, backward and Adam kernels of the
+This module is the oracle for the CUDA forward, backward and Adam kernels of the
 learned warm start (apbf_gb300/csrc/mlp.cu).  Only tests, the smoke check and the
 benchmark's baseline leg may import it; the product never does.  The network has
 no counterpart in the reference (cg-tuwien/APBF solves from lambda = 0 in every

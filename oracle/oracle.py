@@ -1,13 +1,13 @@
 """ctypes wrapper of the oracle library (oracle/_build/libapbf_oracle.so).
 
 TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the CPU
-baseline legs of bench.py as the checker / timed CPU restatement.  The product
+baseline legs of bench.py as the reference for parity and the timed CPU restatement.  The product
 (apbf_gb300) never imports this module.
 
 APBF_ORACLE_VARIANT=f32 in the environment (read when the library is first
 loaded) selects libapbf_oracle_f32.so instead: the same code with the kernels and
 the incompressibility passes in FP32, timed as a CPU baseline and checked against
-the FP64 library, never used as the checker.
+the FP64 library, never used as the parity reference.
 
 States are dicts of numpy arrays in the layout of apbf_gb300.scenes.make_state.
 Every function copies its inputs, so callers keep their arrays.

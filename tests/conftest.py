@@ -29,7 +29,7 @@ def orc():
 
 @pytest.fixture(scope="session")
 def native_lib():
-    """The CUDA library; on a GPU machine it must exist (built by __graft_entry__.build())."""
+    """The CUDA library; on a machine with a GPU it must exist (built by __graft_entry__.build())."""
     from apbf_gb300 import build as b
 
     b.build()

@@ -1,5 +1,5 @@
 """The FP64 warm-start network of the oracle against finite differences and
-torch's bfloat16 rounding (CPU only): the checker of the CUDA training kernels is
+torch's bfloat16 rounding (CPU only): the oracle of the CUDA training kernels is
 itself checked here."""
 import numpy as np
 import pytest
