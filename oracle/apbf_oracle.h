@@ -3,7 +3,7 @@
  *
  * TEST INFRASTRUCTURE ONLY.  This library is the correctness oracle for the CUDA
  * implementation in apbf_gb300/.  Only tests/, __graft_entry__.smoke() and the
- * cpu_baseline / reference legs of bench.py may load it, and only as a checker or
+ * cpu_baseline / reference legs of bench.py may load it, and only as the parity reference or
  * as the timed CPU baseline; the product path never calls it.
  *
  * The reference runs its physics only as GLSL compute shaders through Vulkan; it

@@ -1,5 +1,5 @@
 """The FP32 build of the oracle (libapbf_oracle_f32.so: kernels and incompressibility
-passes in float, everything else as in the FP64 checker) tracks the FP64 oracle:
+passes in float, everything else as in the FP64 oracle) tracks the FP64 oracle:
 after five substeps of a compressed block in free fall every particle has a partner
 within a thousandth of a radius in the other run.  The FP32 build runs in a child
 process, so that this process keeps the FP64 library."""
