@@ -24,3 +24,16 @@ def test_reference_arm_maps_no_product_library():
     assert line["value"] > 0 and line["cpu_baseline"]["cores"] == os.cpu_count()
     # a bounded sample: 1/8 of the scene's particles per replica
     assert line["config"]["sample_scale"] == 0.125 and line["config"]["sample_particles"] == 16 ** 3
+
+
+def test_samples_scale_with_their_workload():
+    """A bounded sample of a workload has about the requested fraction of its particles
+    (the reference arm and the CPU baseline time such samples)."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    for w in ("dam_break_32k", "water_drop_250k", "water_drop_250k_plain", "waterfall_1m"):
+        full = bench.make_spec(w).n
+        for scale in (1.0 / 8.0, 1.0 / 64.0):
+            n = bench.make_spec(w, scale=scale).n
+            assert 0.5 * scale * full <= n <= 2.0 * scale * full, (w, scale, n, full)
